@@ -1,0 +1,181 @@
+/*
+ * pyturb_gb300 — C-ABI of the GB300 (sm_103a) phase-screen hot path.
+ *
+ * Plain C types only: device buffers are raw pointers (float data, complex
+ * values as interleaved (re, im) float pairs), streams are `void*`
+ * (a cudaStream_t, NULL = the legacy default stream). Every entry point
+ * returns a status code (PT_OK on success) and leaves a message readable
+ * through pt_last_error() on failure. Hot-path calls never allocate: their
+ * scratch lives in a caller-provided workspace whose size the matching
+ * *_workspace_bytes() query returns. Arguments are validated before any
+ * launch, so a bad call returns PT_ERR_ARG and touches no memory.
+ *
+ * Each entry point names the reference (jacotay7/pyturb) interface it
+ * replaces as `path:line`.
+ */
+#ifndef PYTURB_GB300_H
+#define PYTURB_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  PT_OK = 0,
+  PT_ERR_ARG = 1,         /* invalid argument (sizes, NULL pointers, workspace too small) */
+  PT_ERR_CUDA = 2,        /* a CUDA runtime call or kernel launch failed */
+  PT_ERR_UNSUPPORTED = 3  /* valid request outside what this build implements */
+};
+
+/* Library version (major*10000 + minor*100 + patch). */
+int pt_version(void);
+
+/* Message of the last failed call on this host thread ("" if none). */
+const char* pt_last_error(void);
+
+/* Number of kernels this library has launched since load (all threads). */
+uint64_t pt_launch_count(void);
+
+/* ------------------------------------------------------------------ grid plan
+ * An ns x ns FFT grid with pixel_scale dx and n_levels subharmonic levels:
+ * twiddles, the subharmonic sinusoid bases and their grid means. Mirrors the
+ * geometry part of PhaseScreen._build_filters (src/pyturb/fourier.py:174-228).
+ * sh_freq: (n_levels, 3) host FP64 subharmonic frequencies f_p = {-1,0,1} df/3^p.
+ * Allocates its constant tables on the current device; not a hot-path call.
+ */
+typedef struct pt_grid pt_grid;
+
+int pt_grid_create(pt_grid** out, int ns, double pixel_scale, int n_levels,
+                   const double* sh_freq);
+int pt_grid_destroy(pt_grid* grid);
+
+/* Workspace needed by pt_generate / pt_frames / pt_ifft2 on this grid
+ * (largest over the three, for the chunk sizes the library uses). */
+size_t pt_grid_workspace_bytes(const pt_grid* grid, int n_layers);
+
+/* Unnormalised inverse 2-D DFT, numpy.fft.ifft2(x) * ns^2, of `batch`
+ * complex ns x ns images (in and out may alias). The transform under
+ * PhaseScreen.generate (src/pyturb/fourier.py:259) and
+ * Atmosphere._integrate (src/pyturb/atmosphere.py:918). */
+int pt_ifft2(const pt_grid* grid, const float* in, float* out, int batch, void* work,
+             size_t work_bytes, void* stream);
+
+/* PhaseScreen.generate(count) (src/pyturb/fourier.py:233-282): coloured
+ * complex noise x amplitude -> inverse FFT -> real parts are screens
+ * [0, n_fft), imaginary parts screens [n_fft, 2 n_fft) (n_fft = ceil(count/2))
+ * -> plus the 3x3-per-level subharmonic sum minus its screen mean.
+ *   amplitude (ns, ns)      device f32, sqrt(PSD) * df with DC zeroed
+ *   sh_amp    (P, 3, 3)     device f32 (NULL when P = 0)
+ *   noise     (2, n_fft, ns, ns) device f32 normals, or NULL: in-kernel
+ *                           Philox4x32-10 keyed by (seed, call)
+ *   sh_noise  (P, 2, count, 3, 3) device f32, or NULL (Philox)
+ * Output (count, n_out, n_out): the crop window [crop, crop + n_out) of each
+ * screen times `scale`, added to `out` when accumulate != 0 (the L0-group sum
+ * of Atmosphere.sample, src/pyturb/atmosphere.py:1213-1219). */
+int pt_generate(const pt_grid* grid, int count, const float* amplitude, const float* sh_amp,
+                const float* noise, const float* sh_noise, uint64_t seed, uint64_t call,
+                int crop, int n_out, float scale, int accumulate, float* out, void* work,
+                size_t work_bytes, void* stream);
+
+/* FourierFlowScreen.reseed (src/pyturb/flow.py:71-94) for L layers at once:
+ *   spectra[l] = (noise[l,0] + i noise[l,1]) * amplitude[l]   (L, ns, ns) complex
+ *   sh_coef[p, l] = (sh_noise[l,p,0] + i sh_noise[l,p,1]) * sh_amp[p, l]  (P, L, 3, 3) complex
+ * noise / sh_noise NULL draws Philox normals keyed by seeds[l] (host array). */
+int pt_layers_fill(const pt_grid* grid, int n_layers, const float* amplitude,
+                   const float* sh_amp, const float* noise, const float* sh_noise,
+                   const uint64_t* seeds, float* spectra, float* sh_coef, void* stream);
+
+/* Frozen-flow readout of the spectral engine. Frame f is
+ *   Re ifft2( sum_l S_l . exp(2 pi i (f_x sx[f,l] + f_y sy[f,l])) ) * ns^2
+ *   + Re(sum_p basis^T shifted_p basis) - mean, cropped, times scale,
+ * i.e. Atmosphere._integrate (src/pyturb/atmosphere.py:882-938), one frame
+ * per (t, direction) pair of Atmosphere._integrate_dirs (940-998) and
+ * FourierFlowScreen.translate (src/pyturb/flow.py:96-129) for L = 1.
+ *   spectra (L, ns, ns) complex, sh_coef (P, L, 3, 3) complex (device)
+ *   sx, sy  (F, L) host FP64 displacements [m] along axes 0 and 1
+ * per_layer != 0 gives Atmosphere._integrate_lgs's per-layer screens
+ * (src/pyturb/atmosphere.py:1013-1040): F must equal L, sx / sy are (L)
+ * and frame l is layer l alone at shift (sx[l], sy[l]), uncropped. */
+int pt_frames(const pt_grid* grid, int n_layers, const float* spectra, const float* sh_coef,
+              int n_frames, const double* sx, const double* sy, int per_layer, int crop,
+              int n_out, float scale, float* out, void* work, size_t work_bytes, void* stream);
+
+/* Atmosphere._lgs_zoom (src/pyturb/atmosphere.py:1047-1090): separable
+ * T-tap cone zoom of L (ns, ns) layer screens into one (n, n) pupil,
+ * summed over layers, times scale. idx (L, T, n) int32, w (L, T, n) f32. */
+int pt_lgs_zoom(int n_layers, int ns, int n, int n_taps, const int32_t* idx, const float* w,
+                const float* screens, float scale, float* out, void* stream);
+
+/* Atmosphere._boil_step (src/pyturb/atmosphere.py:1092-1126): per-mode AR(1)
+ *   S <- a S + sqrt(1 - a^2) (n0 + i n1) amplitude,  a = exp(-dt / tau)
+ * on the stacked spectra and subharmonic coefficients, in place.
+ * main_tau (L, ns, ns) f32, sh_tau (P, L, 3, 3) f32, amplitude (L, ns, ns),
+ * sh_amp (P, L, 3, 3). noise (2, L, ns, ns) / sh_noise (2, P, L, 3, 3)
+ * device normals, or NULL for Philox keyed by (seed, call). */
+int pt_boil_step(const pt_grid* grid, int n_layers, float* spectra, float* sh_coef,
+                 const float* amplitude, const float* sh_amp, const float* main_tau,
+                 const float* sh_tau, double dt, const float* noise, const float* sh_noise,
+                 uint64_t seed, uint64_t call, void* stream);
+
+/* ------------------------------------------------------------------ extrusion
+ * One Assemat-Wilson row step for a set of ring-buffer screens
+ * (_ExtrudeLayer._extrude_one, src/pyturb/extrude.py:424-430;
+ * InfinitePhaseScreen._extrude_one, src/pyturb/infinite.py:274-281):
+ *   buf[s, head] = A_g . buf[s, head-m .. head-1] + B_g . (bscale * beta)
+ * with ring rows taken modulo cap. M holds [A_g | B_unit_g] row-major,
+ * shape (G, W, (m+1) W). Jobs are processed in `step` order; the jobs of
+ * one step are independent (distinct screens). */
+typedef struct {
+  int32_t screen;     /* slab of buf: (screen, cap, W) */
+  int32_t group;      /* which [A | B] matrix */
+  int32_t head;       /* physical ring row receiving the new row */
+  int32_t step;       /* sequential step index (non-decreasing over the job list) */
+  float bscale;       /* r0^(-5/6) of the screen */
+  int32_t pad;
+  uint64_t key;       /* Philox key for beta when noise == NULL */
+  uint64_t row;       /* virtual row index (Philox counter) */
+  int64_t noise_off;  /* element offset of this row's W normals in `noise` */
+} pt_extrude_job;
+
+size_t pt_extrude_workspace_bytes(int W, int m, int max_jobs_per_step);
+
+int pt_extrude_rows(int W, int m, int cap, int n_groups, const float* M, float* buf,
+                    int n_jobs, const pt_extrude_job* jobs, const float* noise, void* work,
+                    size_t work_bytes, void* stream);
+
+/* Fused multi-layer rotated sub-pixel readout of the extrusion engine
+ * (ExtrudedAtmosphere._integrate_fused_kernel / _integrate_looped,
+ * src/pyturb/extrude.py:864-915, kernels 91-198): per pupil pixel and layer
+ *   row = along + shift_along, col = perp + W/2 + shift_perp
+ * with along/perp the pupil grid rotated onto the layer's wind axis and
+ * scaled by the LGS magnification; rows clamp to [0, row_max], columns to
+ * [0, W-1]; 2/4/6-tap separable weights; layers summed, times scale.
+ * interp: 0 linear, 1 cubic (Catmull-Rom), 2 Lanczos-3. */
+typedef struct {
+  int32_t screen;       /* slab of buf */
+  int32_t row_max;      /* last readable row, relative to anchor */
+  int32_t anchor_phys;  /* physical ring row of relative row 0 */
+  int32_t pad;
+  double cos_t, sin_t;  /* wind axis */
+  double mag;           /* LGS cone magnification (1 = none) */
+  double shift_along;   /* travel + off_along - anchor (rows) */
+  double shift_perp;    /* off_perp (columns) */
+} pt_readout_layer;
+
+int pt_readout(int n, int W, int cap, int interp, int n_layers, const pt_readout_layer* layers,
+               const float* buf, float scale, float* out, void* stream);
+
+/* InfinitePhaseScreen._sample (src/pyturb/infinite.py:308-341): row-only
+ * interpolation of an (n, n) window of one ring-buffer screen at relative
+ * row position shift (rows clamp to [0, row_max], ring rows modulo cap). */
+int pt_rows_sample(int n, int cap, int interp, int anchor_phys, int row_max, double shift,
+                   const float* buf, float* out, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PYTURB_GB300_H */

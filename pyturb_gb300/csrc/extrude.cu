@@ -1,0 +1,390 @@
+// Assemat-Wilson extrusion and the fused multi-layer readout on the GB300.
+//
+// Ring buffers: screen s occupies buf[s] = (cap, W) floats; virtual row v of
+// the screen lives in physical row v mod cap, so advancing the wind moves an
+// index instead of compacting rows.
+//
+// Extrusion step: every screen needing a row this step contributes one
+// column X_j = [stencil rows (m W values) ; bscale_j * beta_j (W values)] and
+// the new rows are the "TN" product out[j][r] = sum_k M_g[r][k] X_j[k] with
+// M_g = [A_g | B_unit_g] (W x (m+1) W). A split-K SIMT GEMM with a
+// deterministic reduction writes them straight into the ring.
+//
+// Readout: one thread per pupil pixel; per layer the rotated, magnified,
+// shifted sample position is formed in 64-bit fixed point (exact up to
+// 2^-40 px whatever the travel), the 2/4/6 separable taps gather from the
+// ring and the layers are summed.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <map>
+#include <vector>
+
+#include "common.cuh"
+
+namespace pt {
+uint64_t* launch_counter();
+static inline void count_launch_e(int k = 1) {
+  __atomic_add_fetch(launch_counter(), (uint64_t)k, __ATOMIC_RELAXED);
+}
+
+constexpr int kTM = 64;   // output rows per CTA
+constexpr int kTJ = 32;   // jobs (columns) per CTA
+constexpr int kTK = 32;   // K step
+constexpr int kMaxSplit = 16;
+
+struct GatherJob {
+  int screen, head;
+  float bscale;
+  uint64_t key, row;
+  long long noise_off;
+};
+// Jobs travel inside the launch parameters (no pageable copy, no sync).
+constexpr int kJobsPerLaunch = 192;
+struct JobParams {
+  GatherJob j[kJobsPerLaunch];
+};
+
+// X[j][k], k < mW: stencil rows; k >= mW: bscale * beta
+__global__ void k_extrude_gather(int W, int m, int cap, const float* __restrict__ buf,
+                                 const JobParams jobs, int J, const float* __restrict__ noise,
+                                 float* __restrict__ X) {
+  const int j = blockIdx.y;
+  if (j >= J) return;
+  const GatherJob& jb = jobs.j[j];
+  const int K = (m + 1) * W;
+  const float* slab = buf + (size_t)jb.screen * cap * W;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < K; k += gridDim.x * blockDim.x) {
+    float v;
+    if (k < m * W) {
+      const int r = k / W, c = k % W;
+      int phys = jb.head - m + r;
+      if (phys < 0) phys += cap;
+      v = slab[(size_t)phys * W + c];
+    } else {
+      const int c = k - m * W;
+      float z;
+      if (noise) {
+        z = noise[jb.noise_off + c];
+      } else {
+        // one Philox call yields a pair: even/odd columns share it
+        const float2 p = philox_cnormal(jb.key, (uint64_t)(c >> 1), jb.row, kDomainExtrude);
+        z = (c & 1) ? p.y : p.x;
+      }
+      v = jb.bscale * z;
+    }
+    X[(size_t)j * K + k] = v;
+  }
+}
+
+// partial[z][j][r] = sum_{k in slice z} M[r][k] X[j][k]
+__global__ void __launch_bounds__(256)
+k_extrude_gemm(int W, int K, int J, int kslice, const float* __restrict__ M,
+               const float* __restrict__ X, float* __restrict__ partial) {
+  __shared__ float sA[kTM][kTK + 1];
+  __shared__ float sX[kTJ][kTK + 1];
+  const int r0 = blockIdx.x * kTM;
+  const int j0 = blockIdx.y * kTJ;
+  const int kb = blockIdx.z * kslice;
+  const int ke = min(K, kb + kslice);
+  const int tid = threadIdx.x;
+  const int tr = tid / 16;  // 16 row groups of 4
+  const int tj = tid % 16;  // 16 job groups of 2
+  float acc[4][2] = {};
+  for (int k0 = kb; k0 < ke; k0 += kTK) {
+    for (int i = tid; i < kTM * kTK; i += 256) {
+      const int rr = i / kTK, kk = i % kTK;
+      const int r = r0 + rr, k = k0 + kk;
+      sA[rr][kk] = (r < W && k < ke) ? M[(size_t)r * K + k] : 0.f;
+    }
+    for (int i = tid; i < kTJ * kTK; i += 256) {
+      const int jj = i / kTK, kk = i % kTK;
+      const int j = j0 + jj, k = k0 + kk;
+      sX[jj][kk] = (j < J && k < ke) ? X[(size_t)j * K + k] : 0.f;
+    }
+    __syncthreads();
+#pragma unroll 8
+    for (int kk = 0; kk < kTK; ++kk) {
+      float a[4], x[2];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) a[u] = sA[tr * 4 + u][kk];
+#pragma unroll
+      for (int v = 0; v < 2; ++v) x[v] = sX[tj * 2 + v][kk];
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 2; ++v) acc[u][v] = fmaf(a[u], x[v], acc[u][v]);
+    }
+    __syncthreads();
+  }
+  float* pz = partial + (size_t)blockIdx.z * J * W;
+#pragma unroll
+  for (int u = 0; u < 4; ++u)
+#pragma unroll
+    for (int v = 0; v < 2; ++v) {
+      const int r = r0 + tr * 4 + u, j = j0 + tj * 2 + v;
+      if (r < W && j < J) pz[(size_t)j * W + r] = acc[u][v];
+    }
+}
+
+__global__ void k_extrude_reduce(int W, int J, int cap, int nsplit, const float* __restrict__ partial,
+                                 const JobParams jobs, float* __restrict__ buf) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y;
+  if (r >= W || j >= J) return;
+  float s = 0.f;
+  for (int z = 0; z < nsplit; ++z) s += partial[((size_t)z * J + j) * W + r];
+  const GatherJob& jb = jobs.j[j];
+  buf[((size_t)jb.screen * cap + jb.head) * W + r] = s;
+}
+
+// ---------------------------------------------------------------- readout
+struct RLayer {
+  int screen, row_max, anchor_phys;
+  long long ca, sa, ra, rp;  // fixed-point (2^-40) constants
+};
+constexpr int kMaxReadoutLayers = 64;
+struct RLayers {
+  RLayer l[kMaxReadoutLayers];
+};
+
+constexpr int kFix = 40;
+
+__device__ __forceinline__ void split_fixed(long long v, int& i, float& f) {
+  i = (int)(v >> kFix);
+  f = (float)(v & ((1ll << kFix) - 1)) * (1.0f / 1099511627776.0f);
+}
+
+__device__ __forceinline__ float sincpi_f(float x) {
+  if (x == 0.f) return 1.f;
+  return sinpif(x) / (3.14159265358979323846f * x);
+}
+
+template <int T>
+__device__ __forceinline__ void taps(float t, float* w) {
+  if (T == 2) {
+    w[0] = 1.f - t;
+    w[1] = t;
+  } else if (T == 4) {
+    const float t2 = t * t, t3 = t2 * t;
+    w[0] = 0.5f * (-t + 2.f * t2 - t3);
+    w[1] = 0.5f * (2.f - 5.f * t2 + 3.f * t3);
+    w[2] = 0.5f * (t + 4.f * t2 - 3.f * t3);
+    w[3] = 0.5f * (-t2 + t3);
+  } else {
+    float tot = 0.f;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+      const float x = t - (float)(k - 2);
+      w[k] = sincpi_f(x) * sincpi_f(x * (1.0f / 3.0f));
+      tot += w[k];
+    }
+    const float inv = 1.f / tot;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) w[k] *= inv;
+  }
+}
+
+template <int T>
+__global__ void __launch_bounds__(256)
+k_readout(int n, int W, int cap, int L, RLayers P, const float* __restrict__ buf, float scale,
+          float* __restrict__ out) {
+  const int y = blockIdx.x * blockDim.x + threadIdx.x;
+  const int x = blockIdx.y;
+  if (y >= n) return;
+  const int off0 = (T == 2) ? 0 : (T == 4 ? -1 : -2);
+  const long long kx = 2ll * x - (n - 1), ky = 2ll * y - (n - 1);
+  float acc = 0.f;
+  for (int l = 0; l < L; ++l) {
+    const RLayer p = P.l[l];
+    const long long rowf = kx * p.ca + ky * p.sa + p.ra;
+    const long long colf = -kx * p.sa + ky * p.ca + p.rp;
+    int r0, c0;
+    float fr, fc;
+    split_fixed(rowf, r0, fr);
+    split_fixed(colf, c0, fc);
+    float wr[T], wc[T];
+    taps<T>(fr, wr);
+    taps<T>(fc, wc);
+    const float* slab = buf + (size_t)p.screen * cap * W;
+    int cc[T];
+#pragma unroll
+    for (int b = 0; b < T; ++b) cc[b] = min(max(c0 + off0 + b, 0), W - 1);
+    float val = 0.f;
+#pragma unroll
+    for (int a = 0; a < T; ++a) {
+      int rr = min(max(r0 + off0 + a, 0), p.row_max);
+      int phys = p.anchor_phys + rr;
+      if (phys >= cap) phys -= cap;
+      const float* row = slab + (size_t)phys * W;
+      float rs = 0.f;
+#pragma unroll
+      for (int b = 0; b < T; ++b) rs = fmaf(wc[b], __ldg(row + cc[b]), rs);
+      val = fmaf(wr[a], rs, val);
+    }
+    acc += val;
+  }
+  out[(size_t)x * n + y] = scale * acc;
+}
+
+template <int T>
+__global__ void k_rows_sample(int n, int cap, int anchor_phys, int row_max, int i0, float t,
+                              const float* __restrict__ buf, float* __restrict__ out) {
+  const int y = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.y;
+  if (y >= n) return;
+  const int off0 = (T == 2) ? 0 : (T == 4 ? -1 : -2);
+  float w[T];
+  taps<T>(t, w);
+  float v = 0.f;
+#pragma unroll
+  for (int a = 0; a < T; ++a) {
+    const int rr = min(max(i0 + i + off0 + a, 0), row_max);
+    int phys = anchor_phys + rr;
+    if (phys >= cap) phys -= cap;
+    v = fmaf(w[a], buf[(size_t)phys * n + y], v);
+  }
+  out[(size_t)i * n + y] = v;
+}
+
+static inline size_t al256(size_t x) { return (x + 255) & ~size_t(255); }
+
+static int split_for(int W, int J, int K) {
+  const int ctas = ((W + kTM - 1) / kTM) * ((J + kTJ - 1) / kTJ);
+  int s = std::max(1, std::min(kMaxSplit, (2 * 152 + ctas - 1) / ctas));
+  // keep each slice at least 4 K-steps long
+  s = std::max(1, std::min(s, K / (4 * kTK)));
+  return s;
+}
+
+}  // namespace pt
+
+using namespace pt;
+
+extern "C" size_t pt_extrude_workspace_bytes(int W, int m, int max_jobs) {
+  if (W < 1 || m < 1 || max_jobs < 1) return 0;
+  const size_t K = (size_t)(m + 1) * W;
+  const size_t J = (size_t)std::min(max_jobs, kJobsPerLaunch);
+  return al256(J * K * sizeof(float)) + al256((size_t)kMaxSplit * J * W * sizeof(float));
+}
+
+extern "C" int pt_extrude_rows(int W, int m, int cap, int G, const float* M, float* buf,
+                               int n_jobs, const pt_extrude_job* jobs, const float* noise,
+                               void* work, size_t work_bytes, void* stream) {
+  if (W < 1 || m < 1 || cap < m + 1 || G < 1) return fail(PT_ERR_ARG, "pt_extrude_rows: bad sizes");
+  if (!M || !buf || (n_jobs > 0 && !jobs)) return fail(PT_ERR_ARG, "pt_extrude_rows: NULL pointer");
+  if (n_jobs == 0) return PT_OK;
+  // group jobs by (step, group), validating order and ranges
+  int max_j = 0;
+  {
+    int cur = 1, prev_step = jobs[0].step;
+    for (int i = 0; i < n_jobs; ++i) {
+      const pt_extrude_job& jb = jobs[i];
+      if (jb.group < 0 || jb.group >= G) return fail(PT_ERR_ARG, "pt_extrude_rows: job group out of range");
+      if (jb.head < 0 || jb.head >= cap) return fail(PT_ERR_ARG, "pt_extrude_rows: job head out of range");
+      if (jb.screen < 0) return fail(PT_ERR_ARG, "pt_extrude_rows: negative screen index");
+      if (i > 0) {
+        if (jb.step < prev_step) return fail(PT_ERR_ARG, "pt_extrude_rows: jobs must be sorted by step");
+        cur = (jb.step == prev_step) ? cur + 1 : 1;
+      }
+      prev_step = jb.step;
+      max_j = std::max(max_j, cur);
+    }
+  }
+  const size_t need = pt_extrude_workspace_bytes(W, m, max_j);
+  if (!work || work_bytes < need) return fail(PT_ERR_ARG, "pt_extrude_rows: workspace too small");
+  const int K = (m + 1) * W;
+  const int jcap = std::min(max_j, kJobsPerLaunch);
+  float* X = (float*)work;
+  float* partial = (float*)((char*)work + al256((size_t)jcap * K * sizeof(float)));
+  cudaStream_t s = (cudaStream_t)stream;
+  std::vector<GatherJob> hj;
+  int i = 0;
+  while (i < n_jobs) {
+    int e = i;
+    while (e < n_jobs && jobs[e].step == jobs[i].step) ++e;
+    // within one step, one launch chain per group
+    std::map<int, std::vector<int>> by_group;
+    for (int q = i; q < e; ++q) by_group[jobs[q].group].push_back(q);
+    for (auto& kv : by_group) {
+      hj.clear();
+      for (int q : kv.second) {
+        const pt_extrude_job& jb = jobs[q];
+        hj.push_back(GatherJob{jb.screen, jb.head, jb.bscale, jb.key, jb.row, (long long)jb.noise_off});
+      }
+      for (size_t b = 0; b < hj.size(); b += kJobsPerLaunch) {
+        const int J = (int)std::min<size_t>(kJobsPerLaunch, hj.size() - b);
+        JobParams jp;
+        for (int q = 0; q < J; ++q) jp.j[q] = hj[b + q];
+        k_extrude_gather<<<dim3(std::min((K + 255) / 256, 64), J), 256, 0, s>>>(W, m, cap, buf, jp,
+                                                                              J, noise, X);
+        const int nsplit = split_for(W, J, K);
+        const int kslice = ((K + nsplit - 1) / nsplit + kTK - 1) / kTK * kTK;
+        const int nz = (K + kslice - 1) / kslice;
+        const float* Mg = M + (size_t)kv.first * W * K;
+        k_extrude_gemm<<<dim3((W + kTM - 1) / kTM, (J + kTJ - 1) / kTJ, nz), 256, 0, s>>>(
+            W, K, J, kslice, Mg, X, partial);
+        k_extrude_reduce<<<dim3((W + 255) / 256, J), 256, 0, s>>>(W, J, cap, nz, partial, jp, buf);
+        count_launch_e(3);
+        if (int rc = check_launch("pt_extrude_rows")) return rc;
+      }
+    }
+    i = e;
+  }
+  return PT_OK;
+}
+
+extern "C" int pt_readout(int n, int W, int cap, int interp, int L, const pt_readout_layer* layers,
+                          const float* buf, float scale, float* out, void* stream) {
+  if (n < 1 || W < 1 || cap < 1 || L < 1) return fail(PT_ERR_ARG, "pt_readout: bad sizes");
+  if (L > kMaxReadoutLayers) return fail(PT_ERR_UNSUPPORTED, "pt_readout: at most 64 layers");
+  if (n > 8192) return fail(PT_ERR_UNSUPPORTED, "pt_readout: n must be <= 8192");
+  if (!layers || !buf || !out) return fail(PT_ERR_ARG, "pt_readout: NULL pointer");
+  if (interp < 0 || interp > 2) return fail(PT_ERR_ARG, "pt_readout: interp must be 0, 1 or 2");
+  RLayers P{};
+  const double one = (double)(1ll << kFix);
+  for (int l = 0; l < L; ++l) {
+    const pt_readout_layer& q = layers[l];
+    if (q.row_max < 0 || q.anchor_phys < 0 || q.anchor_phys >= cap || q.screen < 0)
+      return fail(PT_ERR_ARG, "pt_readout: bad layer ring parameters");
+    if (q.row_max >= cap) return fail(PT_ERR_ARG, "pt_readout: row_max beyond the ring");
+    const double lim = 4.0e6;
+    if (!(std::fabs(q.shift_along) < lim) || !(std::fabs(q.shift_perp) + W < lim) ||
+        !(std::fabs(q.mag) <= 4.0))
+      return fail(PT_ERR_ARG, "pt_readout: shift or magnification out of range");
+    P.l[l].screen = q.screen;
+    P.l[l].row_max = q.row_max;
+    P.l[l].anchor_phys = q.anchor_phys;
+    P.l[l].ca = std::llround(q.mag * q.cos_t * 0.5 * one);
+    P.l[l].sa = std::llround(q.mag * q.sin_t * 0.5 * one);
+    P.l[l].ra = std::llround(q.shift_along * one);
+    P.l[l].rp = std::llround((W / 2.0 + q.shift_perp) * one);
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  dim3 grid((n + 255) / 256, n);
+  if (interp == 0) k_readout<2><<<grid, 256, 0, s>>>(n, W, cap, L, P, buf, scale, out);
+  else if (interp == 1) k_readout<4><<<grid, 256, 0, s>>>(n, W, cap, L, P, buf, scale, out);
+  else k_readout<6><<<grid, 256, 0, s>>>(n, W, cap, L, P, buf, scale, out);
+  count_launch_e();
+  return check_launch("pt_readout");
+}
+
+extern "C" int pt_rows_sample(int n, int cap, int interp, int anchor_phys, int row_max,
+                              double shift, const float* buf, float* out, void* stream) {
+  if (n < 1 || cap < 1 || row_max < 0 || row_max >= cap || anchor_phys < 0 || anchor_phys >= cap)
+    return fail(PT_ERR_ARG, "pt_rows_sample: bad sizes");
+  if (!buf || !out) return fail(PT_ERR_ARG, "pt_rows_sample: NULL pointer");
+  if (interp < 0 || interp > 2) return fail(PT_ERR_ARG, "pt_rows_sample: interp must be 0, 1 or 2");
+  if (!(std::fabs(shift) < 1e9)) return fail(PT_ERR_ARG, "pt_rows_sample: shift out of range");
+  const double fl = std::floor(shift);
+  const int i0 = (int)fl;
+  const float t = (float)(shift - fl);
+  cudaStream_t s = (cudaStream_t)stream;
+  dim3 grid((n + 255) / 256, n);
+  if (interp == 0) k_rows_sample<2><<<grid, 256, 0, s>>>(n, cap, anchor_phys, row_max, i0, t, buf, out);
+  else if (interp == 1) k_rows_sample<4><<<grid, 256, 0, s>>>(n, cap, anchor_phys, row_max, i0, t, buf, out);
+  else k_rows_sample<6><<<grid, 256, 0, s>>>(n, cap, anchor_phys, row_max, i0, t, buf, out);
+  count_launch_e();
+  return check_launch("pt_rows_sample");
+}

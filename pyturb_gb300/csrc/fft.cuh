@@ -1,0 +1,232 @@
+// Shared-memory Stockham autosort FFT (mixed radix 8/4/2/3/5/7 plus a
+// direct-sum stage for any larger prime factor), inverse sign, unnormalised:
+//   X[k] = sum_j x[j] exp(+2 pi i j k / n)
+// which is numpy.fft.ifft(x) * n. Every transform of a pass lives in shared
+// memory; passes run along rows (contiguous) or along columns (tiles of C
+// columns), so a 2-D transform is two passes over HBM/L2.
+#pragma once
+
+#include "common.cuh"
+
+namespace pt {
+
+constexpr int kMaxStages = 24;
+
+struct FftDesc {
+  int n;
+  int nstages;
+  int radix[kMaxStages];
+};
+
+// Factor n into the stage radices used by the Stockham passes. Radix 8
+// first keeps the stage count low; leftover prime factors > 7 become a
+// single direct-sum stage each.
+inline FftDesc make_fft_desc(int n) {
+  FftDesc d{};
+  d.n = n;
+  int m = n, s = 0;
+  const int pref[] = {8, 4, 2, 3, 5, 7};
+  for (int r : pref) {
+    while (m % r == 0 && s < kMaxStages) {
+      d.radix[s++] = r;
+      m /= r;
+    }
+  }
+  for (int p = 11; m > 1 && s < kMaxStages; p += 2) {
+    while (m % p == 0 && s < kMaxStages) {
+      d.radix[s++] = p;
+      m /= p;
+    }
+    if ((long long)p * p > m && m > 1) {
+      d.radix[s++] = m;
+      m = 1;
+    }
+  }
+  d.nstages = s;
+  return d;
+}
+
+// ------------------------------------------------------------------ butterflies
+// In-register radix-R inverse DFTs, v[q] <- sum_r v[r] exp(+2 pi i q r / R).
+__device__ __forceinline__ void bfly2(float2* v) {
+  float2 a = v[0], b = v[1];
+  v[0] = cadd(a, b);
+  v[1] = csub(a, b);
+}
+
+__device__ __forceinline__ void bfly4(float2* v) {
+  float2 a0 = cadd(v[0], v[2]), a1 = csub(v[0], v[2]);
+  float2 b0 = cadd(v[1], v[3]), b1 = cmul_i(csub(v[1], v[3]));
+  v[0] = cadd(a0, b0);
+  v[2] = csub(a0, b0);
+  v[1] = cadd(a1, b1);
+  v[3] = csub(a1, b1);
+}
+
+__device__ __forceinline__ void bfly8(float2* v) {
+  const float h = 0.70710678118654752440f;
+  // radix-2 over pairs (r, r+4)
+  float2 a[4], b[4];
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    a[r] = cadd(v[r], v[r + 4]);
+    b[r] = csub(v[r], v[r + 4]);
+  }
+  // twiddle b[r] by w8^r, w8 = exp(+i pi/4)
+  b[1] = make_float2(h * (b[1].x - b[1].y), h * (b[1].x + b[1].y));
+  b[2] = cmul_i(b[2]);
+  b[3] = make_float2(-h * (b[3].x + b[3].y), h * (b[3].x - b[3].y));
+  bfly4(a);
+  bfly4(b);
+  // outputs: even q from a, odd q from b
+  v[0] = a[0];
+  v[2] = a[1];
+  v[4] = a[2];
+  v[6] = a[3];
+  v[1] = b[0];
+  v[3] = b[1];
+  v[5] = b[2];
+  v[7] = b[3];
+}
+
+__device__ __forceinline__ void bfly3(float2* v) {
+  const float c1 = -0.5f, s1 = 0.86602540378443864676f;  // exp(+2 pi i/3)
+  float2 t = cadd(v[1], v[2]);
+  float2 d = csub(v[1], v[2]);
+  float2 m = make_float2(v[0].x + c1 * t.x, v[0].y + c1 * t.y);
+  float2 r = make_float2(-s1 * d.y, s1 * d.x);  // i*s1*d
+  v[0] = cadd(v[0], t);
+  v[1] = cadd(m, r);
+  v[2] = csub(m, r);
+}
+
+__device__ __forceinline__ void bfly5(float2* v) {
+  const float c1 = 0.30901699437494742410f, c2 = -0.80901699437494742410f;
+  const float s1 = 0.95105651629515357212f, s2 = 0.58778525229247312917f;
+  float2 t1 = cadd(v[1], v[4]), d1 = csub(v[1], v[4]);
+  float2 t2 = cadd(v[2], v[3]), d2 = csub(v[2], v[3]);
+  float2 m1 = make_float2(v[0].x + c1 * t1.x + c2 * t2.x, v[0].y + c1 * t1.y + c2 * t2.y);
+  float2 m2 = make_float2(v[0].x + c2 * t1.x + c1 * t2.x, v[0].y + c2 * t1.y + c1 * t2.y);
+  // i*(s1 d1 + s2 d2) and i*(s2 d1 - s1 d2)
+  float2 r1 = make_float2(-(s1 * d1.y + s2 * d2.y), s1 * d1.x + s2 * d2.x);
+  float2 r2 = make_float2(-(s2 * d1.y - s1 * d2.y), s2 * d1.x - s1 * d2.x);
+  v[0] = cadd(v[0], cadd(t1, t2));
+  v[1] = cadd(m1, r1);
+  v[4] = csub(m1, r1);
+  v[2] = cadd(m2, r2);
+  v[3] = csub(m2, r2);
+}
+
+// Generic small radix (7): direct sum with the transform's own twiddle table.
+template <int R>
+__device__ __forceinline__ void bfly_direct(float2* v, const float2* tw, int n) {
+  float2 o[R];
+  const int step = n / R;
+#pragma unroll
+  for (int q = 0; q < R; ++q) {
+    float2 acc = v[0];
+#pragma unroll
+    for (int r = 1; r < R; ++r) acc = cfma(v[r], tw[((q * r) % R) * step], acc);
+    o[q] = acc;
+  }
+#pragma unroll
+  for (int q = 0; q < R; ++q) v[q] = o[q];
+}
+
+// One Stockham stage with a compile-time radix. Work items are (vector,
+// butterfly) pairs; `vfast` selects whether consecutive threads walk the
+// vector index (column tiles) or the butterfly index (rows).
+template <int R>
+__device__ __forceinline__ void stage_r(const float2* __restrict__ a, float2* __restrict__ b,
+                                        const float2* __restrict__ tw, int n, int Ns, int nvec,
+                                        int vs, int es, bool vfast) {
+  const int nb = n / R;
+  const int total = nb * nvec;
+  const int twstep = n / (Ns * R);
+  for (int t = threadIdx.x; t < total; t += blockDim.x) {
+    int v, j;
+    if (vfast) {
+      v = t % nvec;
+      j = t / nvec;
+    } else {
+      j = t % nb;
+      v = t / nb;
+    }
+    const float2* src = a + v * vs;
+    float2* dst = b + v * vs;
+    const int jm = j % Ns;
+    float2 x[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) x[r] = src[(j + r * nb) * es];
+    if (Ns > 1) {
+#pragma unroll
+      for (int r = 1; r < R; ++r) x[r] = cmul(x[r], tw[r * jm * twstep]);
+    }
+    if (R == 2) bfly2(x);
+    else if (R == 4) bfly4(x);
+    else if (R == 8) bfly8(x);
+    else if (R == 3) bfly3(x);
+    else if (R == 5) bfly5(x);
+    else bfly_direct<R>(x, tw, n);
+    const int idxD = (j / Ns) * Ns * R + jm;
+#pragma unroll
+    for (int q = 0; q < R; ++q) dst[(idxD + q * Ns) * es] = x[q];
+  }
+}
+
+// Direct-sum stage for a large prime radix: every output is its own
+// R-term sum, so the work items are (vector, butterfly, output) triples.
+__device__ __forceinline__ void stage_generic(const float2* __restrict__ a, float2* __restrict__ b,
+                                              const float2* __restrict__ tw, int n, int R, int Ns,
+                                              int nvec, int vs, int es) {
+  const int nb = n / R;
+  const long total = (long)nb * R * nvec;
+  const int twstep = n / (Ns * R);
+  for (long t = threadIdx.x; t < total; t += blockDim.x) {
+    const int v = (int)(t % nvec);
+    const long rest = t / nvec;
+    const int q = (int)(rest % R);
+    const int j = (int)(rest / R);
+    const float2* src = a + v * vs;
+    const int jm = j % Ns;
+    // exponent of input r: r * (jm * twstep + q * n / R)  (mod n)
+    const int base = jm * twstep + q * (n / R);
+    float2 acc = make_float2(0.f, 0.f);
+    int e = 0;
+    for (int r = 0; r < R; ++r) {
+      acc = cfma(src[(j + r * nb) * es], tw[e], acc);
+      e += base;
+      if (e >= n) e -= n;
+    }
+    const int idxD = (j / Ns) * Ns * R + jm;
+    b[v * vs + (idxD + q * Ns) * es] = acc;
+  }
+}
+
+// Run all stages on `nvec` vectors held in shared memory. Element e of vector
+// v sits at buf[v * vs + e * es]. Returns the buffer holding the result
+// (a or b). Ends with __syncthreads().
+__device__ inline float2* fft_smem(float2* a, float2* b, const FftDesc& d, const float2* tw,
+                                   int nvec, int vs, int es, bool vfast) {
+  int Ns = 1;
+  for (int s = 0; s < d.nstages; ++s) {
+    const int R = d.radix[s];
+    switch (R) {
+      case 2: stage_r<2>(a, b, tw, d.n, Ns, nvec, vs, es, vfast); break;
+      case 3: stage_r<3>(a, b, tw, d.n, Ns, nvec, vs, es, vfast); break;
+      case 4: stage_r<4>(a, b, tw, d.n, Ns, nvec, vs, es, vfast); break;
+      case 5: stage_r<5>(a, b, tw, d.n, Ns, nvec, vs, es, vfast); break;
+      case 7: stage_r<7>(a, b, tw, d.n, Ns, nvec, vs, es, vfast); break;
+      case 8: stage_r<8>(a, b, tw, d.n, Ns, nvec, vs, es, vfast); break;
+      default: stage_generic(a, b, tw, d.n, R, Ns, nvec, vs, es); break;
+    }
+    __syncthreads();
+    float2* t = a;
+    a = b;
+    b = t;
+    Ns *= R;
+  }
+  return a;
+}
+
+}  // namespace pt

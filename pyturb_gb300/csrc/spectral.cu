@@ -1,0 +1,860 @@
+// Spectral synthesis on the GB300: PhaseScreen.generate, the frozen-flow
+// frame readout of the spectral engine, per-layer LGS screens, the LGS cone
+// zoom and spectral boiling.
+//
+// A 2-D inverse transform is two shared-memory passes:
+//   pass 1 (rows, axis 1): a producer writes one complex row into shared
+//     memory (coloured noise, or the phasor-weighted layer sum), the row is
+//     transformed and written to the workspace;
+//   pass 2 (columns, axis 0): tiles of C columns are transformed and the
+//     epilogue writes the real/imaginary parts as two real screens with the
+//     subharmonic low-frequency sum added, cropped and scaled.
+// Two real outputs share one complex transform: generate() uses the
+// reference's own Re/Im pairing, frames are paired through their
+// Hermitian parts, H = (X(k) + conj X(-k)) / 2, so Re ifft2(X1) + i Re
+// ifft2(X2) = ifft2(H1 + i H2).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "common.cuh"
+#include "fft.cuh"
+
+namespace pt {
+uint64_t* launch_counter();
+}
+
+struct pt_grid {
+  int ns;
+  double dx;
+  int P;
+  pt::FftDesc desc;
+  float2* tw;       // (ns) exp(+2 pi i k / ns)
+  float2* basis;    // (P, 3, ns) exp(2 pi i f_p (x - ns/2) dx)
+  double* sh_freq;  // (P, 3)
+  double* beta;     // (P, 3, 2) grid mean of each basis row
+};
+
+namespace pt {
+
+constexpr int kMaxLevels = 16;
+constexpr int kThreads = 256;
+
+static inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+// Number of complex ns x ns images one internal pass batches.
+static inline int image_chunk(int ns) {
+  size_t per = (size_t)ns * ns * sizeof(float2);
+  size_t c = (size_t)(64u << 20) / per;
+  return (int)std::max<size_t>(1, std::min<size_t>(32, c));
+}
+static inline int rows_per_cta(int ns) { return std::max(1, std::min(8, 1024 / ns)); }
+static inline int cols_per_cta(int ns) { return std::max(1, std::min(16, 4096 / ns)); }
+
+static inline void count_launch(int k = 1) {
+  __atomic_add_fetch(launch_counter(), (uint64_t)k, __ATOMIC_RELAXED);
+}
+
+// fftfreq index: k for k < (n+1)/2, else k - n
+__device__ __forceinline__ int signed_freq(int k, int n) { return k < (n + 1) / 2 ? k : k - n; }
+
+// ---------------------------------------------------------------- workspace
+struct SpecWork {
+  float2* img;     // (chunk, ns, ns)
+  float2* coef;    // (2 chunk, P, 9)
+  float* mean;     // (2 chunk)
+  float2* px;      // (2 chunk, J, ns)
+  float2* py;      // (2 chunk, J, ns)
+  size_t bytes;
+};
+
+static SpecWork carve(const pt_grid* g, int L, void* base) {
+  const int ns = g->ns, ch = image_chunk(ns), P = std::max(1, g->P);
+  const int F = 2 * ch;
+  const int J = std::max(1, L);
+  size_t off = 0;
+  SpecWork w{};
+  char* b = (char*)base;
+  auto take = [&](size_t bytes) {
+    char* p = b ? b + off : nullptr;
+    off += align256(bytes);
+    return p;
+  };
+  w.img = (float2*)take((size_t)ch * ns * ns * sizeof(float2));
+  w.coef = (float2*)take((size_t)F * P * 9 * sizeof(float2));
+  w.mean = (float*)take((size_t)F * sizeof(float));
+  w.px = (float2*)take((size_t)F * J * ns * sizeof(float2));
+  w.py = (float2*)take((size_t)F * J * ns * sizeof(float2));
+  w.bytes = off;
+  return w;
+}
+
+// ================================================================ pass 1 producers
+// Generate: X[kx, ky] = (n0 + i n1) * amplitude[kx, ky]
+struct GenRowArgs {
+  const float* amplitude;
+  const float* noise;  // (2, n_fft, ns, ns) or null
+  int n_fft;
+  int img0;            // first FFT index of this chunk
+  uint64_t seed, call;
+};
+
+// Plain complex rows (pt_ifft2) and generate rows share this kernel: `gen`
+// selects the producer. rpc rows per CTA, one transform per row.
+__global__ void __launch_bounds__(kThreads)
+k_rows(FftDesc d, const float2* __restrict__ tw, int rpc, const float2* __restrict__ in,
+       int gen, GenRowArgs ga, float2* __restrict__ work) {
+  extern __shared__ float2 sm[];
+  const int ns = d.n;
+  const int row0 = blockIdx.x * rpc;
+  const int img = blockIdx.y;  // image within this chunk
+  const int vs = ns + 1;
+  float2* bufA = sm;
+  float2* bufB = sm + rpc * vs;
+  float2* stw = sm + 2 * rpc * vs;
+  for (int i = threadIdx.x; i < ns; i += blockDim.x) stw[i] = tw[i];
+  for (int i = threadIdx.x; i < rpc * ns; i += blockDim.x) {
+    const int r = i / ns, ky = i % ns;
+    const int kx = row0 + r;
+    float2 v = make_float2(0.f, 0.f);
+    if (kx < ns) {
+      if (gen) {
+        const size_t e = ((size_t)(ga.img0 + img) * ns + kx) * ns + ky;
+        float2 z;
+        if (ga.noise) {
+          const size_t plane = (size_t)ga.n_fft * ns * ns;
+          z = make_float2(ga.noise[e], ga.noise[plane + e]);
+        } else {
+          z = philox_cnormal(ga.seed, e, ga.call, kDomainScreen);
+        }
+        const float amp = ga.amplitude[(size_t)kx * ns + ky];
+        v = make_float2(z.x * amp, z.y * amp);
+      } else {
+        v = in[((size_t)img * ns + kx) * ns + ky];
+      }
+    }
+    bufA[r * vs + ky] = v;
+  }
+  __syncthreads();
+  float2* res = fft_smem(bufA, bufB, d, stw, rpc, vs, 1, false);
+  for (int i = threadIdx.x; i < rpc * ns; i += blockDim.x) {
+    const int r = i / ns, ky = i % ns;
+    const int kx = row0 + r;
+    if (kx < ns) work[((size_t)img * ns + kx) * ns + ky] = res[r * vs + ky];
+  }
+}
+
+// Frames: CTA = (row pair {kx, ns-kx}, frame pair). Each frame's row is the
+// phasor-weighted layer sum X_f[kx, ky] = sum_j S_l[kx,ky] Px[f,j,kx] Py[f,j,ky]
+// (l = j, or l = the frame's own layer in per-layer mode); the pair is then
+// folded through its Hermitian parts into one complex row per kx.
+struct FrameRowArgs {
+  const float2* spectra;  // (L, ns, ns)
+  const float2* px;       // (F, J, ns) for this chunk
+  const float2* py;       // (F, J, ns)
+  int J, F;               // J = terms per frame (L, or 1 per-layer); F frames in chunk
+  int frame0;             // global index of the chunk's first frame (per-layer: its layer)
+  int per_layer;
+};
+
+__global__ void __launch_bounds__(kThreads)
+k_frame_rows(FftDesc d, const float2* __restrict__ tw, FrameRowArgs a, float2* __restrict__ work) {
+  extern __shared__ float2 sm[];
+  const int ns = d.n;
+  const int rp = blockIdx.x;  // 0 .. ns/2
+  const int pair = blockIdx.y;
+  const int kxa = rp, kxb = (ns - rp) % ns;
+  const int nrows = (kxa == kxb) ? 1 : 2;
+  const int vs = ns + 1;
+  // X rows: [frame 0 row a, frame 0 row b, frame 1 row a, frame 1 row b]
+  float2* X = sm;                // 4 * vs
+  float2* bufA = sm + 4 * vs;    // 2 * vs
+  float2* bufB = bufA + 2 * vs;  // 2 * vs
+  float2* stw = bufB + 2 * vs;   // ns
+  for (int i = threadIdx.x; i < ns; i += blockDim.x) stw[i] = tw[i];
+  const int f0 = 2 * pair, f1 = 2 * pair + 1;
+  const bool has1 = f1 < a.F;
+  for (int i = threadIdx.x; i < nrows * ns; i += blockDim.x) {
+    const int r = i / ns, ky = i % ns;
+    const int kx = r == 0 ? kxa : kxb;
+    float2 acc0 = make_float2(0.f, 0.f), acc1 = make_float2(0.f, 0.f);
+    for (int j = 0; j < a.J; ++j) {
+      const int l0 = a.per_layer ? (a.frame0 + f0) : j;
+      const float2 s0 = a.spectra[((size_t)l0 * ns + kx) * ns + ky];
+      const size_t t0 = ((size_t)f0 * a.J + j) * ns;
+      acc0 = cfma(s0, cmul(a.px[t0 + kx], a.py[t0 + ky]), acc0);
+      if (has1) {
+        const float2 s1 =
+            a.per_layer ? a.spectra[((size_t)(a.frame0 + f1) * ns + kx) * ns + ky] : s0;
+        const size_t t1 = ((size_t)f1 * a.J + j) * ns;
+        acc1 = cfma(s1, cmul(a.px[t1 + kx], a.py[t1 + ky]), acc1);
+      }
+    }
+    X[(0 * 2 + r) * vs + ky] = acc0;
+    X[(1 * 2 + r) * vs + ky] = acc1;
+  }
+  __syncthreads();
+  // Y[kx] = H0[kx] + i H1[kx], H_f[kx,ky] = (X_f[kx,ky] + conj X_f[-kx,-ky]) / 2
+  for (int i = threadIdx.x; i < nrows * ns; i += blockDim.x) {
+    const int r = i / ns, ky = i % ns;
+    const int ro = (nrows == 1) ? 0 : 1 - r;  // row holding -kx
+    const int kyn = (ns - ky) % ns;
+    const float2 a0 = X[(0 * 2 + r) * vs + ky], b0 = X[(0 * 2 + ro) * vs + kyn];
+    const float2 a1 = X[(1 * 2 + r) * vs + ky], b1 = X[(1 * 2 + ro) * vs + kyn];
+    const float2 h0 = make_float2(0.5f * (a0.x + b0.x), 0.5f * (a0.y - b0.y));
+    const float2 h1 = make_float2(0.5f * (a1.x + b1.x), 0.5f * (a1.y - b1.y));
+    bufA[r * vs + ky] = make_float2(h0.x - h1.y, h0.y + h1.x);
+  }
+  __syncthreads();
+  float2* res = fft_smem(bufA, bufB, d, stw, nrows, vs, 1, false);
+  for (int i = threadIdx.x; i < nrows * ns; i += blockDim.x) {
+    const int r = i / ns, ky = i % ns;
+    const int kx = r == 0 ? kxa : kxb;
+    work[((size_t)pair * ns + kx) * ns + ky] = res[r * vs + ky];
+  }
+}
+
+// ================================================================ pass 2
+// Column transform of a tile of C columns plus the paired real epilogue:
+// Re -> output image (pair*re_mul + re_add), Im -> (pair*im_mul + im_add),
+// each plus its subharmonic sum (coefficient row pl*crow_mul + crow_add_*)
+// minus that sum's grid mean, cropped and scaled.
+struct PairStore {
+  float* out;
+  int n_out, crop;
+  float scale;
+  int accumulate;
+  int count;  // valid output images (global)
+  int re_mul, re_add, im_mul, im_add;
+  int crow_mul, crow_re, crow_im;
+  const float2* coef;   // (rows, P, 9)
+  const float* mean;    // (rows)
+  const float2* basis;  // (P, 3, ns)
+  int P;
+};
+
+__global__ void __launch_bounds__(kThreads)
+k_pair_cols(FftDesc d, const float2* __restrict__ tw, const float2* __restrict__ work, int C,
+            int pair0, PairStore st) {
+  extern __shared__ float2 sm[];
+  const int ns = d.n;
+  const int y0 = blockIdx.x * C;
+  const int pl = blockIdx.y;  // pair within chunk
+  const int pair = pair0 + pl;
+  float2* bufA = sm;
+  float2* bufB = sm + ns * C;
+  float2* stw = bufB + ns * C;
+  float2* mtab = stw + ns;  // (2, 3P, C)
+  for (int i = threadIdx.x; i < ns; i += blockDim.x) stw[i] = tw[i];
+  for (int i = threadIdx.x; i < ns * C; i += blockDim.x) {
+    const int x = i / C, c = i % C;
+    const int y = y0 + c;
+    bufA[i] = y < ns ? work[((size_t)pl * ns + x) * ns + y] : make_float2(0.f, 0.f);
+  }
+  const int img_re = pair * st.re_mul + st.re_add;
+  const int img_im = pair * st.im_mul + st.im_add;
+  const bool do_re = img_re < st.count, do_im = img_im < st.count;
+  const int row_re = pl * st.crow_mul + st.crow_re, row_im = pl * st.crow_mul + st.crow_im;
+  const int P = st.P;
+  // m[o][p*3+i][c] = sum_j coef[o][p][i][j] basis[p][j][y]
+  for (int i = threadIdx.x; i < 2 * 3 * P * C; i += blockDim.x) {
+    const int c = i % C;
+    const int pi = (i / C) % (3 * P);
+    const int o = i / (C * 3 * P);
+    const bool ok = o == 0 ? do_re : do_im;
+    const int row = o == 0 ? row_re : row_im;
+    const int y = y0 + c;
+    float2 m = make_float2(0.f, 0.f);
+    if (ok && y < ns) {
+      const int p = pi / 3, ii = pi % 3;
+      const float2* cf = st.coef + ((size_t)row * P + p) * 9 + ii * 3;
+#pragma unroll
+      for (int j = 0; j < 3; ++j) m = cfma(cf[j], st.basis[((size_t)p * 3 + j) * ns + y], m);
+    }
+    mtab[i] = m;
+  }
+  __syncthreads();
+  float2* res = fft_smem(bufA, bufB, d, stw, C, 1, C, true);
+  const float mre = (P > 0 && do_re) ? st.mean[row_re] : 0.f;
+  const float mim = (P > 0 && do_im) ? st.mean[row_im] : 0.f;
+  const size_t plane = (size_t)st.n_out * st.n_out;
+  for (int i = threadIdx.x; i < ns * C; i += blockDim.x) {
+    const int x = i / C, c = i % C;
+    const int y = y0 + c;
+    if (y >= ns) continue;
+    const int xo = x - st.crop, yo = y - st.crop;
+    if (xo < 0 || yo < 0 || xo >= st.n_out || yo >= st.n_out) continue;
+    const float2 v = res[i];
+    float lre = 0.f, lim = 0.f;
+    for (int pi = 0; pi < 3 * P; ++pi) {
+      const float2 b = st.basis[(size_t)pi * ns + x];
+      const float2 m0 = mtab[(0 * 3 * P + pi) * C + c];
+      const float2 m1 = mtab[(1 * 3 * P + pi) * C + c];
+      lre = fmaf(b.x, m0.x, fmaf(-b.y, m0.y, lre));
+      lim = fmaf(b.x, m1.x, fmaf(-b.y, m1.y, lim));
+    }
+    const size_t o = (size_t)xo * st.n_out + yo;
+    if (do_re) {
+      const float val = st.scale * (v.x + (lre - mre));
+      float* dst = st.out + (size_t)img_re * plane + o;
+      *dst = st.accumulate ? *dst + val : val;
+    }
+    if (do_im) {
+      const float val = st.scale * (v.y + (lim - mim));
+      float* dst = st.out + (size_t)img_im * plane + o;
+      *dst = st.accumulate ? *dst + val : val;
+    }
+  }
+}
+
+// plain complex column pass (pt_ifft2)
+__global__ void __launch_bounds__(kThreads)
+k_plain_cols(FftDesc d, const float2* __restrict__ tw, const float2* __restrict__ work, int C,
+             float2* __restrict__ out) {
+  extern __shared__ float2 sm[];
+  const int ns = d.n;
+  const int y0 = blockIdx.x * C;
+  const int img = blockIdx.y;
+  float2* bufA = sm;
+  float2* bufB = sm + ns * C;
+  float2* stw = bufB + ns * C;
+  for (int i = threadIdx.x; i < ns; i += blockDim.x) stw[i] = tw[i];
+  for (int i = threadIdx.x; i < ns * C; i += blockDim.x) {
+    const int x = i / C, c = i % C;
+    const int y = y0 + c;
+    bufA[i] = y < ns ? work[((size_t)img * ns + x) * ns + y] : make_float2(0.f, 0.f);
+  }
+  __syncthreads();
+  float2* res = fft_smem(bufA, bufB, d, stw, C, 1, C, true);
+  for (int i = threadIdx.x; i < ns * C; i += blockDim.x) {
+    const int x = i / C, c = i % C;
+    const int y = y0 + c;
+    if (y < ns) out[((size_t)img * ns + x) * ns + y] = res[i];
+  }
+}
+
+// ================================================================ coefficient prep
+// generate(): coef[c][p][ij] = (n0 + i n1) * sh_amp[p][ij] for screens
+// gc = c0 + c, c < nc; mean[c] = Re sum_ij coef beta_i beta_j.
+__global__ void k_gen_coef(int count, int c0, int nc, int P, const float* __restrict__ sh_amp,
+                           const float* __restrict__ sh_noise, uint64_t seed, uint64_t call,
+                           const double* __restrict__ beta, float2* __restrict__ coef,
+                           float* __restrict__ mean) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nc) return;
+  const int gc = c0 + c;
+  double mr = 0.0;
+  for (int p = 0; p < P; ++p) {
+    for (int ij = 0; ij < 9; ++ij) {
+      float2 z;
+      if (sh_noise) {
+        // layout (P, 2, count, 3, 3)
+        const size_t base = (size_t)p * 2 * count * 9;
+        z = make_float2(sh_noise[base + (size_t)gc * 9 + ij],
+                        sh_noise[base + (size_t)count * 9 + (size_t)gc * 9 + ij]);
+      } else {
+        z = philox_cnormal(seed, ((uint64_t)gc * kMaxLevels + p) * 9 + ij, call, kDomainSub);
+      }
+      const float amp = sh_amp[p * 9 + ij];
+      const float2 cf = make_float2(z.x * amp, z.y * amp);
+      coef[((size_t)c * P + p) * 9 + ij] = cf;
+      const int i = ij / 3, j = ij % 3;
+      const double bir = beta[(p * 3 + i) * 2], bii = beta[(p * 3 + i) * 2 + 1];
+      const double bjr = beta[(p * 3 + j) * 2], bji = beta[(p * 3 + j) * 2 + 1];
+      const double br = bir * bjr - bii * bji, bi = bir * bji + bii * bjr;
+      mr += (double)cf.x * br - (double)cf.y * bi;
+    }
+  }
+  mean[c] = (float)mr;
+}
+
+// frames: per frame f of a chunk, shifted-and-summed subharmonic
+// coefficients (FP64 phases), their grid mean, and the main-grid phasor tables.
+// Displacements travel to the device inside the launch parameters (no
+// pageable copy, hence no stream synchronisation on the frame path).
+constexpr int kShiftDoubles = 1792;
+struct ShiftParams {
+  double v[kShiftDoubles];  // (nf, J, 2) for frames [fbeg, fbeg + nf) of the chunk
+};
+
+struct FramePrepArgs {
+  const float2* sh_coef;  // (P, L, 3, 3)
+  const double* sh_freq;  // (P, 3)
+  const double* beta;     // (P, 3, 2)
+  float2* coef;           // (F, P, 9)
+  float* mean;            // (F)
+  float2* px;             // (F, J, ns)
+  float2* py;
+  int F, L, J, P, ns, per_layer, frame0;
+  double df;
+};
+
+__global__ void k_frame_coef(FramePrepArgs a, ShiftParams sp, int fbeg, int nf) {
+  const int fl = blockIdx.x * blockDim.x + threadIdx.x;
+  if (fl >= nf) return;
+  const int f = fbeg + fl;
+  double mr = 0.0;
+  for (int p = 0; p < a.P; ++p) {
+    double sr[9], si[9];
+    for (int ij = 0; ij < 9; ++ij) sr[ij] = si[ij] = 0.0;
+    for (int j = 0; j < a.J; ++j) {
+      const int l = a.per_layer ? a.frame0 + f : j;
+      const double sx = sp.v[(fl * a.J + j) * 2];
+      const double sy = sp.v[(fl * a.J + j) * 2 + 1];
+      double cxr[3], cxi[3], cyr[3], cyi[3];
+      for (int i = 0; i < 3; ++i) {
+        sincospi(2.0 * a.sh_freq[p * 3 + i] * sx, &cxi[i], &cxr[i]);
+        sincospi(2.0 * a.sh_freq[p * 3 + i] * sy, &cyi[i], &cyr[i]);
+      }
+      for (int i = 0; i < 3; ++i)
+        for (int k = 0; k < 3; ++k) {
+          const float2 c = a.sh_coef[(((size_t)p * a.L + l) * 3 + i) * 3 + k];
+          const double pr = cxr[i] * cyr[k] - cxi[i] * cyi[k];
+          const double pim = cxr[i] * cyi[k] + cxi[i] * cyr[k];
+          sr[i * 3 + k] += (double)c.x * pr - (double)c.y * pim;
+          si[i * 3 + k] += (double)c.x * pim + (double)c.y * pr;
+        }
+    }
+    for (int ij = 0; ij < 9; ++ij) {
+      a.coef[((size_t)f * a.P + p) * 9 + ij] = make_float2((float)sr[ij], (float)si[ij]);
+      const int i = ij / 3, k = ij % 3;
+      const double bir = a.beta[(p * 3 + i) * 2], bii = a.beta[(p * 3 + i) * 2 + 1];
+      const double bkr = a.beta[(p * 3 + k) * 2], bki = a.beta[(p * 3 + k) * 2 + 1];
+      const double br = bir * bkr - bii * bki, bi = bir * bki + bii * bkr;
+      mr += sr[ij] * br - si[ij] * bi;
+    }
+  }
+  a.mean[f] = (float)mr;
+}
+
+// px[f][j][k] = exp(2 pi i f_k sx[f][j]), f_k = k' df, phase wrapped exactly
+// in 64-bit fixed point.
+__global__ void k_frame_phasors(FramePrepArgs a, ShiftParams sp, int fbeg) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const int fjl = blockIdx.y;  // (frame - fbeg) * J + j
+  if (k >= a.ns) return;
+  const double sx = sp.v[fjl * 2];
+  const double sy = sp.v[fjl * 2 + 1];
+  const size_t fj = (size_t)fbeg * a.J + fjl;
+  const uint64_t ux = phase_fixed(sx * a.df), uy = phase_fixed(sy * a.df);
+  const uint64_t kk = (uint64_t)(int64_t)signed_freq(k, a.ns);
+  a.px[fj * a.ns + k] = phasor_from_fixed(kk * ux);
+  a.py[fj * a.ns + k] = phasor_from_fixed(kk * uy);
+}
+
+// ================================================================ layers / boiling
+struct SeedTable {
+  uint64_t s[64];
+};
+
+__global__ void k_fill_spectra(int ns, const float* __restrict__ amplitude,
+                               const float* __restrict__ noise, SeedTable seeds,
+                               float2* __restrict__ spectra) {
+  const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const size_t plane = (size_t)ns * ns;
+  const int l = blockIdx.y;
+  if (e >= plane) return;
+  float2 z;
+  if (noise) {
+    const float* nl = noise + (size_t)l * 2 * plane;
+    z = make_float2(nl[e], nl[plane + e]);
+  } else {
+    z = philox_cnormal(seeds.s[l], e, 0, kDomainLayer);
+  }
+  const float amp = amplitude[(size_t)l * plane + e];
+  spectra[(size_t)l * plane + e] = make_float2(z.x * amp, z.y * amp);
+}
+
+__global__ void k_fill_sh(int L, int P, const float* __restrict__ sh_amp,
+                          const float* __restrict__ sh_noise, SeedTable seeds,
+                          float2* __restrict__ sh_coef) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= P * L * 9) return;
+  const int ij = i % 9, l = (i / 9) % L, p = i / (9 * L);
+  float2 z;
+  if (sh_noise) {
+    // (L, P, 2, 3, 3)
+    const float* b = sh_noise + ((size_t)l * P + p) * 18;
+    z = make_float2(b[ij], b[9 + ij]);
+  } else {
+    z = philox_cnormal(seeds.s[l], (uint64_t)p * 9 + ij, 0, kDomainLayerSub);
+  }
+  const float amp = sh_amp[i];
+  sh_coef[i] = make_float2(z.x * amp, z.y * amp);
+}
+
+__global__ void k_boil(size_t n_el, float2* __restrict__ s, const float* __restrict__ amplitude,
+                       const float* __restrict__ tau, float dt, const float* __restrict__ noise,
+                       uint64_t seed, uint64_t call, uint64_t idx_base) {
+  const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n_el) return;
+  const float a = expf(-dt / tau[e]);
+  const float b = sqrtf(fmaxf(1.0f - a * a, 0.0f));
+  const float2 z = noise ? make_float2(noise[e], noise[n_el + e])
+                         : philox_cnormal(seed, idx_base + e, call, kDomainBoil);
+  const float amp = amplitude[e];
+  const float2 v = s[e];
+  s[e] = make_float2(fmaf(a, v.x, b * (z.x * amp)), fmaf(a, v.y, b * (z.y * amp)));
+}
+
+// ================================================================ LGS zoom
+__global__ void k_lgs_zoom(int L, int ns, int n, int T, const int32_t* __restrict__ idx,
+                           const float* __restrict__ w, const float* __restrict__ screens,
+                           float scale, float* __restrict__ out) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.y;
+  if (j >= n) return;
+  float acc = 0.f;
+  for (int l = 0; l < L; ++l) {
+    const float* s = screens + (size_t)l * ns * ns;
+    const int32_t* il = idx + (size_t)l * T * n;
+    const float* wl = w + (size_t)l * T * n;
+    float v = 0.f;
+    for (int a = 0; a < T; ++a) {
+      const float* row = s + (size_t)il[a * n + i] * ns;
+      float rs = 0.f;
+      for (int b = 0; b < T; ++b) rs = fmaf(wl[b * n + j], row[il[b * n + j]], rs);
+      v = fmaf(wl[a * n + i], rs, v);
+    }
+    acc += v;
+  }
+  out[(size_t)i * n + j] = scale * acc;
+}
+
+// ================================================================ host helpers
+static size_t rows_smem(int ns, int rpc) {
+  return (size_t)(2 * rpc * (ns + 1) + ns) * sizeof(float2);
+}
+static size_t frame_rows_smem(int ns) { return (size_t)(8 * (ns + 1) + ns) * sizeof(float2); }
+static size_t cols_smem(int ns, int C, int P) {
+  return (size_t)(2 * ns * C + ns + 2 * 3 * std::max(P, 1) * C) * sizeof(float2);
+}
+
+template <class K>
+static int set_smem(K kernel, size_t bytes, const char* name) {
+  if (bytes > 227 * 1024)
+    return fail(PT_ERR_UNSUPPORTED, std::string(name) + ": grid too large for shared memory");
+  if (bytes > 48 * 1024) {
+    cudaError_t e =
+        cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e != cudaSuccess) return check_cuda(e, name);
+  }
+  return PT_OK;
+}
+
+static int check_grid(const pt_grid* g, const char* who) {
+  if (!g) return fail(PT_ERR_ARG, std::string(who) + ": grid is NULL");
+  return PT_OK;
+}
+
+}  // namespace pt
+
+using namespace pt;
+
+// ================================================================ C-ABI
+extern "C" int pt_grid_create(pt_grid** out, int ns, double dx, int P, const double* sh_freq) {
+  if (!out) return fail(PT_ERR_ARG, "pt_grid_create: out is NULL");
+  *out = nullptr;
+  if (ns < 2 || ns > 8192) return fail(PT_ERR_ARG, "pt_grid_create: ns must be in [2, 8192]");
+  if (!(dx > 0) || !std::isfinite(dx))
+    return fail(PT_ERR_ARG, "pt_grid_create: pixel_scale must be positive and finite");
+  if (P < 0 || P > kMaxLevels) return fail(PT_ERR_ARG, "pt_grid_create: n_levels must be in [0, 16]");
+  if (P > 0 && !sh_freq) return fail(PT_ERR_ARG, "pt_grid_create: sh_freq is NULL");
+  pt_grid* g = new pt_grid{};
+  g->ns = ns;
+  g->dx = dx;
+  g->P = P;
+  g->desc = make_fft_desc(ns);
+  if (g->desc.nstages >= kMaxStages) {
+    delete g;
+    return fail(PT_ERR_UNSUPPORTED, "pt_grid_create: too many FFT stages");
+  }
+  std::vector<float2> tw(ns);
+  for (int k = 0; k < ns; ++k) {
+    const double a = 2.0 * M_PI * (double)k / ns;
+    tw[k] = make_float2((float)std::cos(a), (float)std::sin(a));
+  }
+  const int Pm = std::max(P, 1);
+  std::vector<float2> basis((size_t)Pm * 3 * ns, make_float2(0.f, 0.f));
+  std::vector<double> beta((size_t)Pm * 3 * 2, 0.0);
+  for (int p = 0; p < P; ++p)
+    for (int i = 0; i < 3; ++i) {
+      const double f = sh_freq[p * 3 + i];
+      double br = 0, bi = 0;
+      for (int x = 0; x < ns; ++x) {
+        const double arg = 2.0 * M_PI * f * (((double)x - ns / 2.0) * dx);
+        const double c = std::cos(arg), s = std::sin(arg);
+        basis[((size_t)p * 3 + i) * ns + x] = make_float2((float)c, (float)s);
+        br += c;
+        bi += s;
+      }
+      beta[(p * 3 + i) * 2] = br / ns;
+      beta[(p * 3 + i) * 2 + 1] = bi / ns;
+    }
+  std::vector<double> freq((size_t)Pm * 3, 0.0);
+  for (int i = 0; i < P * 3; ++i) freq[i] = sh_freq[i];
+  int rc = check_cuda(cudaMalloc(&g->tw, ns * sizeof(float2)), "pt_grid_create: cudaMalloc");
+  if (!rc) rc = check_cuda(cudaMalloc(&g->basis, basis.size() * sizeof(float2)), "pt_grid_create: cudaMalloc");
+  if (!rc) rc = check_cuda(cudaMalloc(&g->sh_freq, freq.size() * sizeof(double)), "pt_grid_create: cudaMalloc");
+  if (!rc) rc = check_cuda(cudaMalloc(&g->beta, beta.size() * sizeof(double)), "pt_grid_create: cudaMalloc");
+  if (!rc) rc = check_cuda(cudaMemcpy(g->tw, tw.data(), ns * sizeof(float2), cudaMemcpyHostToDevice), "pt_grid_create: cudaMemcpy");
+  if (!rc) rc = check_cuda(cudaMemcpy(g->basis, basis.data(), basis.size() * sizeof(float2), cudaMemcpyHostToDevice), "pt_grid_create: cudaMemcpy");
+  if (!rc) rc = check_cuda(cudaMemcpy(g->sh_freq, freq.data(), freq.size() * sizeof(double), cudaMemcpyHostToDevice), "pt_grid_create: cudaMemcpy");
+  if (!rc) rc = check_cuda(cudaMemcpy(g->beta, beta.data(), beta.size() * sizeof(double), cudaMemcpyHostToDevice), "pt_grid_create: cudaMemcpy");
+  if (rc) {
+    pt_grid_destroy(g);
+    return rc;
+  }
+  *out = g;
+  return PT_OK;
+}
+
+extern "C" int pt_grid_destroy(pt_grid* g) {
+  if (!g) return PT_OK;
+  cudaFree(g->tw);
+  cudaFree(g->basis);
+  cudaFree(g->sh_freq);
+  cudaFree(g->beta);
+  delete g;
+  return PT_OK;
+}
+
+extern "C" size_t pt_grid_workspace_bytes(const pt_grid* g, int L) {
+  if (!g) return 0;
+  return carve(g, std::max(1, L), nullptr).bytes;
+}
+
+extern "C" int pt_ifft2(const pt_grid* g, const float* in, float* out, int batch, void* work,
+                        size_t work_bytes, void* stream) {
+  if (int rc = check_grid(g, "pt_ifft2")) return rc;
+  if (!in || !out || batch < 0) return fail(PT_ERR_ARG, "pt_ifft2: bad arguments");
+  SpecWork w = carve(g, 1, work);
+  if (!work || work_bytes < w.bytes) return fail(PT_ERR_ARG, "pt_ifft2: workspace too small");
+  cudaStream_t s = (cudaStream_t)stream;
+  const int ns = g->ns, ch = image_chunk(ns), rpc = rows_per_cta(ns), C = cols_per_cta(ns);
+  const size_t rs = rows_smem(ns, rpc), cs = cols_smem(ns, C, 0);
+  if (int rc = set_smem(k_rows, rs, "k_rows")) return rc;
+  if (int rc = set_smem(k_plain_cols, cs, "k_plain_cols")) return rc;
+  GenRowArgs none{};
+  for (int b0 = 0; b0 < batch; b0 += ch) {
+    const int nb = std::min(ch, batch - b0);
+    const float2* src = (const float2*)in + (size_t)b0 * ns * ns;
+    float2* dst = (float2*)out + (size_t)b0 * ns * ns;
+    k_rows<<<dim3((ns + rpc - 1) / rpc, nb), kThreads, rs, s>>>(g->desc, g->tw, rpc, src, 0, none, w.img);
+    k_plain_cols<<<dim3((ns + C - 1) / C, nb), kThreads, cs, s>>>(g->desc, g->tw, w.img, C, dst);
+    count_launch(2);
+    if (int rc = check_launch("pt_ifft2")) return rc;
+  }
+  return PT_OK;
+}
+
+extern "C" int pt_generate(const pt_grid* g, int count, const float* amplitude,
+                           const float* sh_amp, const float* noise, const float* sh_noise,
+                           uint64_t seed, uint64_t call, int crop, int n_out, float scale,
+                           int accumulate, float* out, void* work, size_t work_bytes,
+                           void* stream) {
+  if (int rc = check_grid(g, "pt_generate")) return rc;
+  const int ns = g->ns, P = g->P;
+  if (count < 1) return fail(PT_ERR_ARG, "pt_generate: count must be >= 1");
+  if (!amplitude || !out) return fail(PT_ERR_ARG, "pt_generate: NULL amplitude or out");
+  if (P > 0 && !sh_amp) return fail(PT_ERR_ARG, "pt_generate: sh_amp is NULL");
+  if (crop < 0 || n_out < 1 || crop + n_out > ns)
+    return fail(PT_ERR_ARG, "pt_generate: crop window outside the grid");
+  SpecWork w = carve(g, 1, work);
+  if (!work || work_bytes < w.bytes) return fail(PT_ERR_ARG, "pt_generate: workspace too small");
+  cudaStream_t s = (cudaStream_t)stream;
+  const int n_fft = (count + 1) / 2;
+  const int ch = image_chunk(ns), rpc = rows_per_cta(ns), C = cols_per_cta(ns);
+  const size_t rs = rows_smem(ns, rpc), cs = cols_smem(ns, C, P);
+  if (int rc = set_smem(k_rows, rs, "k_rows")) return rc;
+  if (int rc = set_smem(k_pair_cols, cs, "k_pair_cols")) return rc;
+  for (int b0 = 0; b0 < n_fft; b0 += ch) {
+    const int nb = std::min(ch, n_fft - b0);
+    GenRowArgs ga{amplitude, noise, n_fft, b0, seed, call};
+    k_rows<<<dim3((ns + rpc - 1) / rpc, nb), kThreads, rs, s>>>(g->desc, g->tw, rpc, nullptr, 1, ga, w.img);
+    count_launch();
+    PairStore st{};
+    st.out = out;
+    st.n_out = n_out;
+    st.crop = crop;
+    st.scale = scale;
+    st.accumulate = accumulate;
+    st.count = count;
+    st.re_mul = 1;
+    st.re_add = 0;
+    st.im_mul = 1;
+    st.im_add = n_fft;
+    st.crow_mul = 1;
+    st.crow_re = 0;   // rows [0, ch): screens b0 + pl
+    st.crow_im = ch;  // rows [ch, 2 ch): screens n_fft + b0 + pl
+    st.coef = w.coef;
+    st.mean = w.mean;
+    st.basis = g->basis;
+    st.P = P;
+    if (P > 0) {
+      const int n_re = std::min(nb, count - b0);
+      const int n_im = std::max(0, std::min(nb, count - (n_fft + b0)));
+      k_gen_coef<<<(n_re + 127) / 128, 128, 0, s>>>(count, b0, n_re, P, sh_amp, sh_noise, seed,
+                                                    call, g->beta, w.coef, w.mean);
+      count_launch();
+      if (n_im > 0) {
+        k_gen_coef<<<(n_im + 127) / 128, 128, 0, s>>>(count, n_fft + b0, n_im, P, sh_amp,
+                                                      sh_noise, seed, call, g->beta,
+                                                      w.coef + (size_t)ch * P * 9, w.mean + ch);
+        count_launch();
+      }
+    }
+    k_pair_cols<<<dim3((ns + C - 1) / C, nb), kThreads, cs, s>>>(g->desc, g->tw, w.img, C, b0, st);
+    count_launch();
+    if (int rc = check_launch("pt_generate")) return rc;
+  }
+  return PT_OK;
+}
+
+extern "C" int pt_layers_fill(const pt_grid* g, int L, const float* amplitude,
+                              const float* sh_amp, const float* noise, const float* sh_noise,
+                              const uint64_t* seeds, float* spectra, float* sh_coef,
+                              void* stream) {
+  if (int rc = check_grid(g, "pt_layers_fill")) return rc;
+  if (L < 1 || L > 64) return fail(PT_ERR_ARG, "pt_layers_fill: n_layers must be in [1, 64]");
+  if (!amplitude || !spectra) return fail(PT_ERR_ARG, "pt_layers_fill: NULL amplitude or spectra");
+  if (g->P > 0 && (!sh_amp || !sh_coef)) return fail(PT_ERR_ARG, "pt_layers_fill: NULL sh_amp or sh_coef");
+  if ((!noise || (g->P > 0 && !sh_noise)) && !seeds)
+    return fail(PT_ERR_ARG, "pt_layers_fill: seeds required when noise is not injected");
+  SeedTable st{};
+  for (int l = 0; l < L; ++l) st.s[l] = seeds ? seeds[l] : 0;
+  cudaStream_t s = (cudaStream_t)stream;
+  const size_t plane = (size_t)g->ns * g->ns;
+  k_fill_spectra<<<dim3((unsigned)((plane + 255) / 256), L), 256, 0, s>>>(
+      g->ns, amplitude, noise, st, (float2*)spectra);
+  count_launch();
+  if (g->P > 0) {
+    const int n = g->P * L * 9;
+    k_fill_sh<<<(n + 127) / 128, 128, 0, s>>>(L, g->P, sh_amp, sh_noise, st, (float2*)sh_coef);
+    count_launch();
+  }
+  return check_launch("pt_layers_fill");
+}
+
+extern "C" int pt_frames(const pt_grid* g, int L, const float* spectra, const float* sh_coef,
+                         int F, const double* sx, const double* sy, int per_layer, int crop,
+                         int n_out, float scale, float* out, void* work, size_t work_bytes,
+                         void* stream) {
+  if (int rc = check_grid(g, "pt_frames")) return rc;
+  const int ns = g->ns, P = g->P;
+  if (L < 1) return fail(PT_ERR_ARG, "pt_frames: n_layers must be >= 1");
+  if (F < 1) return fail(PT_ERR_ARG, "pt_frames: n_frames must be >= 1");
+  if (!spectra || !out || !sx || !sy) return fail(PT_ERR_ARG, "pt_frames: NULL pointer");
+  if (P > 0 && !sh_coef) return fail(PT_ERR_ARG, "pt_frames: sh_coef is NULL");
+  if (per_layer && F != L) return fail(PT_ERR_ARG, "pt_frames: per-layer mode needs n_frames == n_layers");
+  if (per_layer && (crop != 0 || n_out != ns)) return fail(PT_ERR_ARG, "pt_frames: per-layer screens are uncropped");
+  if (crop < 0 || n_out < 1 || crop + n_out > ns)
+    return fail(PT_ERR_ARG, "pt_frames: crop window outside the grid");
+  SpecWork w = carve(g, L, work);
+  if (!work || work_bytes < w.bytes) return fail(PT_ERR_ARG, "pt_frames: workspace too small");
+  cudaStream_t s = (cudaStream_t)stream;
+  const int ch = image_chunk(ns), C = cols_per_cta(ns);
+  const int J = per_layer ? 1 : L;
+  const size_t rs = frame_rows_smem(ns), cs = cols_smem(ns, C, P);
+  if (int rc = set_smem(k_frame_rows, rs, "k_frame_rows")) return rc;
+  if (int rc = set_smem(k_pair_cols, cs, "k_pair_cols")) return rc;
+  const int fchunk = 2 * ch;
+  const int fsub = std::max(1, kShiftDoubles / (2 * J));  // frames per parameter block
+  for (int f0 = 0; f0 < F; f0 += fchunk) {
+    const int nf = std::min(fchunk, F - f0);
+    const int npair = (nf + 1) / 2;
+    FramePrepArgs pa{};
+    pa.sh_coef = (const float2*)sh_coef;
+    pa.sh_freq = g->sh_freq;
+    pa.beta = g->beta;
+    pa.coef = w.coef;
+    pa.mean = w.mean;
+    pa.px = w.px;
+    pa.py = w.py;
+    pa.F = nf;
+    pa.L = L;
+    pa.J = J;
+    pa.P = P;
+    pa.ns = ns;
+    pa.per_layer = per_layer;
+    pa.frame0 = f0;
+    pa.df = 1.0 / (ns * g->dx);
+    for (int fb = 0; fb < nf; fb += fsub) {
+      const int nb = std::min(fsub, nf - fb);
+      ShiftParams sp;
+      for (int f = 0; f < nb; ++f)
+        for (int j = 0; j < J; ++j) {
+          const int gf = f0 + fb + f;
+          const size_t src = per_layer ? (size_t)gf : (size_t)gf * L + j;
+          sp.v[(f * J + j) * 2] = sx[src];
+          sp.v[(f * J + j) * 2 + 1] = sy[src];
+        }
+      if (P > 0) {
+        k_frame_coef<<<(nb + 63) / 64, 64, 0, s>>>(pa, sp, fb, nb);
+        count_launch();
+      }
+      k_frame_phasors<<<dim3((ns + 255) / 256, nb * J), 256, 0, s>>>(pa, sp, fb);
+      count_launch();
+    }
+    FrameRowArgs fa{(const float2*)spectra, w.px, w.py, J, nf, f0, per_layer};
+    k_frame_rows<<<dim3(ns / 2 + 1, npair), kThreads, rs, s>>>(g->desc, g->tw, fa, w.img);
+    count_launch();
+    PairStore st{};
+    st.out = out + (size_t)f0 * n_out * n_out;
+    st.n_out = n_out;
+    st.crop = crop;
+    st.scale = scale;
+    st.accumulate = 0;
+    st.count = nf;
+    st.re_mul = 2;
+    st.re_add = 0;
+    st.im_mul = 2;
+    st.im_add = 1;
+    st.crow_mul = 2;
+    st.crow_re = 0;
+    st.crow_im = 1;
+    st.coef = w.coef;
+    st.mean = w.mean;
+    st.basis = g->basis;
+    st.P = P;
+    k_pair_cols<<<dim3((ns + C - 1) / C, npair), kThreads, cs, s>>>(g->desc, g->tw, w.img, C, 0, st);
+    count_launch();
+    if (int rc = check_launch("pt_frames")) return rc;
+  }
+  return PT_OK;
+}
+
+extern "C" int pt_lgs_zoom(int L, int ns, int n, int T, const int32_t* idx, const float* w,
+                           const float* screens, float scale, float* out, void* stream) {
+  if (L < 1 || ns < 1 || n < 1 || T < 1 || T > 6) return fail(PT_ERR_ARG, "pt_lgs_zoom: bad sizes");
+  if (!idx || !w || !screens || !out) return fail(PT_ERR_ARG, "pt_lgs_zoom: NULL pointer");
+  cudaStream_t s = (cudaStream_t)stream;
+  k_lgs_zoom<<<dim3((n + 127) / 128, n), 128, 0, s>>>(L, ns, n, T, idx, w, screens, scale, out);
+  count_launch();
+  return check_launch("pt_lgs_zoom");
+}
+
+extern "C" int pt_boil_step(const pt_grid* g, int L, float* spectra, float* sh_coef,
+                            const float* amplitude, const float* sh_amp, const float* main_tau,
+                            const float* sh_tau, double dt, const float* noise,
+                            const float* sh_noise, uint64_t seed, uint64_t call, void* stream) {
+  if (int rc = check_grid(g, "pt_boil_step")) return rc;
+  if (L < 1 || !spectra || !amplitude || !main_tau) return fail(PT_ERR_ARG, "pt_boil_step: bad arguments");
+  if (g->P > 0 && (!sh_coef || !sh_amp || !sh_tau)) return fail(PT_ERR_ARG, "pt_boil_step: NULL subharmonic table");
+  if (!(dt > 0)) return fail(PT_ERR_ARG, "pt_boil_step: dt must be positive");
+  cudaStream_t s = (cudaStream_t)stream;
+  const size_t n_main = (size_t)L * g->ns * g->ns;
+  k_boil<<<(unsigned)((n_main + 255) / 256), 256, 0, s>>>(n_main, (float2*)spectra, amplitude,
+                                                         main_tau, (float)dt, noise, seed, call, 0);
+  count_launch();
+  if (g->P > 0) {
+    const size_t n_sh = (size_t)g->P * L * 9;
+    k_boil<<<(unsigned)((n_sh + 127) / 128), 128, 0, s>>>(n_sh, (float2*)sh_coef, sh_amp, sh_tau,
+                                                         (float)dt, sh_noise, seed, call,
+                                                         1ull << 40);
+    count_launch();
+  }
+  return check_launch("pt_boil_step");
+}

@@ -1,0 +1,349 @@
+"""Non-periodic frozen flow by Assemat-Wilson row extrusion on the GB300
+(drop-in for ``pyturb.extrude.ExtrudedAtmosphere``).
+
+Setup (host, FP64, once per outer scale — as in the reference): the von
+Karman covariances of the stencil rows and the new row, ``A = C_xz C_zz^-1``
+by Cholesky and ``B`` from the eigen-decomposition of the conditional
+covariance (``src/pyturb/extrude.py:250-304``), uploaded once as the float32
+operator ``M = [A | B_unit]`` (W x (m+1) W).
+
+Device state: one ``(L, cap, W)`` float32 slab of ring buffers. Virtual row v
+of a layer sits in physical row ``(v - v0) mod cap``, so the wind advances an
+index. The host keeps the reference's ``base``/``fill`` bookkeeping,
+compaction included (``src/pyturb/ring.py:9-28``), purely as integers: it
+fixes which rows a readout may touch (its clamp range) exactly as the
+reference does, without moving any data.
+
+Per frame: all layers' new rows for one row step are one native GEMM
+(``pt_extrude_rows``), then one fused readout kernel samples every layer's
+rotated, magnified, shifted pupil grid and sums the layers
+(``pt_readout``, the reference's ``extrude_readout_*`` kernels).
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+from math import floor
+from typing import Any, List, Optional, Sequence, Tuple, Union
+
+import numpy as np
+
+from . import _lib
+from .backend import NoiseStream, cuda_device, dptr, stream_handle, torch_module, upload
+from .config import ExtrusionConfig
+from .fourier import PhaseScreen
+
+__all__ = ["ExtrudedAtmosphere", "build_extrusion", "phase_covariance", "RingExtruder"]
+
+_INTERP = {"linear": 0, "cubic": 1, "lanczos": 2}
+
+
+def phase_covariance(r, r0: float, L0: float) -> np.ndarray:
+    """Von Karman phase covariance [rad^2] (``src/pyturb/infinite.py:88-117``):
+    ``C(r) = (L0/r0)^{5/3} 2^{-5/6} Gamma(11/6) / pi^{8/3} ((24/5) Gamma(6/5))^{5/6}
+    x^{5/6} K_{5/6}(x)``, ``x = 2 pi r / L0``, with the ``x -> 0`` limit
+    ``2^{-1/6} Gamma(5/6)``."""
+    from scipy.special import gamma, kv
+
+    if not np.isfinite(L0):
+        raise ValueError("phase_covariance requires a finite outer scale L0")
+    r = np.asarray(r, dtype=np.float64)
+    pref = ((L0 / r0) ** (5.0 / 3.0)
+            * (2.0 ** (-5.0 / 6.0) * gamma(11.0 / 6.0) / np.pi ** (8.0 / 3.0))
+            * ((24.0 / 5.0) * gamma(6.0 / 5.0)) ** (5.0 / 6.0))
+    x = 2.0 * np.pi * r / L0
+    core = np.full_like(x, 2.0 ** (-1.0 / 6.0) * gamma(5.0 / 6.0))
+    nz = x > 0
+    core[nz] = x[nz] ** (5.0 / 6.0) * kv(5.0 / 6.0, x[nz])
+    return pref * core
+
+
+def _spd_solve(spd: np.ndarray, rhs: np.ndarray) -> np.ndarray:
+    """Cholesky solve with a least-squares fallback (``src/pyturb/infinite.py:54-64``)."""
+    from scipy import linalg
+
+    try:
+        return linalg.cho_solve(linalg.cho_factor(spd), rhs)
+    except np.linalg.LinAlgError:
+        return np.linalg.lstsq(spd, rhs, rcond=None)[0]
+
+
+def build_extrusion(width: int, stencil_rows: int, pixel_scale: float, L0: float,
+                    r0: float = 1.0) -> Tuple[np.ndarray, np.ndarray]:
+    """FP64 ``(A (W, mW), B (W, W))`` for extruding one W-pixel row from the m
+    rows below it (``src/pyturb/extrude.py:250-304``, ``src/pyturb/infinite.py:231-269``).
+    Stencil rows sit at y = 0..m-1, the new row at y = m; the stencil is
+    flattened row-major, matching ``buf[fill-m:fill].ravel()``."""
+    m, n = int(stencil_rows), int(width)
+    yz, xz = np.mgrid[0:m, 0:n]
+    stencil = np.column_stack((xz.ravel(), yz.ravel())).astype(np.float64)
+    new_row = np.column_stack((np.arange(n, dtype=np.float64), np.full(n, float(m))))
+
+    def cov(a, b):
+        sep = np.hypot(a[:, None, 0] - b[None, :, 0], a[:, None, 1] - b[None, :, 1])
+        return phase_covariance(sep * pixel_scale, r0, L0)
+
+    c_zz = cov(stencil, stencil)
+    c_xz = cov(new_row, stencil)
+    c_xx = cov(new_row, new_row)
+    a = _spd_solve(c_zz, c_xz.T).T
+    res = c_xx - a @ c_xz.T
+    res = (res + res.T) / 2.0
+    w, v = np.linalg.eigh(res)
+    b = v * np.sqrt(np.clip(w, 0.0, None))
+    return a, b
+
+
+def along_extent_and_span(n: int, vx: float, vy: float, mag: float,
+                          fov_margin_pix: float) -> Tuple[float, int]:
+    """A layer's along-wind half extent and buffer span (``src/pyturb/extrude.py:222-247``)."""
+    speed = float(np.hypot(vx, vy))
+    c = vx / speed if speed > 0 else 1.0
+    s = vy / speed if speed > 0 else 0.0
+    half = (n - 1) / 2.0 * float(mag)
+    ext = half * (abs(c) + abs(s))
+    span = int(np.ceil(ext + fov_margin_pix)) - int(np.floor(-ext - fov_margin_pix)) + 3
+    return ext, span
+
+
+def compact_bounds(base: int, fill: int, m: int, first_readable_row: float) -> Tuple[int, int]:
+    """New ``(base, fill)`` after the reference's ring compaction
+    (``src/pyturb/ring.py:9-28``): rows below the readable window and the
+    stencil are dropped, at least one."""
+    target = int(floor(first_readable_row)) - 1
+    stencil = base + fill - m
+    keep_from = max(1, min(target, stencil) - base)
+    return base + keep_from, fill - keep_from
+
+
+class RingExtruder:
+    """The device ring slabs plus the per-screen host bookkeeping.
+
+    ``screens`` independent ring buffers of ``cap`` rows x ``W`` columns; screen
+    s uses operator group ``groups[s]`` scaled by ``bscale[s]``."""
+
+    def __init__(self, W: int, m: int, cap: int, operators: List[Tuple[np.ndarray, np.ndarray]],
+                 groups: Sequence[int], bscale: Sequence[float], streams: Sequence[NoiseStream]):
+        torch = torch_module()
+        self.W, self.m, self.cap = int(W), int(m), int(cap)
+        self.S = len(groups)
+        self.groups = [int(g) for g in groups]
+        self.bscale = [float(b) for b in bscale]
+        self.streams = list(streams)
+        M = np.stack([np.concatenate([a, b], axis=1) for a, b in operators])  # (G, W, (m+1)W)
+        self.G = M.shape[0]
+        self.M = upload(M)
+        self.buf = torch.empty((self.S, self.cap, self.W), dtype=torch.float32,
+                               device=cuda_device())
+        self.top = [0] * self.S  # rows extruded so far (relative virtual rows [0, top))
+        self.work_bytes = 0
+        self.work = None
+        self._jobs_cap = 0
+
+    def _ensure_work(self, jobs_per_step: int) -> None:
+        need = int(_lib.load().pt_extrude_workspace_bytes(self.W, self.m, max(1, jobs_per_step)))
+        if need > self.work_bytes:
+            torch = torch_module()
+            self.work = torch.empty(need, dtype=torch.uint8, device=cuda_device())
+            self.work_bytes = need
+
+    def seed_rows(self, s: int, rows) -> None:
+        """Copy the initial (span, W) rows of screen s into ring rows [0, span)."""
+        k = rows.shape[0]
+        self.buf[s, :k].copy_(rows)
+        self.top[s] = k
+
+    def extrude(self, counts: Sequence[int]) -> None:
+        """Extrude ``counts[s]`` new rows on every screen s, in as many row steps
+        as the largest count; each step is one native call chain."""
+        steps = max(counts) if len(counts) else 0
+        if steps <= 0:
+            return
+        jobs = []
+        noise_rows = []
+        injected = any(st.injected for st in self.streams)
+        for k in range(steps):
+            for s in range(self.S):
+                if k >= counts[s]:
+                    continue
+                st = self.streams[s]
+                row = self.top[s]
+                j = _lib.ExtrudeJob()
+                j.screen = s
+                j.group = self.groups[s]
+                j.head = row % self.cap
+                j.step = k
+                j.bscale = self.bscale[s]
+                j.key = st.key
+                j.row = row
+                if injected:
+                    j.noise_off = len(noise_rows) * self.W
+                    noise_rows.append(st.draw((self.W,)))
+                jobs.append(j)
+                self.top[s] = row + 1
+        per_step = max(sum(1 for c in counts if c > k) for k in range(steps))
+        self._ensure_work(per_step)
+        arr = (_lib.ExtrudeJob * len(jobs))(*jobs)
+        noise = upload(np.stack(noise_rows)) if injected else None
+        _lib.call("pt_extrude_rows", self.W, self.m, self.cap, self.G, dptr(self.M),
+                  dptr(self.buf), len(jobs), arr, dptr(noise), dptr(self.work),
+                  self.work_bytes, stream_handle())
+
+
+class _LayerGeom:
+    """Per-layer geometry and reference bookkeeping (``src/pyturb/extrude.py:307-496``)."""
+
+    def __init__(self, n, W, dx, vx, vy, altitude_los, m, mag, fov_margin_pix):
+        speed = float(np.hypot(vx, vy))
+        self.speed = speed
+        self.cos = vx / speed if speed > 0 else 1.0
+        self.sin = vy / speed if speed > 0 else 0.0
+        self.altitude_pix = float(altitude_los) / dx
+        self.mag = float(mag)
+        g = (np.arange(n, dtype=np.float64) - (n - 1) / 2.0) * self.mag
+        along = g[:, None] * self.cos + g[None, :] * self.sin
+        self.along_min = float(along.min())
+        self.along_max = float(along.max())
+        self.fov = float(fov_margin_pix)
+        extent_min = self.along_min - self.fov
+        self.span = int(np.ceil(self.along_max + self.fov)) - int(np.floor(extent_min)) + 3
+        self.base = int(np.floor(extent_min)) - 2  # virtual row of buffer row 0
+        self.v0 = self.base                         # virtual row of ring row 0
+        self.fill = self.span
+        self.travel = 0.0
+        self.m = m
+
+    def offsets_for_direction(self, thx: float, thy: float) -> Tuple[float, float]:
+        dxp = self.altitude_pix * thx
+        dyp = self.altitude_pix * thy
+        return dxp * self.cos + dyp * self.sin, -dxp * self.sin + dyp * self.cos
+
+
+class ExtrudedAtmosphere:
+    """Multi-layer extrusion engine (``src/pyturb/extrude.py:499-915``).
+
+    Constructor as the reference's plus ``host_noise`` (parity mode).
+    :meth:`integrate` returns a float32 CUDA tensor ``(n, n)``.
+    """
+
+    def __init__(self, n: int, pixel_scale: float, layer_r0: Sequence[float],
+                 layer_L0: Sequence[float], layer_wind: Sequence[Tuple[float, float]],
+                 layer_altitude_los: Sequence[float],
+                 field_of_view_pix: Union[float, Sequence[float]] = 0.0,
+                 stencil_rows: int = 2, interp: str = "cubic",
+                 lgs_altitude_los: Optional[float] = None, device: str = "gpu",
+                 dtype: Any = "float32", seeds: Optional[Sequence[Any]] = None,
+                 tau_boil: Optional[Sequence[float]] = None, boil_seed: Optional[Any] = None,
+                 host_noise=None) -> None:
+        config = ExtrusionConfig.create(
+            n, pixel_scale, layer_r0, layer_L0, layer_wind, layer_altitude_los,
+            field_of_view_pix, stencil_rows, interp, lgs_altitude_los, device, dtype, seeds,
+            tau_boil, boil_seed)
+        if any(np.isfinite(t) for t in config.tau_boil):
+            raise NotImplementedError(
+                "boiling on engine='extrude' is not implemented on the GPU backend yet; "
+                "use engine='spectral' boiling")
+        self.config = config
+        self.n = config.grid.n
+        self.dx = config.grid.pixel_scale
+        self.device = config.grid.device
+        self.dtype = config.grid.dtype
+        self.interp = config.interp
+        self.m = config.stencil_rows
+        L = len(config.layer_r0)
+        if config.lgs_altitude_los is not None:
+            mags = [1.0 - a / config.lgs_altitude_los for a in config.layer_altitude_los]
+        else:
+            mags = [1.0] * L
+        extents, spans = [], []
+        for (vx, vy), mag, fov in zip(config.layer_wind, mags, config.field_of_view_pix):
+            e, s = along_extent_and_span(self.n, vx, vy, mag, fov)
+            extents.append(e)
+            spans.append(s)
+        self.width = int(np.ceil(2.0 * max(extents) + 2.0 * max(config.field_of_view_pix))) + 4
+        self.capacity = max(spans) + self.n + self.m + 32
+        W = self.width
+
+        op_index: dict = {}
+        operators = []
+        groups = []
+        for L0 in config.layer_L0:
+            key = round(float(L0), 9)
+            if key not in op_index:
+                op_index[key] = len(operators)
+                operators.append(build_extrusion(W, self.m, self.dx, float(L0)))
+            groups.append(op_index[key])
+        streams = [NoiseStream(s, host_noise) for s in config.seeds]
+        self._streams = streams
+        self.layers: List[_LayerGeom] = []
+        for (vx, vy), alt, mag, fov in zip(config.layer_wind, config.layer_altitude_los, mags,
+                                           config.field_of_view_pix):
+            self.layers.append(_LayerGeom(self.n, W, self.dx, vx, vy, alt, self.m, mag, fov))
+        bscale = [float(r0) ** (-5.0 / 6.0) for r0 in config.layer_r0]
+        self._ring = RingExtruder(W, self.m, self.capacity, operators, groups, bscale, streams)
+        # seed each ring with a von Karman screen from the layer's own stream
+        for i, (r0, L0) in enumerate(zip(config.layer_r0, config.layer_L0)):
+            gen = PhaseScreen(n=W, pixel_scale=self.dx, r0=float(r0), L0=float(L0),
+                              _stream=streams[i], host_noise=host_noise)
+            init = gen.generate()
+            self._ring.seed_rows(i, init[: self.layers[i].span])
+            del gen
+
+    @property
+    def _buf(self):
+        return self._ring.buf
+
+    def _plan(self, ly: _LayerGeom) -> int:
+        """Rows the layer needs to cover its travel, with the reference's
+        compaction bookkeeping applied (``src/pyturb/extrude.py:424-449``)."""
+        top = int(np.ceil(ly.along_max + ly.fov + ly.travel)) + 2
+        count = 0
+        while ly.base + ly.fill - 1 < top:
+            if ly.fill == self.capacity:
+                ly.base, ly.fill = compact_bounds(ly.base, ly.fill, ly.m,
+                                                  ly.along_min - ly.fov + ly.travel)
+            ly.fill += 1
+            count += 1
+        return count
+
+    def set_time(self, t: float) -> None:
+        """Advance every layer to time ``t`` (``src/pyturb/extrude.py:656-659``)."""
+        counts = []
+        for ly in self.layers:
+            travel = ly.speed * t / self.dx
+            if travel < ly.travel:
+                raise ValueError("wind travel is monotonic; travel cannot decrease")
+            ly.travel = float(travel)
+            counts.append(self._plan(ly))
+        self._ring.extrude(counts)
+
+    def boil_step(self, dt: float) -> None:
+        """Frozen flow only on this backend (boiling is refused at construction)."""
+        return None
+
+    def readout_params(self, thx: float = 0.0, thy: float = 0.0):
+        arr = (_lib.ReadoutLayer * len(self.layers))()
+        for i, ly in enumerate(self.layers):
+            off_a, off_p = ly.offsets_for_direction(thx, thy)
+            p = arr[i]
+            p.screen = i
+            p.row_max = ly.fill - 1
+            p.anchor_phys = (ly.base - ly.v0) % self.capacity
+            p.cos_t = ly.cos
+            p.sin_t = ly.sin
+            p.mag = ly.mag
+            p.shift_along = (ly.travel - ly.base) + off_a
+            p.shift_perp = off_p
+        return arr
+
+    def integrate(self, thx: float = 0.0, thy: float = 0.0, scale: float = 1.0, out=None):
+        """Summed phase ``(n, n)`` toward direction tangents (thx, thy)
+        (``src/pyturb/extrude.py:754-770``)."""
+        torch = torch_module()
+        if out is None:
+            out = torch.empty((self.n, self.n), dtype=torch.float32, device=self._buf.device)
+        params = self.readout_params(thx, thy)
+        _lib.call("pt_readout", self.n, self.width, self.capacity, _INTERP[self.interp],
+                  len(self.layers), params, dptr(self._buf), float(scale), dptr(out),
+                  stream_handle())
+        return out

@@ -1,0 +1,74 @@
+"""The C-ABI library builds, loads and exports every entry point the header
+declares; argument errors are reported before any device work (no GPU needed)."""
+
+import ctypes as C
+import re
+from pathlib import Path
+
+import pytest
+
+from pyturb_gb300 import _build, _lib
+
+HEADER = Path(__file__).resolve().parent.parent / "include" / "pyturb_gb300.h"
+
+
+def declared_functions():
+    text = HEADER.read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    names = re.findall(r"\b(pt_[a-z0-9_]+)\s*\(", text)
+    return sorted(set(names))
+
+
+def test_header_declares_the_entry_points():
+    names = declared_functions()
+    for must in ("pt_generate", "pt_frames", "pt_extrude_rows", "pt_readout", "pt_ifft2",
+                 "pt_grid_create", "pt_last_error"):
+        assert must in names
+
+
+def test_library_exports_every_declared_symbol():
+    lib = _lib.load()
+    for name in declared_functions():
+        assert hasattr(lib, name), name
+
+
+def test_binding_covers_the_header_exactly():
+    assert sorted(_lib.SIGNATURES) == declared_functions()
+
+
+def test_library_is_built_for_sm_103a_only():
+    assert _build.ARCH == ["-gencode", "arch=compute_103a,code=sm_103a"]
+    assert _build.library_path().exists()
+
+
+def test_struct_layouts_match_header():
+    assert C.sizeof(_lib.ExtrudeJob) == 48
+    assert C.sizeof(_lib.ReadoutLayer) == 56
+
+
+def _status(name, *args):
+    return getattr(_lib.load(), name)(*args)
+
+
+def test_argument_errors_before_device_work():
+    lib = _lib.load()
+    h = C.c_void_p()
+    assert _status("pt_grid_create", C.byref(h), 1, 0.1, 0, None) == _lib.PT_ERR_ARG
+    assert "ns must be" in _lib.last_error()
+    assert _status("pt_grid_create", C.byref(h), 64, -1.0, 0, None) == _lib.PT_ERR_ARG
+    assert _status("pt_grid_create", C.byref(h), 64, 0.1, 17, None) == _lib.PT_ERR_ARG
+    assert _status("pt_generate", None, 1, None, None, None, None, 0, 0, 0, 1, 1.0, 0, None,
+                   None, 0, None) == _lib.PT_ERR_ARG
+    assert _status("pt_readout", 0, 8, 8, 1, 1, None, None, 1.0, None, None) == _lib.PT_ERR_ARG
+    assert _status("pt_lgs_zoom", 1, 8, 8, 7, None, None, None, 1.0, None, None) == _lib.PT_ERR_ARG
+    assert _status("pt_rows_sample", 8, 8, 3, 0, 4, 0.0, None, None, None) == _lib.PT_ERR_ARG
+    assert _status("pt_extrude_rows", 0, 2, 8, 1, None, None, 0, None, None, None, 0,
+                   None) == _lib.PT_ERR_ARG
+    assert lib.pt_version() >= 100
+    with pytest.raises(ValueError, match="pt_grid_create"):
+        _lib.call("pt_grid_create", C.byref(h), 1, 0.1, 0, None)
+
+
+def test_workspace_queries_are_pure():
+    assert _lib.load().pt_extrude_workspace_bytes(100, 2, 9) > 100 * 3 * 9 * 4
+    assert _lib.load().pt_extrude_workspace_bytes(0, 2, 9) == 0
