@@ -757,6 +757,7 @@ extern "C" int pt_frames(const pt_grid* g, int L, const float* spectra, const fl
   cudaStream_t s = (cudaStream_t)stream;
   const int ch = image_chunk(ns), C = cols_per_cta(ns);
   const int J = per_layer ? 1 : L;
+  if (2 * J > kShiftDoubles) return fail(PT_ERR_UNSUPPORTED, "pt_frames: at most 896 layers");
   const size_t rs = frame_rows_smem(ns), cs = cols_smem(ns, C, P);
   if (int rc = set_smem(k_frame_rows, rs, "k_frame_rows")) return rc;
   if (int rc = set_smem(k_pair_cols, cs, "k_pair_cols")) return rc;
