@@ -1,0 +1,361 @@
+"""Benchmark: 9-layer 512^2 OPD frames/s (spectral frozen flow) and Monte-Carlo
+screens/s on the GB300, with the reference's CPU path timed beside it.
+
+Workload (one step): ``Atmosphere`` with 9 layers at h = [0, 0.5, 1, 2, 4, 8,
+12, 16, 20] km, Cn2 fractions [0.52, 0.10, 0.07, 0.06, 0.05, 0.06, 0.06, 0.05,
+0.03], winds U[5, 30] m/s with seeded directions, n = 512, D = 8 m,
+r0 = 0.157 m, L0 = 25 m, zenith 30 deg, 3 subharmonic levels, dt = 1 ms:
+2000 frames rendered into HBM. Secondary: ``Atmosphere.sample(64)`` at 512^2
+(MC screens/s). Synthetic seeded inputs throughout.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+N > 1 runs under torchrun: each rank renders its own, disjoint time window
+(replicas, weak scaling); rank 0 prints the JSON line with the max time over
+ranks. ``--impl reference`` times the reference's own CPU path (the float32
+NumPy/SciPy port in ``oracle/baseline.py``) on the host cores.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+HEIGHTS = [0, 500, 1000, 2000, 4000, 8000, 12000, 16000, 20000]
+FRACTIONS = [0.52, 0.10, 0.07, 0.06, 0.05, 0.06, 0.06, 0.05, 0.03]
+N_PIX, DIAM, R0, L0, ZENITH, LEVELS, DT = 512, 8.0, 0.157, 25.0, 30.0, 3, 1e-3
+FRAMES_PER_STEP = 2000
+MC_BATCH = 64
+WORKLOAD = ("spectral frozen flow: 9 layers, 512^2 pupil, D=8 m, r0=0.157 m, L0=25 m, "
+            "z=30 deg, 3 subharmonic levels, dt=1 ms, 2000 frames per step")
+METRIC = "9-layer 512^2 OPD frames/s"
+
+
+def layer_table(seed: int = 2024):
+    rng = np.random.default_rng(seed)
+    speeds = rng.uniform(5.0, 30.0, 9)
+    dirs = rng.uniform(0.0, 360.0, 9)
+    return list(zip(HEIGHTS, FRACTIONS, speeds, dirs))
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), float(d["bf16_tflops"]), "measured"
+    return 6800.0, 1900.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi SM clock / throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = Path(os.environ.get("TMPDIR", "/tmp")) / f"pt_clocks_{os.getpid()}.csv"
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        self.proc.wait(timeout=10)
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.path.read_text().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for name, flag in zip(names, parts[5:9]):
+                if flag.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_reference(frames: int, mc_count: int, budget_s: float = 12.0):
+    """Time the reference CPU path (float32 NumPy/SciPy port) on a bounded sample."""
+    import warnings
+
+    from oracle.baseline import ReferenceCPU
+
+    warnings.simplefilter("ignore")
+    tab = layer_table()
+    cos_z = np.cos(np.deg2rad(ZENITH))
+    frac = np.array(FRACTIONS) / np.sum(FRACTIONS)
+    r0_los = R0 * cos_z ** 0.6
+    r0s = [r0_los * f ** (-0.6) for f in frac]
+    vx = [v * np.cos(np.deg2rad(d)) for _, _, v, d in tab]
+    vy = [v * np.sin(np.deg2rad(d)) for _, _, v, d in tab]
+    alt = [h / cos_z for h, *_ in tab]
+    cores = len(os.sched_getaffinity(0))
+    ref = ReferenceCPU(N_PIX, N_PIX, DIAM / N_PIX, r0s, [L0] * 9, LEVELS, vx, vy, alt, 0,
+                       workers=-1)
+    for k in range(3):
+        ref.frame(k * DT)
+    t0 = time.perf_counter()
+    done = 0
+    while done < frames and time.perf_counter() - t0 < budget_s:
+        ref.frame(done * DT)
+        done += 1
+    fps = done / (time.perf_counter() - t0)
+    rng = np.random.default_rng(0)
+    ref.sample(mc_count, rng)
+    t0 = time.perf_counter()
+    drawn = 0
+    while drawn < 4 * mc_count and time.perf_counter() - t0 < budget_s / 2:
+        ref.sample(mc_count, rng)
+        drawn += mc_count
+    sps = drawn / (time.perf_counter() - t0)
+    return fps, sps, cores, done, drawn
+
+
+def run_reference(args, rank: int) -> None:
+    if rank != 0:
+        return
+    budget = 8.0
+    per_step_frames = max(1, min(FRAMES_PER_STEP, 200))
+    times = []
+    for s in range(args.warmup + args.steps):
+        fps, sps, cores, done, drawn = cpu_reference(per_step_frames, MC_BATCH, budget)
+        if s >= args.warmup:
+            times.append((fps, sps, done, drawn))
+    fps = statistics.median([t[0] for t in times])
+    sps = statistics.median([t[1] for t in times])
+    line = {
+        "impl": "reference", "metric": METRIC, "value": fps, "unit": "frames/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000.0 * FRAMES_PER_STEP / fps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD},
+        "mc_screens_per_s": sps,
+        "cpu_baseline": {"value": fps, "unit": "frames/s", "cores": cores, "kind": "port",
+                         "sample": f"{times[-1][2]} frames and {times[-1][3]} MC screens per "
+                                   "step (bounded ~8 s), float32 NumPy/SciPy port of "
+                                   "Atmosphere._integrate / PhaseScreen.generate, scipy "
+                                   "FFT workers=all cores"},
+        "e2e": {"value": fps, "unit": "frames/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank)
+        return
+
+    import torch
+
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+
+    import warnings
+
+    import pyturb_gb300 as G
+    from pyturb_gb300 import _lib
+
+    warnings.simplefilter("ignore")
+    dev = torch.device("cuda", torch.cuda.current_device())
+    layers = [G.Layer(h, f, v, d, L0) for h, f, v, d in layer_table()]
+    atm = G.Atmosphere(layers, r0=R0, zenith_angle=ZENITH, diameter=DIAM, n=N_PIX,
+                       subharmonics=LEVELS, seed=1000 + rank, frames_chunk=64)
+    out = torch.empty((FRAMES_PER_STEP, N_PIX, N_PIX), dtype=torch.float32, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)  # > 129 MB L2
+
+    # each rank renders its own time window: rank r, step s starts at
+    # (r * 1e6 + s * FRAMES_PER_STEP) * DT
+    def step_times(s: int) -> np.ndarray:
+        t0 = (rank * 1_000_000 + s * FRAMES_PER_STEP) * DT
+        return t0 + DT * np.arange(FRAMES_PER_STEP)
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    for s in range(args.warmup):
+        atm.render(step_times(s), out=out)
+    barrier()
+
+    stream = torch.cuda.current_stream()
+    clocks = Clocks(torch.cuda.current_device())
+    launches0 = _lib.launch_count()
+    _lib.prof_enable(True)
+    _lib.prof_report()  # clear
+    _lib.prof_enable(True)
+    clocks.start()
+    barrier()
+    wall0 = time.perf_counter()
+    events = []
+    for s in range(args.steps):
+        flush.fill_(s & 0xFF)  # evict L2 between steps (outside the step's events)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        atm.render(step_times(args.warmup + s), out=out)
+        e1.record(stream)
+        events.append((e0, e1))
+    barrier()
+    wall = time.perf_counter() - wall0
+    clk = clocks.stop()
+    prof = _lib.prof_report()
+    _lib.prof_enable(False)
+    launches = _lib.launch_count() - launches0
+    step_ms = [a.elapsed_time(b) for a, b in events]
+    total_ms = float(sum(step_ms))
+    if dist is not None:
+        t = torch.tensor([total_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    frames_total = world * args.steps * FRAMES_PER_STEP
+    value = frames_total / (total_ms / 1000.0)
+
+    # ---- end to end through the public API: frames() with every frame copied to pinned host
+    host = torch.empty((FRAMES_PER_STEP, N_PIX, N_PIX), dtype=torch.float32, pin_memory=True)
+    e2e_ms = []
+    for s in range(2):
+        atm.reset()
+        barrier()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        t0 = time.perf_counter()
+        e0.record(stream)
+        for i, (_t, frame) in enumerate(atm.frames(dt=DT, steps=FRAMES_PER_STEP)):
+            host[i].copy_(frame, non_blocking=True)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        e2e_ms.append(max(e0.elapsed_time(e1), 1000.0 * (time.perf_counter() - t0)))
+    e2e_step = min(e2e_ms[1:] or e2e_ms)
+    if dist is not None:
+        t = torch.tensor([e2e_step], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_step = float(t.item())
+    e2e = {"value": world * FRAMES_PER_STEP / (e2e_step / 1000.0), "unit": "frames/s",
+           "h2d_bytes_per_step": FRAMES_PER_STEP * 9 * 2 * 8,
+           "d2h_bytes_per_step": FRAMES_PER_STEP * N_PIX * N_PIX * 4,
+           "path": "Atmosphere.frames(dt, 2000) generator, each frame copied to pinned host "
+                   "memory; per-frame shifts travel as kernel parameters"}
+
+    # ---- Monte-Carlo screens/s: Atmosphere.sample(64) at 512^2
+    mc_out = None
+    for _ in range(3):
+        mc_out = atm.sample(MC_BATCH)
+    barrier()
+    reps = 20
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        mc_out = atm.sample(MC_BATCH)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    mc_sps = world * reps * MC_BATCH / (e0.elapsed_time(e1) / 1000.0)
+    mc_host = torch.empty((MC_BATCH, N_PIX, N_PIX), dtype=torch.float32, pin_memory=True)
+    t0 = time.perf_counter()
+    for _ in range(5):
+        mc_host.copy_(atm.sample(MC_BATCH), non_blocking=True)
+    torch.cuda.synchronize()
+    mc_e2e = world * 5 * MC_BATCH / (time.perf_counter() - t0)
+
+    # ---- roofline of the dominant kernel (live event timing over the timed region)
+    hbm, _tf, peak_kind = peaks()
+    top = max(prof.items(), key=lambda kv: kv[1][1]) if prof else ("none", (1, 1.0))
+    name, (nlaunch, kms) = top
+    ns, L = N_PIX, 9
+    frames_per_launch = FRAMES_PER_STEP * args.steps / max(1, nlaunch)
+    pairs = frames_per_launch / 2.0
+    # algorithmic DRAM bytes per launch ("Roofline accounting")
+    algo = {
+        "k_frame_rows": pairs * (L * ns * ns * 8 + ns * ns * 8),
+        "k_pair_cols": pairs * (ns * ns * 8 + 2 * N_PIX * N_PIX * 4),
+        "k_frame_phasors": frames_per_launch * L * ns * 2 * 8,
+    }.get(name, 0.0)
+    achieved = algo / (kms / nlaunch / 1000.0) / 1e9 if algo else None
+    roofline = {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": hbm,
+                "unit": "GB/s", "frac": (achieved / hbm) if achieved else None,
+                "traffic": None, "peak_source": f"MEASURED_PEAKS.json hbm_gbs ({peak_kind})",
+                "kernel_share": {k: round(v[1] / max(1e-9, sum(x[1] for x in prof.values())), 4)
+                                 for k, v in prof.items()},
+                "kernel_ms_per_launch": {k: v[1] / v[0] for k, v in prof.items()}}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD, "frames_per_step": FRAMES_PER_STEP,
+                   "l2": "flushed between steps by a 256 MB write outside the step events",
+                   "parallelism": f"replicas x{world} (disjoint time windows)",
+                   "noise": "in-kernel Philox4x32-10"},
+        "mc_screens_per_s": mc_sps,
+        "mc_e2e_screens_per_s": mc_e2e,
+        "e2e": e2e,
+        "gpu_launches": int(launches),
+        "roofline": roofline,
+        "clocks": clk,
+        "wall_s_timed_region": wall,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        fps, sps, cores, done, drawn = cpu_reference(200, MC_BATCH, 12.0)
+        line["cpu_baseline"] = {
+            "value": fps, "unit": "frames/s", "cores": cores, "kind": "port",
+            "mc_screens_per_s": sps,
+            "sample": f"{done} frames + {drawn} MC screens of the same workload (bounded "
+                      "~12 s), float32 NumPy/SciPy port of Atmosphere._integrate, scipy FFT "
+                      "workers=all cores"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -39,6 +39,13 @@ const char* pt_last_error(void);
 /* Number of kernels this library has launched since load (all threads). */
 uint64_t pt_launch_count(void);
 
+/* Per-kernel timing with CUDA events recorded on each launch's stream
+ * (no reference counterpart: measurement support). pt_prof_enable(1)
+ * starts recording, pt_prof_report() synchronises the device, writes one
+ * line "kernel launches total_ms" per kernel into buf and clears the log. */
+int pt_prof_enable(int on);
+int pt_prof_report(char* buf, size_t len);
+
 /* ------------------------------------------------------------------ grid plan
  * An ns x ns FFT grid with pixel_scale dx and n_levels subharmonic levels:
  * twiddles, the subharmonic sinusoid bases and their grid means. Mirrors the

@@ -66,6 +66,8 @@ SIGNATURES = {
     "pt_version": (i32, []),
     "pt_last_error": (C.c_char_p, []),
     "pt_launch_count": (u64, []),
+    "pt_prof_enable": (i32, [i32]),
+    "pt_prof_report": (i32, [C.c_char_p, sz]),
     "pt_grid_create": (i32, [C.POINTER(vp), i32, f64, i32, dptr]),
     "pt_grid_destroy": (i32, [vp]),
     "pt_grid_workspace_bytes": (sz, [vp, i32]),
@@ -117,6 +119,21 @@ def call(name: str, *args: Any) -> None:
 
 def launch_count() -> int:
     return int(load().pt_launch_count())
+
+
+def prof_enable(on: bool) -> None:
+    load().pt_prof_enable(1 if on else 0)
+
+
+def prof_report() -> dict:
+    """{kernel: (launches, total_ms)} since the last report (synchronises)."""
+    buf = C.create_string_buffer(1 << 16)
+    call("pt_prof_report", buf, len(buf))
+    out = {}
+    for line in buf.value.decode().splitlines():
+        name, count, ms = line.split()
+        out[name] = (int(count), float(ms))
+    return out
 
 
 def as_dptr(arr) -> Any:

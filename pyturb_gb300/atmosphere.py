@@ -411,13 +411,19 @@ class Atmosphere:
                 self._t = float(times[i]) + dt
             done += k
 
-    def render(self, times: Sequence[float], wavelength: Optional[float] = None):
-        """All frames at ``times`` in one call, ``(F, n, n)`` (spectral engine, frozen flow)."""
-        if self.engine != "spectral" or self._boiling:
-            raise ValueError("render() needs the spectral engine without boiling")
+    def render(self, times: Sequence[float], wavelength: Optional[float] = None, out=None):
+        """All on-axis frames at ``times`` in one call, ``(F, n, n)`` — each equal to
+        ``opd(t)`` (spectral engine, frozen flow, no LGS). ``out`` may be a
+        preallocated float32 CUDA tensor of that shape."""
+        if self.engine != "spectral" or self._boiling or self._lgs_mag is not None:
+            raise ValueError("render() needs the spectral engine without boiling or LGS")
         t = np.asarray(times, dtype=np.float64).reshape(-1)
-        return self._phase_frames(t, np.zeros_like(t), np.zeros_like(t),
-                                  self._scale(wavelength))
+        disp_x = self._vx[None, :] * t[:, None]
+        disp_y = self._vy[None, :] * t[:, None]
+        if not self._wrap_warned:
+            self._check_wrap(disp_x, disp_y)
+        return self._spec.frames(disp_x, disp_y, self.margin_pix, self.n,
+                                 self._scale(wavelength), out=out)
 
     def evolve(self, dt: float, wavelength: Optional[float] = None):
         """Advance the clock by ``dt`` and return the new OPD

@@ -19,6 +19,22 @@ int fail(int code, const std::string& msg);
 int check_cuda(cudaError_t e, const char* what);
 int check_launch(const char* what);
 
+// ---------------------------------------------------------------- profiling
+// Optional per-kernel timing with CUDA events recorded on the launching
+// stream (pt_prof_enable / pt_prof_report). Off by default: a disabled scope
+// costs one branch.
+class ProfScope {
+ public:
+  ProfScope(const char* name, cudaStream_t s);
+  ~ProfScope();
+
+ private:
+  const char* name_;
+  cudaStream_t s_;
+  cudaEvent_t a_;
+  bool on_;
+};
+
 // ---------------------------------------------------------------- complex
 __host__ __device__ __forceinline__ float2 cadd(float2 a, float2 b) {
   return make_float2(a.x + b.x, a.y + b.y);

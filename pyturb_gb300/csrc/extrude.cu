@@ -323,8 +323,11 @@ extern "C" int pt_extrude_rows(int W, int m, int cap, int G, const float* M, flo
         const int kslice = ((K + nsplit - 1) / nsplit + kTK - 1) / kTK * kTK;
         const int nz = (K + kslice - 1) / kslice;
         const float* Mg = M + (size_t)kv.first * W * K;
-        k_extrude_gemm<<<dim3((W + kTM - 1) / kTM, (J + kTJ - 1) / kTJ, nz), 256, 0, s>>>(
-            W, K, J, kslice, Mg, X, partial);
+        {
+          ProfScope ps("k_extrude_gemm", s);
+          k_extrude_gemm<<<dim3((W + kTM - 1) / kTM, (J + kTJ - 1) / kTJ, nz), 256, 0, s>>>(
+              W, K, J, kslice, Mg, X, partial);
+        }
         k_extrude_reduce<<<dim3((W + 255) / 256, J), 256, 0, s>>>(W, J, cap, nz, partial, jp, buf);
         count_launch_e(3);
         if (int rc = check_launch("pt_extrude_rows")) return rc;
@@ -363,6 +366,7 @@ extern "C" int pt_readout(int n, int W, int cap, int interp, int L, const pt_rea
   }
   cudaStream_t s = (cudaStream_t)stream;
   dim3 grid((n + 255) / 256, n);
+  ProfScope ps("k_readout", s);
   if (interp == 0) k_readout<2><<<grid, 256, 0, s>>>(n, W, cap, L, P, buf, scale, out);
   else if (interp == 1) k_readout<4><<<grid, 256, 0, s>>>(n, W, cap, L, P, buf, scale, out);
   else k_readout<6><<<grid, 256, 0, s>>>(n, W, cap, L, P, buf, scale, out);

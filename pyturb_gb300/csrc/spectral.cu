@@ -67,6 +67,7 @@ struct SpecWork {
   float* mean;     // (2 chunk)
   float2* px;      // (2 chunk, J, ns)
   float2* py;      // (2 chunk, J, ns)
+  float2* hn;      // (2 chunk, 2 ns) Hermitian parts on the Nyquist cross
   size_t bytes;
 };
 
@@ -87,6 +88,7 @@ static SpecWork carve(const pt_grid* g, int L, void* base) {
   w.mean = (float*)take((size_t)F * sizeof(float));
   w.px = (float2*)take((size_t)F * J * ns * sizeof(float2));
   w.py = (float2*)take((size_t)F * J * ns * sizeof(float2));
+  w.hn = (float2*)take((size_t)F * 2 * ns * sizeof(float2));
   w.bytes = off;
   return w;
 }
@@ -213,6 +215,137 @@ k_frame_rows(FftDesc d, const float2* __restrict__ tw, FrameRowArgs a, float2* _
     const int r = i / ns, ky = i % ns;
     const int kx = r == 0 ? kxa : kxb;
     work[((size_t)pair * ns + kx) * ns + ky] = res[r * vs + ky];
+  }
+}
+
+// Uniformly spaced frames (shift of frame f, layer l = s0_l + f delta_l):
+// only the Hermitian part Sh_l = (S_l(k) + conj S_l(-k)) / 2 of each layer
+// contributes to a real frame, and its phasor is a geometric sequence in f,
+//   H_f(k) = sum_l Sh_l(k) Q_l(k) R_l(k)^f,
+// so each thread keeps A_l = Sh_l Q_l R_l^f and R_l in registers and advances
+// a frame with one complex multiply-add per layer — no phasor tables. Anchors
+// (exact 64-bit fixed-point phases, u0 + f du mod 1) are re-taken every
+// kAnchor frames, bounding the float32 drift of the recurrence.
+// CTA = one row kx x kFramesPerCta frames; thread = one column ky; frame
+// pairs are packed as Y = H_f0 + i H_f1 and kPairsPerFft rows are transformed
+// together.
+constexpr int kMaxUniformLayers = 16;
+constexpr int kAnchor = 32;
+constexpr int kPairsPerFft = 4;
+
+struct UniformParams {
+  uint64_t ux0[kMaxUniformLayers], uy0[kMaxUniformLayers];  // frac(s0 df) of frame 0
+  uint64_t dux[kMaxUniformLayers], duy[kMaxUniformLayers];  // frac(delta df) per frame
+};
+
+__device__ __forceinline__ float2 phasor2(int kxs, int kys, uint64_t ux, uint64_t uy) {
+  return phasor_from_fixed((uint64_t)(int64_t)kxs * ux + (uint64_t)(int64_t)kys * uy);
+}
+
+// The phasor of the Nyquist index ns/2 is exp(-i pi ns u) on both k and -k
+// (fftfreq gives -ns/2 for it), so Q(-k) = conj Q(k) fails on the Nyquist
+// row and column and the shortcut through Sh does not hold there. This kernel
+// forms H_f(k) = (X_f(k) + conj X_f(-k)) / 2 exactly on that cross (element e:
+// e < ns is (ns/2, e), else (e - ns, ns/2)) for every frame of the chunk.
+__global__ void k_nyquist_h(int ns, const float2* __restrict__ spectra, int L, int F,
+                            UniformParams up, float2* __restrict__ hn) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  const int f = blockIdx.y;
+  if (e >= 2 * ns || f >= F) return;
+  const int kx = e < ns ? ns / 2 : e - ns;
+  const int ky = e < ns ? e : ns / 2;
+  const int nkx = (ns - kx) % ns, nky = (ns - ky) % ns;
+  const int a = signed_freq(kx, ns), b = signed_freq(ky, ns);
+  const int na = signed_freq(nkx, ns), nb = signed_freq(nky, ns);
+  float2 h = make_float2(0.f, 0.f);
+  for (int l = 0; l < L; ++l) {
+    const uint64_t ux = up.ux0[l] + (uint64_t)f * up.dux[l];
+    const uint64_t uy = up.uy0[l] + (uint64_t)f * up.duy[l];
+    const float2 x = cmul(spectra[((size_t)l * ns + kx) * ns + ky], phasor2(a, b, ux, uy));
+    const float2 y = cmul(spectra[((size_t)l * ns + nkx) * ns + nky], phasor2(na, nb, ux, uy));
+    h = cadd(h, make_float2(0.5f * (x.x + y.x), 0.5f * (x.y - y.y)));
+  }
+  hn[(size_t)f * 2 * ns + e] = h;
+}
+
+template <int LM, int E>
+__global__ void __launch_bounds__(512)
+k_frame_rows_uniform(FftDesc d, const float2* __restrict__ tw,
+                     const float2* __restrict__ spectra, int L, int F, UniformParams up,
+                     const float2* __restrict__ hn, float2* __restrict__ work) {
+  extern __shared__ float2 sm[];
+  const int ns = d.n;
+  const int kx = blockIdx.x;
+  const int fbeg = blockIdx.y * kAnchor;  // this CTA's frames [fbeg, fbeg + kAnchor)
+  const int vs = ns + 1;
+  float2* bufA = sm;
+  float2* bufB = sm + kPairsPerFft * vs;
+  float2* stw = sm + 2 * kPairsPerFft * vs;
+  for (int i = threadIdx.x; i < ns; i += blockDim.x) stw[i] = tw[i];
+  const int kxs = signed_freq(kx, ns), nkx = (ns - kx) % ns;
+  float2 A[E][LM], R[E][LM];
+#pragma unroll
+  for (int e = 0; e < E; ++e) {
+    const int ky = threadIdx.x + e * blockDim.x;
+    const bool live = ky < ns;
+    const int kys = live ? signed_freq(ky, ns) : 0, nky = live ? (ns - ky) % ns : 0;
+#pragma unroll
+    for (int l = 0; l < LM; ++l) {
+      A[e][l] = make_float2(0.f, 0.f);
+      R[e][l] = make_float2(1.f, 0.f);
+      if (l < L && live) {
+        const float2 s = spectra[((size_t)l * ns + kx) * ns + ky];
+        const float2 t = spectra[((size_t)l * ns + nkx) * ns + nky];
+        const float2 sh = make_float2(0.5f * (s.x + t.x), 0.5f * (s.y - t.y));
+        A[e][l] = cmul(sh, phasor2(kxs, kys, up.ux0[l] + (uint64_t)fbeg * up.dux[l],
+                                   up.uy0[l] + (uint64_t)fbeg * up.duy[l]));
+        R[e][l] = phasor2(kxs, kys, up.dux[l], up.duy[l]);
+      }
+    }
+  }
+  const int nfr = min(kAnchor, F - fbeg);
+  const int npairs = (nfr + 1) / 2;
+  for (int pb = 0; pb < npairs; pb += kPairsPerFft) {
+    const int np = min(kPairsPerFft, npairs - pb);
+    for (int p = 0; p < np; ++p) {
+      const bool two = 2 * (pb + p) + 1 < nfr;
+#pragma unroll
+      for (int e = 0; e < E; ++e) {
+        float2 h0a = make_float2(0.f, 0.f), h0b = h0a, h1a = h0a, h1b = h0a;
+#pragma unroll
+        for (int l = 0; l < LM; ++l) {
+          if (l & 1) h0b = cadd(h0b, A[e][l]);
+          else h0a = cadd(h0a, A[e][l]);
+          A[e][l] = cmul(A[e][l], R[e][l]);
+        }
+        if (two) {
+#pragma unroll
+          for (int l = 0; l < LM; ++l) {
+            if (l & 1) h1b = cadd(h1b, A[e][l]);
+            else h1a = cadd(h1a, A[e][l]);
+            A[e][l] = cmul(A[e][l], R[e][l]);
+          }
+        }
+        float2 h0 = cadd(h0a, h0b), h1 = cadd(h1a, h1b);
+        const int ky = threadIdx.x + e * blockDim.x;
+        const bool even = (ns & 1) == 0;
+        if (even && (kx == ns / 2 || ky == ns / 2) && ky < ns) {
+          const int el = kx == ns / 2 ? ky : ns + kx;
+          const int fa = fbeg + 2 * (pb + p);
+          h0 = hn[(size_t)fa * 2 * ns + el];
+          h1 = two ? hn[(size_t)(fa + 1) * 2 * ns + el] : make_float2(0.f, 0.f);
+        }
+        if (ky < ns) bufA[p * vs + ky] = make_float2(h0.x - h1.y, h0.y + h1.x);
+      }
+    }
+    __syncthreads();
+    float2* res = fft_smem(bufA, bufB, d, stw, np, vs, 1, false);
+    for (int i = threadIdx.x; i < np * ns; i += blockDim.x) {
+      const int p = i / ns, c = i % ns;
+      const int pair = fbeg / 2 + pb + p;
+      work[((size_t)pair * ns + kx) * ns + c] = res[p * vs + c];
+    }
+    __syncthreads();
   }
 }
 
@@ -391,42 +524,46 @@ struct FramePrepArgs {
   double df;
 };
 
+// One CTA per frame, one thread per (level, 3x3 cell): the per-layer phases
+// f_p . s are FP64 products reduced mod 1 (so the error does not grow with the
+// travel), the phasors and the layer sum are float32 (the reference's own
+// complex64 path), and the CTA reduces the grid mean of the low-order screen.
 __global__ void k_frame_coef(FramePrepArgs a, ShiftParams sp, int fbeg, int nf) {
-  const int fl = blockIdx.x * blockDim.x + threadIdx.x;
+  __shared__ double part[32];
+  const int fl = blockIdx.x;
   if (fl >= nf) return;
   const int f = fbeg + fl;
-  double mr = 0.0;
-  for (int p = 0; p < a.P; ++p) {
-    double sr[9], si[9];
-    for (int ij = 0; ij < 9; ++ij) sr[ij] = si[ij] = 0.0;
+  const int t = threadIdx.x;
+  double term = 0.0;
+  if (t < a.P * 9) {
+    const int p = t / 9, ij = t % 9, i = ij / 3, k = ij % 3;
+    const double fi = a.sh_freq[p * 3 + i], fk = a.sh_freq[p * 3 + k];
+    float2 acc = make_float2(0.f, 0.f);
     for (int j = 0; j < a.J; ++j) {
       const int l = a.per_layer ? a.frame0 + f : j;
       const double sx = sp.v[(fl * a.J + j) * 2];
       const double sy = sp.v[(fl * a.J + j) * 2 + 1];
-      double cxr[3], cxi[3], cyr[3], cyi[3];
-      for (int i = 0; i < 3; ++i) {
-        sincospi(2.0 * a.sh_freq[p * 3 + i] * sx, &cxi[i], &cxr[i]);
-        sincospi(2.0 * a.sh_freq[p * 3 + i] * sy, &cyi[i], &cyr[i]);
-      }
-      for (int i = 0; i < 3; ++i)
-        for (int k = 0; k < 3; ++k) {
-          const float2 c = a.sh_coef[(((size_t)p * a.L + l) * 3 + i) * 3 + k];
-          const double pr = cxr[i] * cyr[k] - cxi[i] * cyi[k];
-          const double pim = cxr[i] * cyi[k] + cxi[i] * cyr[k];
-          sr[i * 3 + k] += (double)c.x * pr - (double)c.y * pim;
-          si[i * 3 + k] += (double)c.x * pim + (double)c.y * pr;
-        }
+      double ph = fi * sx + fk * sy;
+      ph -= floor(ph);
+      float sn, cs;
+      sincospif(2.0f * (float)ph, &sn, &cs);
+      const float2 c = a.sh_coef[(((size_t)p * a.L + l) * 3 + i) * 3 + k];
+      acc = cfma(c, make_float2(cs, sn), acc);
     }
-    for (int ij = 0; ij < 9; ++ij) {
-      a.coef[((size_t)f * a.P + p) * 9 + ij] = make_float2((float)sr[ij], (float)si[ij]);
-      const int i = ij / 3, k = ij % 3;
-      const double bir = a.beta[(p * 3 + i) * 2], bii = a.beta[(p * 3 + i) * 2 + 1];
-      const double bkr = a.beta[(p * 3 + k) * 2], bki = a.beta[(p * 3 + k) * 2 + 1];
-      const double br = bir * bkr - bii * bki, bi = bir * bki + bii * bkr;
-      mr += sr[ij] * br - si[ij] * bi;
-    }
+    a.coef[((size_t)f * a.P + p) * 9 + ij] = acc;
+    const double bir = a.beta[(p * 3 + i) * 2], bii = a.beta[(p * 3 + i) * 2 + 1];
+    const double bkr = a.beta[(p * 3 + k) * 2], bki = a.beta[(p * 3 + k) * 2 + 1];
+    const double br = bir * bkr - bii * bki, bi = bir * bki + bii * bkr;
+    term = (double)acc.x * br - (double)acc.y * bi;
   }
-  a.mean[f] = (float)mr;
+  for (int o = 16; o > 0; o >>= 1) term += __shfl_down_sync(0xffffffffu, term, o);
+  if ((t & 31) == 0) part[t >> 5] = term;
+  __syncthreads();
+  if (t == 0) {
+    double m = 0.0;
+    for (int w = 0; w < (int)(blockDim.x + 31) / 32; ++w) m += part[w];
+    a.mean[f] = (float)m;
+  }
 }
 
 // px[f][j][k] = exp(2 pi i f_k sx[f][j]), f_k = k' df, phase wrapped exactly
@@ -549,6 +686,81 @@ static int check_grid(const pt_grid* g, const char* who) {
   return PT_OK;
 }
 
+// 64-bit binary fraction of frac(x), host side (matches phase_fixed on the device).
+static uint64_t host_fixed(double x) {
+  double f = x - std::floor(x);
+  double v = std::ldexp(f, 64);
+  if (!(v < 18446744073709551615.0)) return ~0ull;
+  return (uint64_t)v;
+}
+
+// Frames [f0, f0 + nf) of a layer-sum request are equally spaced in shift
+// (s_f = s_0 + f delta for every layer, to 1e-9 m + 1e-12 relative), on a grid
+// the register-recurrence kernel handles (ns <= 1024, L <= 16).
+static bool uniform_ok(const double* sx, const double* sy, int per_layer, int L, int f0, int nf,
+                       int ns) {
+  if (per_layer || nf < 2 || L > kMaxUniformLayers || ns > 1024) return false;
+  for (int l = 0; l < L; ++l) {
+    const double* v[2] = {sx, sy};
+    for (const double* a : v) {
+      const double s0 = a[(size_t)f0 * L + l];
+      const double d = (a[(size_t)(f0 + nf - 1) * L + l] - s0) / (nf - 1);
+      for (int f = 1; f < nf; ++f) {
+        const double sf = a[(size_t)(f0 + f) * L + l];
+        if (std::fabs(sf - (s0 + f * d)) > 1e-9 + 1e-12 * std::fabs(sf)) return false;
+      }
+    }
+  }
+  return true;
+}
+
+template <int LM>
+static int launch_uniform_t(const pt_grid* g, const float2* spectra, int L, int nf,
+                            const UniformParams& up, float2* hn, float2* img, cudaStream_t s) {
+  const int ns = g->ns;
+  if ((ns & 1) == 0) {
+    k_nyquist_h<<<dim3((2 * ns + 127) / 128, nf), 128, 0, s>>>(ns, spectra, L, nf, up, hn);
+    count_launch();
+  }
+  const size_t smem = (size_t)(2 * kPairsPerFft * (ns + 1) + ns) * sizeof(float2);
+  const dim3 grid(ns, (nf + kAnchor - 1) / kAnchor);
+  ProfScope ps("k_frame_rows_uniform", s);
+  if (ns <= 512) {
+    if (int rc = set_smem(k_frame_rows_uniform<LM, 1>, smem, "k_frame_rows_uniform")) return rc;
+    k_frame_rows_uniform<LM, 1><<<grid, ns, smem, s>>>(g->desc, g->tw, spectra, L, nf, up, hn,
+                                                       img);
+  } else {
+    if (int rc = set_smem(k_frame_rows_uniform<LM, 2>, smem, "k_frame_rows_uniform")) return rc;
+    k_frame_rows_uniform<LM, 2><<<grid, (ns + 1) / 2, smem, s>>>(g->desc, g->tw, spectra, L, nf,
+                                                                up, hn, img);
+  }
+  return PT_OK;
+}
+
+static int launch_uniform_rows(const pt_grid* g, const float2* spectra, int L, const double* sx,
+                               const double* sy, int f0, int nf, float2* hn, float2* img,
+                               cudaStream_t s) {
+  const double df = 1.0 / (g->ns * g->dx);
+  UniformParams up{};
+  for (int l = 0; l < L; ++l) {
+    const double x0 = sx[(size_t)f0 * L + l], y0 = sy[(size_t)f0 * L + l];
+    const double dx = (sx[(size_t)(f0 + nf - 1) * L + l] - x0) / (nf - 1);
+    const double dy = (sy[(size_t)(f0 + nf - 1) * L + l] - y0) / (nf - 1);
+    up.ux0[l] = host_fixed(x0 * df);
+    up.uy0[l] = host_fixed(y0 * df);
+    up.dux[l] = host_fixed(dx * df);
+    up.duy[l] = host_fixed(dy * df);
+  }
+  if (L <= 1) return launch_uniform_t<1>(g, spectra, L, nf, up, hn, img, s);
+  if (L <= 2) return launch_uniform_t<2>(g, spectra, L, nf, up, hn, img, s);
+  if (L <= 3) return launch_uniform_t<3>(g, spectra, L, nf, up, hn, img, s);
+  if (L <= 4) return launch_uniform_t<4>(g, spectra, L, nf, up, hn, img, s);
+  if (L <= 6) return launch_uniform_t<6>(g, spectra, L, nf, up, hn, img, s);
+  if (L <= 9) return launch_uniform_t<9>(g, spectra, L, nf, up, hn, img, s);
+  if (L <= 12) return launch_uniform_t<12>(g, spectra, L, nf, up, hn, img, s);
+  return launch_uniform_t<16>(g, spectra, L, nf, up, hn, img, s);
+}
+
 }  // namespace pt
 
 using namespace pt;
@@ -642,7 +854,8 @@ extern "C" int pt_ifft2(const pt_grid* g, const float* in, float* out, int batch
     const int nb = std::min(ch, batch - b0);
     const float2* src = (const float2*)in + (size_t)b0 * ns * ns;
     float2* dst = (float2*)out + (size_t)b0 * ns * ns;
-    k_rows<<<dim3((ns + rpc - 1) / rpc, nb), kThreads, rs, s>>>(g->desc, g->tw, rpc, src, 0, none, w.img);
+    { ProfScope ps("k_rows", s); k_rows<<<dim3((ns + rpc - 1) / rpc, nb), kThreads, rs, s>>>(g->desc, g->tw, rpc, src, 0, none, w.img); }
+    ProfScope ps("k_plain_cols", s);
     k_plain_cols<<<dim3((ns + C - 1) / C, nb), kThreads, cs, s>>>(g->desc, g->tw, w.img, C, dst);
     count_launch(2);
     if (int rc = check_launch("pt_ifft2")) return rc;
@@ -673,7 +886,10 @@ extern "C" int pt_generate(const pt_grid* g, int count, const float* amplitude,
   for (int b0 = 0; b0 < n_fft; b0 += ch) {
     const int nb = std::min(ch, n_fft - b0);
     GenRowArgs ga{amplitude, noise, n_fft, b0, seed, call};
-    k_rows<<<dim3((ns + rpc - 1) / rpc, nb), kThreads, rs, s>>>(g->desc, g->tw, rpc, nullptr, 1, ga, w.img);
+    {
+      ProfScope ps("k_rows", s);
+      k_rows<<<dim3((ns + rpc - 1) / rpc, nb), kThreads, rs, s>>>(g->desc, g->tw, rpc, nullptr, 1, ga, w.img);
+    }
     count_launch();
     PairStore st{};
     st.out = out;
@@ -706,7 +922,10 @@ extern "C" int pt_generate(const pt_grid* g, int count, const float* amplitude,
         count_launch();
       }
     }
-    k_pair_cols<<<dim3((ns + C - 1) / C, nb), kThreads, cs, s>>>(g->desc, g->tw, w.img, C, b0, st);
+    {
+      ProfScope ps("k_pair_cols", s);
+      k_pair_cols<<<dim3((ns + C - 1) / C, nb), kThreads, cs, s>>>(g->desc, g->tw, w.img, C, b0, st);
+    }
     count_launch();
     if (int rc = check_launch("pt_generate")) return rc;
   }
@@ -793,14 +1012,23 @@ extern "C" int pt_frames(const pt_grid* g, int L, const float* spectra, const fl
           sp.v[(f * J + j) * 2 + 1] = sy[src];
         }
       if (P > 0) {
-        k_frame_coef<<<(nb + 63) / 64, 64, 0, s>>>(pa, sp, fb, nb);
+        k_frame_coef<<<nb, 32 * ((P * 9 + 31) / 32), 0, s>>>(pa, sp, fb, nb);
         count_launch();
       }
+      if (uniform_ok(sx, sy, per_layer, L, f0, nf, ns)) continue;  // no phasor tables needed
+      ProfScope ps("k_frame_phasors", s);
       k_frame_phasors<<<dim3((ns + 255) / 256, nb * J), 256, 0, s>>>(pa, sp, fb);
       count_launch();
     }
-    FrameRowArgs fa{(const float2*)spectra, w.px, w.py, J, nf, f0, per_layer};
-    k_frame_rows<<<dim3(ns / 2 + 1, npair), kThreads, rs, s>>>(g->desc, g->tw, fa, w.img);
+    if (uniform_ok(sx, sy, per_layer, L, f0, nf, ns)) {
+      if (int rc = launch_uniform_rows(g, (const float2*)spectra, L, sx, sy, f0, nf, w.hn, w.img,
+                                       s))
+        return rc;
+    } else {
+      FrameRowArgs fa{(const float2*)spectra, w.px, w.py, J, nf, f0, per_layer};
+      ProfScope ps("k_frame_rows", s);
+      k_frame_rows<<<dim3(ns / 2 + 1, npair), kThreads, rs, s>>>(g->desc, g->tw, fa, w.img);
+    }
     count_launch();
     PairStore st{};
     st.out = out + (size_t)f0 * n_out * n_out;
@@ -820,7 +1048,10 @@ extern "C" int pt_frames(const pt_grid* g, int L, const float* spectra, const fl
     st.mean = w.mean;
     st.basis = g->basis;
     st.P = P;
-    k_pair_cols<<<dim3((ns + C - 1) / C, npair), kThreads, cs, s>>>(g->desc, g->tw, w.img, C, 0, st);
+    {
+      ProfScope ps("k_pair_cols", s);
+      k_pair_cols<<<dim3((ns + C - 1) / C, npair), kThreads, cs, s>>>(g->desc, g->tw, w.img, C, 0, st);
+    }
     count_launch();
     if (int rc = check_launch("pt_frames")) return rc;
   }

@@ -73,6 +73,27 @@ def test_frames_config2_vs_oracle_long_run():
         assert err < TOL, (t, err)
 
 
+def test_uniform_chunk_recurrence_vs_oracle():
+    """Equally spaced frames take the register-recurrence kernel: check the
+    first, anchor-boundary and last frames of full and ragged 64-frame chunks
+    against the float64 oracle."""
+    import oracle
+    import pyturb_gb300 as G
+    from pyturb_gb300.backend import to_numpy
+
+    warnings.simplefilter("ignore")
+    lys = _config2_layers(3)
+    kw = dict(r0=0.157, zenith_angle=30.0, diameter=8.0, n=512, subharmonics=3, seed=9)
+    a = G.Atmosphere([G.Layer(l.altitude, l.cn2_fraction, l.wind_speed, l.wind_direction,
+                              l.L0) for l in lys], host_noise=np.random.default_rng, **kw)
+    o = oracle.OracleAtmosphere(lys, **kw)
+    times = 1.5 + 1e-3 * np.arange(64 + 37)  # one full chunk and one ragged (odd) chunk
+    got = to_numpy(a.render(times))
+    for k in (0, 1, 31, 32, 33, 63, 64, 95, 96, 100):
+        err = cases.rel_l2(got[k], o.opd(times[k]))
+        assert err < TOL, (k, err)
+
+
 def test_frames_generator_equals_render_and_opd():
     import pyturb_gb300 as G
     from pyturb_gb300.backend import to_numpy
