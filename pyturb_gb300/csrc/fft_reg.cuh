@@ -1,0 +1,112 @@
+// Register-resident Stockham FFT for power-of-two sizes N in [8, 4096]
+// (inverse sign, unnormalised, as fft.cuh).
+//
+// A transform is done by a team of T = N / 8 threads; thread j holds the
+// eight elements at positions j + T i (i = 0..7) in registers. Every stage
+// reads that same pattern, so a stage is: twiddle + radix-R butterflies in
+// registers, then (except after the last stage) one exchange through shared
+// memory to the Stockham destinations. Shared indices are padded by one slot
+// per eight (p + p/8), which makes both the strided first-stage writes and
+// the contiguous reads bank-conflict free for 64-bit accesses. All radices,
+// strides and index arithmetic are compile-time constants.
+#pragma once
+
+#include "fft.cuh"
+
+namespace pt {
+
+__host__ __device__ constexpr int fft_pad(int p) { return p + (p >> 3); }
+__host__ __device__ constexpr int fft_padded(int n) { return n + (n >> 3); }
+
+// radix of stage s for N = 8^a * r (r in {1, 2, 4}): all 8s first, the
+// remainder last
+template <int N>
+struct Pow2Plan {
+  static constexpr int log2n = (N <= 1) ? 0 : 1 + Pow2Plan<N / 2>::log2n;
+  static constexpr int n8 = log2n / 3;
+  static constexpr int rem = log2n % 3;  // 0, 1 or 2
+  static constexpr int stages = n8 + (rem ? 1 : 0);
+  __host__ __device__ static constexpr int radix(int s) { return s < n8 ? 8 : (rem == 1 ? 2 : 4); }
+};
+template <>
+struct Pow2Plan<1> {
+  static constexpr int log2n = 0, n8 = 0, rem = 0, stages = 0;
+  __host__ __device__ static constexpr int radix(int) { return 1; }
+};
+
+template <int N>
+struct is_pow2_fft {
+  static constexpr bool value = N >= 8 && N <= 4096 && (N & (N - 1)) == 0;
+};
+
+// Twiddle, butterflies of one stage on the thread's registers (in place:
+// output q of the butterfly in register slot i0 + (8/R) q).
+template <int N, int R, int Ns>
+__device__ __forceinline__ void reg_stage(float2 (&x)[8], int j, const float2* __restrict__ tw) {
+  constexpr int T = N / 8;
+  constexpr int B = 8 / R;                // butterflies per thread
+  constexpr int twstep = N / (Ns * R);
+#pragma unroll
+  for (int i0 = 0; i0 < B; ++i0) {
+    const int b = j + T * i0;  // butterfly index (< N / R)
+    const int jm = b & (Ns - 1);
+    float2 v[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[r] = x[i0 + B * r];
+    if (Ns > 1) {
+#pragma unroll
+      for (int r = 1; r < R; ++r) v[r] = cmul(v[r], tw[(r * jm * twstep) & (N - 1)]);
+    }
+    if (R == 8) bfly8(v);
+    else if (R == 4) bfly4(v);
+    else bfly2(v);
+#pragma unroll
+    for (int q = 0; q < R; ++q) x[i0 + B * q] = v[q];
+  }
+}
+
+// Write the stage outputs to their Stockham destinations (padded).
+template <int N, int R, int Ns>
+__device__ __forceinline__ void reg_scatter(const float2 (&x)[8], int j, float2* s) {
+  constexpr int T = N / 8;
+  constexpr int B = 8 / R;
+#pragma unroll
+  for (int i0 = 0; i0 < B; ++i0) {
+    const int b = j + T * i0;
+    const int idxD = (b / Ns) * Ns * R + (b & (Ns - 1));
+#pragma unroll
+    for (int q = 0; q < R; ++q) s[fft_pad(idxD + q * Ns)] = x[i0 + B * q];
+  }
+}
+
+__device__ __forceinline__ void reg_gather8(float2 (&x)[8], int j, int T, const float2* s) {
+#pragma unroll
+  for (int i = 0; i < 8; ++i) x[i] = s[fft_pad(j + T * i)];
+}
+
+template <int N, int S, int Ns>
+struct RegStages {
+  // run stages S.. ; x holds the inputs of stage S at positions j + T i
+  static __device__ __forceinline__ void run(float2 (&x)[8], int j, const float2* tw, float2* s) {
+    constexpr int R = Pow2Plan<N>::radix(S);
+    reg_stage<N, R, Ns>(x, j, tw);
+    if constexpr (S + 1 < Pow2Plan<N>::stages) {
+      reg_scatter<N, R, Ns>(x, j, s);
+      __syncthreads();
+      reg_gather8(x, j, N / 8, s);
+      __syncthreads();
+      RegStages<N, S + 1, Ns * R>::run(x, j, tw, s);
+    }
+  }
+};
+
+// Full transform of the thread's team. x in: element j + T i of the input;
+// x out: element j + T i of the output. `s` is this team's padded scratch
+// (fft_padded(N) float2); tw the N-entry twiddle table exp(+2 pi i k / N).
+// Every thread of the CTA must call this (it synchronises the CTA).
+template <int N>
+__device__ __forceinline__ void reg_fft(float2 (&x)[8], int j, const float2* tw, float2* s) {
+  RegStages<N, 0, 1>::run(x, j, tw, s);
+}
+
+}  // namespace pt
