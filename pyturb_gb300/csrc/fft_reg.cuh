@@ -5,18 +5,40 @@
 // eight elements at positions j + T i (i = 0..7) in registers. Every stage
 // reads that same pattern, so a stage is: twiddle + radix-R butterflies in
 // registers, then (except after the last stage) one exchange through shared
-// memory to the Stockham destinations. Shared indices are padded by one slot
-// per eight (p + p/8), which makes both the strided first-stage writes and
-// the contiguous reads bank-conflict free for 64-bit accesses. All radices,
-// strides and index arithmetic are compile-time constants.
+// memory to the Stockham destinations. All radices, strides and index
+// arithmetic are compile-time constants.
+//
+// Shared layouts (a functor maps element p of the team's vector to a float2
+// slot) are XOR swizzles, bijective because every key bit that is itself
+// modified depends only on higher, unmodified bits, and chosen so that every
+// gather and every stage's scatter is free of bank conflicts for 64-bit
+// accesses (checked by enumerating each warp's addresses for N = 64..1024):
+//   RowLayout: teams are consecutive threads of one vector, vector v at
+//     base + v (N + 8), slot p ^ ((p >> 3) & 15);
+//   ColLayout: C vectors interleaved, lane c of a warp on vector c, slot
+//     (p ^ ((p >> 3) & 3)) C + c.
 #pragma once
 
 #include "fft.cuh"
 
 namespace pt {
 
-__host__ __device__ constexpr int fft_pad(int p) { return p + (p >> 3); }
-__host__ __device__ constexpr int fft_padded(int n) { return n + (n >> 3); }
+__host__ __device__ constexpr int fft_padded(int n) { return n + 8; }
+
+struct RowLayout {
+  float2* base;
+  __device__ __forceinline__ float2& operator[](int p) const {
+    return base[p ^ ((p >> 3) & 15)];
+  }
+};
+
+template <int C>
+struct ColLayout {
+  float2* base;  // already offset by the lane's column c
+  __device__ __forceinline__ float2& operator[](int p) const {
+    return base[(p ^ ((p >> 3) & 3)) * C];
+  }
+};
 
 // radix of stage s for N = 8^a * r (r in {1, 2, 4}): all 8s first, the
 // remainder last
@@ -65,9 +87,9 @@ __device__ __forceinline__ void reg_stage(float2 (&x)[8], int j, const float2* _
   }
 }
 
-// Write the stage outputs to their Stockham destinations (padded).
-template <int N, int R, int Ns>
-__device__ __forceinline__ void reg_scatter(const float2 (&x)[8], int j, float2* s) {
+// Write the stage outputs to their Stockham destinations.
+template <int N, int R, int Ns, class Lay>
+__device__ __forceinline__ void reg_scatter(const float2 (&x)[8], int j, const Lay& s) {
   constexpr int T = N / 8;
   constexpr int B = 8 / R;
 #pragma unroll
@@ -75,38 +97,42 @@ __device__ __forceinline__ void reg_scatter(const float2 (&x)[8], int j, float2*
     const int b = j + T * i0;
     const int idxD = (b / Ns) * Ns * R + (b & (Ns - 1));
 #pragma unroll
-    for (int q = 0; q < R; ++q) s[fft_pad(idxD + q * Ns)] = x[i0 + B * q];
+    for (int q = 0; q < R; ++q) s[idxD + q * Ns] = x[i0 + B * q];
   }
 }
 
-__device__ __forceinline__ void reg_gather8(float2 (&x)[8], int j, int T, const float2* s) {
+template <int N, class Lay>
+__device__ __forceinline__ void reg_gather8(float2 (&x)[8], int j, const Lay& s) {
 #pragma unroll
-  for (int i = 0; i < 8; ++i) x[i] = s[fft_pad(j + T * i)];
+  for (int i = 0; i < 8; ++i) x[i] = s[j + (N / 8) * i];
 }
 
-template <int N, int S, int Ns>
+template <int N, int S, int Ns, class Lay>
 struct RegStages {
   // run stages S.. ; x holds the inputs of stage S at positions j + T i
-  static __device__ __forceinline__ void run(float2 (&x)[8], int j, const float2* tw, float2* s) {
+  static __device__ __forceinline__ void run(float2 (&x)[8], int j, const float2* tw,
+                                             const Lay& s) {
     constexpr int R = Pow2Plan<N>::radix(S);
     reg_stage<N, R, Ns>(x, j, tw);
     if constexpr (S + 1 < Pow2Plan<N>::stages) {
       reg_scatter<N, R, Ns>(x, j, s);
       __syncthreads();
-      reg_gather8(x, j, N / 8, s);
+      reg_gather8<N>(x, j, s);
       __syncthreads();
-      RegStages<N, S + 1, Ns * R>::run(x, j, tw, s);
+      RegStages<N, S + 1, Ns * R, Lay>::run(x, j, tw, s);
     }
   }
 };
 
 // Full transform of the thread's team. x in: element j + T i of the input;
-// x out: element j + T i of the output. `s` is this team's padded scratch
-// (fft_padded(N) float2); tw the N-entry twiddle table exp(+2 pi i k / N).
-// Every thread of the CTA must call this (it synchronises the CTA).
-template <int N>
-__device__ __forceinline__ void reg_fft(float2 (&x)[8], int j, const float2* tw, float2* s) {
-  RegStages<N, 0, 1>::run(x, j, tw, s);
+// x out: element j + T i of the output. `s` addresses this team's scratch
+// vector through its layout; tw is the N-entry twiddle table
+// exp(+2 pi i k / N). Every thread of the CTA must call this (it
+// synchronises the CTA), and the caller must synchronise between its own
+// last read of `s` and this call.
+template <int N, class Lay>
+__device__ __forceinline__ void reg_fft(float2 (&x)[8], int j, const float2* tw, const Lay& s) {
+  RegStages<N, 0, 1, Lay>::run(x, j, tw, s);
 }
 
 }  // namespace pt

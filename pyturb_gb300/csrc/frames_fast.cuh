@@ -1,0 +1,339 @@
+// Power-of-two fast path of the spectral passes, included by spectral.cu
+// inside namespace pt after the shared argument structs: the register FFT of
+// fft_reg.cuh with bank-conflict-free swizzled layouts, and the frame
+// synthesis with packed float32 pairs (fma.rn.f32x2 / mul / add on two
+// layers at once).
+#pragma once
+
+template <int N>
+struct RegCfg {
+  static constexpr int T = N / 8;
+  static constexpr int NV0 = (512 / T) < 1 ? 1 : (512 / T);
+  static constexpr int NV = NV0 < N ? NV0 : N;  // transforms (rows) per CTA
+  static constexpr int C = NV;                  // columns per CTA
+  static constexpr int THREADS = NV * T;
+};
+
+__device__ __forceinline__ void load_tw(float2* stw, const float2* tw, int n) {
+  for (int i = threadIdx.x; i < n; i += blockDim.x) stw[i] = tw[i];
+}
+
+// ------------------------------------------------------------------ packed f32x2
+typedef unsigned long long f2x;
+__device__ __forceinline__ f2x pk2(float lo, float hi) {
+  f2x r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+  return r;
+}
+__device__ __forceinline__ void upk2(f2x v, float& lo, float& hi) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ f2x fma2(f2x a, f2x b, f2x c) {
+  f2x d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
+}
+__device__ __forceinline__ f2x mul2(f2x a, f2x b) {
+  f2x d;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f2x add2(f2x a, f2x b) {
+  f2x d;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+
+// ------------------------------------------------------------------ rows
+// plain complex input (pt_ifft2) or generate's coloured noise
+template <int N>
+__global__ void __launch_bounds__(RegCfg<N>::THREADS)
+k_rows_reg(const float2* __restrict__ tw, const float2* __restrict__ in, int gen, GenRowArgs ga,
+           float2* __restrict__ work) {
+  constexpr int T = RegCfg<N>::T, NV = RegCfg<N>::NV;
+  extern __shared__ float2 sm[];
+  float2* stw = sm;
+  const int v = threadIdx.x / T, j = threadIdx.x % T;
+  const RowLayout s{sm + N + v * fft_padded(N)};
+  load_tw(stw, tw, N);
+  const int kx = blockIdx.x * NV + v;
+  const int img = blockIdx.y;
+  const bool ok = kx < N;
+  float2 x[8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const int ky = j + T * i;
+    float2 val = make_float2(0.f, 0.f);
+    if (ok) {
+      if (gen) {
+        const size_t e = ((size_t)(ga.img0 + img) * N + kx) * N + ky;
+        float2 z;
+        if (ga.noise) {
+          const size_t plane = (size_t)ga.n_fft * N * N;
+          z = make_float2(ga.noise[e], ga.noise[plane + e]);
+        } else {
+          z = philox_cnormal(ga.seed, e, ga.call, kDomainScreen);
+        }
+        const float amp = ga.amplitude[(size_t)kx * N + ky];
+        val = make_float2(z.x * amp, z.y * amp);
+      } else {
+        val = in[((size_t)img * N + kx) * N + ky];
+      }
+    }
+    x[i] = val;
+  }
+  __syncthreads();  // twiddles loaded
+  reg_fft<N>(x, j, stw, s);
+  if (ok) {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) work[((size_t)img * N + kx) * N + j + T * i] = x[i];
+  }
+}
+
+// ------------------------------------------------------------------ columns
+template <int N>
+__global__ void __launch_bounds__(RegCfg<N>::THREADS)
+k_plain_cols_reg(const float2* __restrict__ tw, const float2* __restrict__ work,
+                 float2* __restrict__ out) {
+  constexpr int T = RegCfg<N>::T, C = RegCfg<N>::C;
+  extern __shared__ float2 sm[];
+  float2* stw = sm;
+  const int c = threadIdx.x % C, j = threadIdx.x / C;
+  const ColLayout<C> s{sm + N + c};
+  load_tw(stw, tw, N);
+  const int y = blockIdx.x * C + c;
+  const int img = blockIdx.y;
+  const bool ok = y < N;
+  float2 x[8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+    x[i] = ok ? work[((size_t)img * N + j + T * i) * N + y] : make_float2(0.f, 0.f);
+  __syncthreads();
+  reg_fft<N>(x, j, stw, s);
+  if (ok) {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) out[((size_t)img * N + j + T * i) * N + y] = x[i];
+  }
+}
+
+// Columns with the paired real epilogue (generate and frames). With the
+// reference's symmetric subharmonic frequencies {-a, 0, +a} the bases obey
+// b1 = 1 and b2 = conj(b0), so the low-order screen of one output is
+//   K + sum_p (Re b0_p(x) U_p + Im b0_p(x) W_p),
+//   K = sum_p Re m1_p - mean, U_p = Re(m0_p + m2_p), W_p = Im(m2_p - m0_p)
+// with m_pi(y) = sum_j coef_pij b_pj(y): 2P FMAs per element and output.
+template <int N>
+__global__ void __launch_bounds__(RegCfg<N>::THREADS)
+k_pair_cols_reg(const float2* __restrict__ tw, const float2* __restrict__ work, int pair0,
+                PairStore st) {
+  constexpr int T = RegCfg<N>::T, C = RegCfg<N>::C;
+  extern __shared__ float2 sm[];
+  float2* stw = sm;
+  float2* buf = sm + N;             // N * C, column-interleaved
+  float2* mtab = buf + N * C;       // (2, 3P, C) or (2, P, C) (U, W) + (2, C) (K, 0)
+  const int c = threadIdx.x % C, j = threadIdx.x / C;
+  const ColLayout<C> s{buf + c};
+  load_tw(stw, tw, N);
+  const int y = blockIdx.x * C + c;
+  const int pl = blockIdx.y;
+  const int pair = pair0 + pl;
+  const bool ok = y < N;
+  const int img_re = pair * st.re_mul + st.re_add;
+  const int img_im = pair * st.im_mul + st.im_add;
+  const bool do_re = img_re < st.count, do_im = img_im < st.count;
+  const int row_re = pl * st.crow_mul + st.crow_re, row_im = pl * st.crow_mul + st.crow_im;
+  const int P = st.P;
+  // m[o][p*3+i][c] = sum_j coef[o][p][i][j] basis[p][j][y]
+  for (int i = threadIdx.x; i < 2 * 3 * P * C; i += blockDim.x) {
+    const int cc = i % C;
+    const int pi = (i / C) % (3 * P);
+    const int o = i / (C * 3 * P);
+    const bool take = o == 0 ? do_re : do_im;
+    const int row = o == 0 ? row_re : row_im;
+    const int yy = blockIdx.x * C + cc;
+    float2 m = make_float2(0.f, 0.f);
+    if (take && yy < N) {
+      const int p = pi / 3, ii = pi % 3;
+      const float2* cf = st.coef + ((size_t)row * P + p) * 9 + ii * 3;
+#pragma unroll
+      for (int jj = 0; jj < 3; ++jj) m = cfma(cf[jj], st.basis[((size_t)p * 3 + jj) * N + yy], m);
+    }
+    mtab[i] = m;
+  }
+  float2 x[8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+    x[i] = ok ? work[((size_t)pl * N + j + T * i) * N + y] : make_float2(0.f, 0.f);
+  __syncthreads();
+  // per-column symmetric-basis constants, read by this thread only
+  float k0 = 0.f, k1 = 0.f;
+  if (st.sym) {
+    for (int p = 0; p < P; ++p) {
+      k0 += mtab[(0 * 3 * P + 3 * p + 1) * C + c].x;
+      k1 += mtab[(1 * 3 * P + 3 * p + 1) * C + c].x;
+    }
+    if (P > 0 && do_re) k0 -= st.mean[row_re];
+    if (P > 0 && do_im) k1 -= st.mean[row_im];
+  }
+  reg_fft<N>(x, j, stw, s);
+  if (!ok) return;
+  const size_t plane = (size_t)st.n_out * st.n_out;
+  const int yo = y - st.crop;
+  if (yo < 0 || yo >= st.n_out) return;
+  const float mre = (P > 0 && do_re) ? st.mean[row_re] : 0.f;
+  const float mim = (P > 0 && do_im) ? st.mean[row_im] : 0.f;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const int xr = j + T * i;
+    const int xo = xr - st.crop;
+    if (xo < 0 || xo >= st.n_out) continue;
+    float lre, lim;
+    if (st.sym) {
+      lre = k0;
+      lim = k1;
+      for (int p = 0; p < P; ++p) {
+        const float2 b = st.basis[(size_t)(3 * p) * N + xr];
+        const float2 m00 = mtab[(0 * 3 * P + 3 * p) * C + c], m02 = mtab[(0 * 3 * P + 3 * p + 2) * C + c];
+        const float2 m10 = mtab[(1 * 3 * P + 3 * p) * C + c], m12 = mtab[(1 * 3 * P + 3 * p + 2) * C + c];
+        lre = fmaf(b.x, m00.x + m02.x, fmaf(b.y, m02.y - m00.y, lre));
+        lim = fmaf(b.x, m10.x + m12.x, fmaf(b.y, m12.y - m10.y, lim));
+      }
+    } else {
+      lre = -mre;
+      lim = -mim;
+      for (int pi = 0; pi < 3 * P; ++pi) {
+        const float2 b = st.basis[(size_t)pi * N + xr];
+        const float2 m0 = mtab[(0 * 3 * P + pi) * C + c];
+        const float2 m1 = mtab[(1 * 3 * P + pi) * C + c];
+        lre = fmaf(b.x, m0.x, fmaf(-b.y, m0.y, lre));
+        lim = fmaf(b.x, m1.x, fmaf(-b.y, m1.y, lim));
+      }
+    }
+    const size_t o = (size_t)xo * st.n_out + yo;
+    if (do_re) {
+      const float val = st.scale * (x[i].x + lre);
+      float* dst = st.out + (size_t)img_re * plane + o;
+      *dst = st.accumulate ? *dst + val : val;
+    }
+    if (do_im) {
+      const float val = st.scale * (x[i].y + lim);
+      float* dst = st.out + (size_t)img_im * plane + o;
+      *dst = st.accumulate ? *dst + val : val;
+    }
+  }
+}
+
+// ------------------------------------------------------------------ uniform frames
+// Fused synthesis + row transform. Threads first own columns (E each) and
+// advance the layer recurrence two layers per packed register pair, writing
+// NV pair rows into shared memory; then NV teams transform those rows.
+template <int LM, int N>
+__global__ void __launch_bounds__(N < 512 ? N : 512)
+k_frame_rows_uniform_reg(const float2* __restrict__ tw, const float2* __restrict__ spectra,
+                         int L, int F, UniformParams up, const float2* __restrict__ hn,
+                         float2* __restrict__ work) {
+  constexpr int THREADS = N < 512 ? N : 512;
+  constexpr int E = N / THREADS;  // columns per thread
+  constexpr int T = N / 8;
+  constexpr int NV = THREADS / T;  // pair rows per batch
+  constexpr int LP = (LM + 1) / 2;  // packed layer pairs
+  extern __shared__ float2 sm[];
+  float2* stw = sm;
+  float2* rows = sm + N;  // NV * fft_padded(N)
+  load_tw(stw, tw, N);
+  const int kx = blockIdx.x;
+  const int fbeg = blockIdx.y * kAnchor;
+  const int kxs = signed_freq(kx, N), nkx = (N - kx) & (N - 1);
+  // packed state: lanes (layer 2q, layer 2q+1)
+  f2x Ax[E][LP], Ay[E][LP], Rx[E][LP], Ry[E][LP], NRy[E][LP];
+#pragma unroll
+  for (int e = 0; e < E; ++e) {
+    const int ky = threadIdx.x + e * THREADS;
+    const int kys = signed_freq(ky, N), nky = (N - ky) & (N - 1);
+#pragma unroll
+    for (int q = 0; q < LP; ++q) {
+      float ax[2], ay[2], rx[2], ry[2];
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int l = 2 * q + h;
+        ax[h] = ay[h] = ry[h] = 0.f;
+        rx[h] = 1.f;
+        if (l < LM && l < L) {
+          const float2 sa = spectra[((size_t)l * N + kx) * N + ky];
+          const float2 sb = spectra[((size_t)l * N + nkx) * N + nky];
+          const float2 sh = make_float2(0.5f * (sa.x + sb.x), 0.5f * (sa.y - sb.y));
+          const float2 a = cmul(sh, phasor2(kxs, kys, up.ux0[l] + (uint64_t)fbeg * up.dux[l],
+                                            up.uy0[l] + (uint64_t)fbeg * up.duy[l]));
+          const float2 r = phasor2(kxs, kys, up.dux[l], up.duy[l]);
+          ax[h] = a.x;
+          ay[h] = a.y;
+          rx[h] = r.x;
+          ry[h] = r.y;
+        }
+      }
+      Ax[e][q] = pk2(ax[0], ax[1]);
+      Ay[e][q] = pk2(ay[0], ay[1]);
+      Rx[e][q] = pk2(rx[0], rx[1]);
+      Ry[e][q] = pk2(ry[0], ry[1]);
+      NRy[e][q] = pk2(-ry[0], -ry[1]);
+    }
+  }
+  const int nfr = min(kAnchor, F - fbeg);
+  const int npairs = (nfr + 1) / 2;
+  const int v = threadIdx.x / T, j = threadIdx.x % T;
+  for (int pb = 0; pb < npairs; pb += NV) {
+    const int np = min(NV, npairs - pb);
+    for (int p = 0; p < np; ++p) {
+      const bool two = 2 * (pb + p) + 1 < nfr;
+#pragma unroll
+      for (int e = 0; e < E; ++e) {
+        float2 h[2];
+#pragma unroll
+        for (int fr = 0; fr < 2; ++fr) {
+          f2x hxa = 0ull, hya = 0ull, hxb = 0ull, hyb = 0ull;
+          if (fr == 0 || two) {
+#pragma unroll
+            for (int q = 0; q < LP; ++q) {
+              if (q & 1) {
+                hxb = add2(hxb, Ax[e][q]);
+                hyb = add2(hyb, Ay[e][q]);
+              } else {
+                hxa = add2(hxa, Ax[e][q]);
+                hya = add2(hya, Ay[e][q]);
+              }
+              const f2x nx = fma2(Ax[e][q], Rx[e][q], mul2(Ay[e][q], NRy[e][q]));
+              const f2x ny = fma2(Ax[e][q], Ry[e][q], mul2(Ay[e][q], Rx[e][q]));
+              Ax[e][q] = nx;
+              Ay[e][q] = ny;
+            }
+          }
+          float a0, a1, b0, b1;
+          upk2(add2(hxa, hxb), a0, a1);
+          upk2(add2(hya, hyb), b0, b1);
+          h[fr] = make_float2(a0 + a1, b0 + b1);
+        }
+        const int ky = threadIdx.x + e * THREADS;
+        if (kx == N / 2 || ky == N / 2) {
+          const int el = kx == N / 2 ? ky : N + kx;
+          const int fa = fbeg + 2 * (pb + p);
+          h[0] = hn[(size_t)fa * 2 * N + el];
+          h[1] = two ? hn[(size_t)(fa + 1) * 2 * N + el] : make_float2(0.f, 0.f);
+        }
+        const RowLayout rp{rows + p * fft_padded(N)};
+        rp[ky] = make_float2(h[0].x - h[1].y, h[0].y + h[1].x);
+      }
+    }
+    __syncthreads();
+    float2 x[8];
+    const RowLayout s{rows + v * fft_padded(N)};
+    if (v < np) reg_gather8<N>(x, j, s);
+    __syncthreads();
+    reg_fft<N>(x, j, stw, s);
+    if (v < np) {
+      const int pair = fbeg / 2 + pb + v;
+#pragma unroll
+      for (int i = 0; i < 8; ++i) work[((size_t)pair * N + kx) * N + j + T * i] = x[i];
+    }
+    __syncthreads();
+  }
+}

@@ -36,6 +36,7 @@ struct pt_grid {
   float2* basis;    // (P, 3, ns) exp(2 pi i f_p (x - ns/2) dx)
   double* sh_freq;  // (P, 3)
   double* beta;     // (P, 3, 2) grid mean of each basis row
+  int sym;          // every level's frequencies are {-a, 0, +a}
 };
 
 namespace pt {
@@ -367,6 +368,7 @@ struct PairStore {
   const float* mean;    // (rows)
   const float2* basis;  // (P, 3, ns)
   int P;
+  int sym;  // symmetric subharmonic frequencies (see k_pair_cols_reg)
 };
 
 __global__ void __launch_bounds__(kThreads)
@@ -661,256 +663,7 @@ __global__ void k_lgs_zoom(int L, int ns, int n, int T, const int32_t* __restric
   out[(size_t)i * n + j] = scale * acc;
 }
 
-// ================================================================ power-of-two fast path
-// The same passes with the register-resident FFT of fft_reg.cuh. Teams of
-// T = N/8 threads own one transform each; CTAs hold up to 512 threads.
-template <int N>
-struct RegCfg {
-  static constexpr int T = N / 8;
-  static constexpr int NV0 = (512 / T) < 1 ? 1 : (512 / T);
-  static constexpr int NV = NV0 < N ? NV0 : N;  // transforms (rows) per CTA
-  static constexpr int C = NV;                  // columns per CTA
-  static constexpr int THREADS = NV * T;
-};
-
-__device__ __forceinline__ void load_tw(float2* stw, const float2* tw, int n) {
-  for (int i = threadIdx.x; i < n; i += blockDim.x) stw[i] = tw[i];
-}
-
-// rows: plain complex input or generate's coloured noise
-template <int N>
-__global__ void __launch_bounds__(RegCfg<N>::THREADS)
-k_rows_reg(const float2* __restrict__ tw, const float2* __restrict__ in, int gen, GenRowArgs ga,
-           float2* __restrict__ work) {
-  constexpr int T = RegCfg<N>::T, NV = RegCfg<N>::NV;
-  extern __shared__ float2 sm[];
-  float2* stw = sm;
-  const int v = threadIdx.x / T, j = threadIdx.x % T;
-  float2* s = sm + N + v * fft_padded(N);
-  load_tw(stw, tw, N);
-  const int kx = blockIdx.x * NV + v;
-  const int img = blockIdx.y;
-  const bool ok = kx < N;
-  float2 x[8];
-#pragma unroll
-  for (int i = 0; i < 8; ++i) {
-    const int ky = j + T * i;
-    float2 val = make_float2(0.f, 0.f);
-    if (ok) {
-      if (gen) {
-        const size_t e = ((size_t)(ga.img0 + img) * N + kx) * N + ky;
-        float2 z;
-        if (ga.noise) {
-          const size_t plane = (size_t)ga.n_fft * N * N;
-          z = make_float2(ga.noise[e], ga.noise[plane + e]);
-        } else {
-          z = philox_cnormal(ga.seed, e, ga.call, kDomainScreen);
-        }
-        const float amp = ga.amplitude[(size_t)kx * N + ky];
-        val = make_float2(z.x * amp, z.y * amp);
-      } else {
-        val = in[((size_t)img * N + kx) * N + ky];
-      }
-    }
-    x[i] = val;
-  }
-  __syncthreads();  // twiddles loaded
-  reg_fft<N>(x, j, stw, s);
-  if (ok) {
-#pragma unroll
-    for (int i = 0; i < 8; ++i) work[((size_t)img * N + kx) * N + j + T * i] = x[i];
-  }
-}
-
-// columns: plain complex output (pt_ifft2)
-template <int N>
-__global__ void __launch_bounds__(RegCfg<N>::THREADS)
-k_plain_cols_reg(const float2* __restrict__ tw, const float2* __restrict__ work,
-                 float2* __restrict__ out) {
-  constexpr int T = RegCfg<N>::T, C = RegCfg<N>::C;
-  extern __shared__ float2 sm[];
-  float2* stw = sm;
-  const int c = threadIdx.x % C, j = threadIdx.x / C;
-  float2* s = sm + N + c * fft_padded(N);
-  load_tw(stw, tw, N);
-  const int y = blockIdx.x * C + c;
-  const int img = blockIdx.y;
-  const bool ok = y < N;
-  float2 x[8];
-#pragma unroll
-  for (int i = 0; i < 8; ++i)
-    x[i] = ok ? work[((size_t)img * N + j + T * i) * N + y] : make_float2(0.f, 0.f);
-  __syncthreads();
-  reg_fft<N>(x, j, stw, s);
-  if (ok) {
-#pragma unroll
-    for (int i = 0; i < 8; ++i) out[((size_t)img * N + j + T * i) * N + y] = x[i];
-  }
-}
-
-// columns with the paired real epilogue (generate and frames)
-template <int N>
-__global__ void __launch_bounds__(RegCfg<N>::THREADS)
-k_pair_cols_reg(const float2* __restrict__ tw, const float2* __restrict__ work, int pair0,
-                PairStore st) {
-  constexpr int T = RegCfg<N>::T, C = RegCfg<N>::C;
-  extern __shared__ float2 sm[];
-  float2* stw = sm;
-  float2* mtab = sm + N + C * fft_padded(N);  // (2, 3P, C)
-  const int c = threadIdx.x % C, j = threadIdx.x / C;
-  float2* s = sm + N + c * fft_padded(N);
-  load_tw(stw, tw, N);
-  const int y = blockIdx.x * C + c;
-  const int pl = blockIdx.y;
-  const int pair = pair0 + pl;
-  const bool ok = y < N;
-  const int img_re = pair * st.re_mul + st.re_add;
-  const int img_im = pair * st.im_mul + st.im_add;
-  const bool do_re = img_re < st.count, do_im = img_im < st.count;
-  const int row_re = pl * st.crow_mul + st.crow_re, row_im = pl * st.crow_mul + st.crow_im;
-  const int P = st.P;
-  for (int i = threadIdx.x; i < 2 * 3 * P * C; i += blockDim.x) {
-    const int cc = i % C;
-    const int pi = (i / C) % (3 * P);
-    const int o = i / (C * 3 * P);
-    const bool take = o == 0 ? do_re : do_im;
-    const int row = o == 0 ? row_re : row_im;
-    const int yy = blockIdx.x * C + cc;
-    float2 m = make_float2(0.f, 0.f);
-    if (take && yy < N) {
-      const int p = pi / 3, ii = pi % 3;
-      const float2* cf = st.coef + ((size_t)row * P + p) * 9 + ii * 3;
-#pragma unroll
-      for (int jj = 0; jj < 3; ++jj) m = cfma(cf[jj], st.basis[((size_t)p * 3 + jj) * N + yy], m);
-    }
-    mtab[i] = m;
-  }
-  float2 x[8];
-#pragma unroll
-  for (int i = 0; i < 8; ++i)
-    x[i] = ok ? work[((size_t)pl * N + j + T * i) * N + y] : make_float2(0.f, 0.f);
-  __syncthreads();
-  reg_fft<N>(x, j, stw, s);
-  if (!ok) return;
-  const float mre = (P > 0 && do_re) ? st.mean[row_re] : 0.f;
-  const float mim = (P > 0 && do_im) ? st.mean[row_im] : 0.f;
-  const size_t plane = (size_t)st.n_out * st.n_out;
-  const int yo = y - st.crop;
-  if (yo < 0 || yo >= st.n_out) return;
-#pragma unroll
-  for (int i = 0; i < 8; ++i) {
-    const int xr = j + T * i;
-    const int xo = xr - st.crop;
-    if (xo < 0 || xo >= st.n_out) continue;
-    float lre = 0.f, lim = 0.f;
-    for (int pi = 0; pi < 3 * P; ++pi) {
-      const float2 b = st.basis[(size_t)pi * N + xr];
-      const float2 m0 = mtab[(0 * 3 * P + pi) * C + c];
-      const float2 m1 = mtab[(1 * 3 * P + pi) * C + c];
-      lre = fmaf(b.x, m0.x, fmaf(-b.y, m0.y, lre));
-      lim = fmaf(b.x, m1.x, fmaf(-b.y, m1.y, lim));
-    }
-    const size_t o = (size_t)xo * st.n_out + yo;
-    if (do_re) {
-      const float val = st.scale * (x[i].x + (lre - mre));
-      float* dst = st.out + (size_t)img_re * plane + o;
-      *dst = st.accumulate ? *dst + val : val;
-    }
-    if (do_im) {
-      const float val = st.scale * (x[i].y + (lim - mim));
-      float* dst = st.out + (size_t)img_im * plane + o;
-      *dst = st.accumulate ? *dst + val : val;
-    }
-  }
-}
-
-// uniform frames, fused synthesis + row transform: the CTA's threads first act
-// as column owners (recurrence state in registers, E columns each), writing
-// NV pair rows into shared memory; then NV teams transform them.
-template <int LM, int N>
-__global__ void __launch_bounds__(N < 512 ? N : 512)
-k_frame_rows_uniform_reg(const float2* __restrict__ tw, const float2* __restrict__ spectra,
-                         int L, int F, UniformParams up, const float2* __restrict__ hn,
-                         float2* __restrict__ work) {
-  constexpr int THREADS = N < 512 ? N : 512;
-  constexpr int E = N / THREADS;  // columns per thread (1 or 2 for N <= 1024)
-  constexpr int T = N / 8;
-  constexpr int NV = THREADS / T;  // pair rows per batch
-  extern __shared__ float2 sm[];
-  float2* stw = sm;
-  float2* rows = sm + N;  // NV * fft_padded(N)
-  load_tw(stw, tw, N);
-  const int kx = blockIdx.x;
-  const int fbeg = blockIdx.y * kAnchor;
-  const int kxs = signed_freq(kx, N), nkx = (N - kx) & (N - 1);
-  float2 A[E][LM], R[E][LM];
-#pragma unroll
-  for (int e = 0; e < E; ++e) {
-    const int ky = threadIdx.x + e * THREADS;
-    const int kys = signed_freq(ky, N), nky = (N - ky) & (N - 1);
-#pragma unroll
-    for (int l = 0; l < LM; ++l) {
-      A[e][l] = make_float2(0.f, 0.f);
-      R[e][l] = make_float2(1.f, 0.f);
-      if (l < L) {
-        const float2 sa = spectra[((size_t)l * N + kx) * N + ky];
-        const float2 sb = spectra[((size_t)l * N + nkx) * N + nky];
-        const float2 sh = make_float2(0.5f * (sa.x + sb.x), 0.5f * (sa.y - sb.y));
-        A[e][l] = cmul(sh, phasor2(kxs, kys, up.ux0[l] + (uint64_t)fbeg * up.dux[l],
-                                   up.uy0[l] + (uint64_t)fbeg * up.duy[l]));
-        R[e][l] = phasor2(kxs, kys, up.dux[l], up.duy[l]);
-      }
-    }
-  }
-  const int nfr = min(kAnchor, F - fbeg);
-  const int npairs = (nfr + 1) / 2;
-  const int v = threadIdx.x / T, j = threadIdx.x % T;
-  for (int pb = 0; pb < npairs; pb += NV) {
-    const int np = min(NV, npairs - pb);
-    for (int p = 0; p < np; ++p) {
-      const bool two = 2 * (pb + p) + 1 < nfr;
-#pragma unroll
-      for (int e = 0; e < E; ++e) {
-        float2 h0a = make_float2(0.f, 0.f), h0b = h0a, h1a = h0a, h1b = h0a;
-#pragma unroll
-        for (int l = 0; l < LM; ++l) {
-          if (l & 1) h0b = cadd(h0b, A[e][l]);
-          else h0a = cadd(h0a, A[e][l]);
-          A[e][l] = cmul(A[e][l], R[e][l]);
-        }
-        if (two) {
-#pragma unroll
-          for (int l = 0; l < LM; ++l) {
-            if (l & 1) h1b = cadd(h1b, A[e][l]);
-            else h1a = cadd(h1a, A[e][l]);
-            A[e][l] = cmul(A[e][l], R[e][l]);
-          }
-        }
-        float2 h0 = cadd(h0a, h0b), h1 = cadd(h1a, h1b);
-        const int ky = threadIdx.x + e * THREADS;
-        if (kx == N / 2 || ky == N / 2) {
-          const int el = kx == N / 2 ? ky : N + kx;
-          const int fa = fbeg + 2 * (pb + p);
-          h0 = hn[(size_t)fa * 2 * N + el];
-          h1 = two ? hn[(size_t)(fa + 1) * 2 * N + el] : make_float2(0.f, 0.f);
-        }
-        rows[p * fft_padded(N) + fft_pad(ky)] = make_float2(h0.x - h1.y, h0.y + h1.x);
-      }
-    }
-    __syncthreads();
-    float2 x[8];
-    float2* s = rows + v * fft_padded(N);
-    if (v < np) reg_gather8(x, j, T, s);
-    __syncthreads();
-    reg_fft<N>(x, j, stw, s);
-    if (v < np) {
-      const int pair = fbeg / 2 + pb + v;
-#pragma unroll
-      for (int i = 0; i < 8; ++i) work[((size_t)pair * N + kx) * N + j + T * i] = x[i];
-    }
-    __syncthreads();
-  }
-}
+#include "frames_fast.cuh"  // power-of-two fast path kernels
 
 // ================================================================ host helpers
 static size_t rows_smem(int ns, int rpc) {
@@ -930,6 +683,10 @@ static int set_smem(K kernel, size_t bytes, const char* name) {
         cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
     if (e != cudaSuccess) return check_cuda(e, name);
   }
+  // prefer the largest shared-memory carveout so several CTAs fit per SM
+  cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                       (int)cudaSharedmemCarveoutMaxShared);
+  if (e != cudaSuccess) return check_cuda(e, name);
   return PT_OK;
 }
 
@@ -1056,7 +813,7 @@ template <int N>
 static int plain_cols_reg_t(const pt_grid* g, const float2* work, int nimg, float2* out,
                             cudaStream_t s) {
   using Cfg = RegCfg<N>;
-  const size_t smem = (size_t)(N + Cfg::C * fft_padded(N)) * sizeof(float2);
+  const size_t smem = (size_t)(N + Cfg::C * N) * sizeof(float2);
   if (int rc = set_smem(k_plain_cols_reg<N>, smem, "k_plain_cols_reg")) return rc;
   ProfScope ps("k_plain_cols", s);
   k_plain_cols_reg<N><<<dim3((N + Cfg::C - 1) / Cfg::C, nimg), Cfg::THREADS, smem, s>>>(g->tw, work,
@@ -1080,7 +837,7 @@ static int pair_cols_reg_t(const pt_grid* g, const float2* work, int npair, int 
                            const PairStore& st, cudaStream_t s) {
   using Cfg = RegCfg<N>;
   const size_t smem =
-      (size_t)(N + Cfg::C * fft_padded(N) + 2 * 3 * std::max(g->P, 1) * Cfg::C) * sizeof(float2);
+      (size_t)(N + Cfg::C * N + 2 * 3 * std::max(g->P, 1) * Cfg::C) * sizeof(float2);
   if (int rc = set_smem(k_pair_cols_reg<N>, smem, "k_pair_cols_reg")) return rc;
   ProfScope ps("k_pair_cols", s);
   k_pair_cols_reg<N><<<dim3((N + Cfg::C - 1) / Cfg::C, npair), Cfg::THREADS, smem, s>>>(
@@ -1145,6 +902,9 @@ extern "C" int pt_grid_create(pt_grid** out, int ns, double dx, int P, const dou
     }
   std::vector<double> freq((size_t)Pm * 3, 0.0);
   for (int i = 0; i < P * 3; ++i) freq[i] = sh_freq[i];
+  g->sym = 1;
+  for (int p = 0; p < P; ++p)
+    if (!(sh_freq[p * 3 + 1] == 0.0 && sh_freq[p * 3] == -sh_freq[p * 3 + 2])) g->sym = 0;
   int rc = check_cuda(cudaMalloc(&g->tw, ns * sizeof(float2)), "pt_grid_create: cudaMalloc");
   if (!rc) rc = check_cuda(cudaMalloc(&g->basis, basis.size() * sizeof(float2)), "pt_grid_create: cudaMalloc");
   if (!rc) rc = check_cuda(cudaMalloc(&g->sh_freq, freq.size() * sizeof(double)), "pt_grid_create: cudaMalloc");
@@ -1259,6 +1019,7 @@ extern "C" int pt_generate(const pt_grid* g, int count, const float* amplitude,
     st.mean = w.mean;
     st.basis = g->basis;
     st.P = P;
+    st.sym = g->sym;
     if (P > 0) {
       const int n_re = std::min(nb, count - b0);
       const int n_im = std::max(0, std::min(nb, count - (n_fft + b0)));
@@ -1400,6 +1161,7 @@ extern "C" int pt_frames(const pt_grid* g, int L, const float* spectra, const fl
     st.mean = w.mean;
     st.basis = g->basis;
     st.P = P;
+    st.sym = g->sym;
     if (pow2_fast(ns)) {
       if (int rc = pair_cols_reg(g, w.img, npair, 0, st, s)) return rc;
     } else {
