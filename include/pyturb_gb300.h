@@ -70,6 +70,18 @@ size_t pt_grid_workspace_bytes(const pt_grid* grid, int n_layers);
 int pt_ifft2(const pt_grid* grid, const float* in, float* out, int batch, void* work,
              size_t work_bytes, void* stream);
 
+/* Allocation-free variant of pt_ifft2 — no counterpart in the reference.
+ * For callers that cannot call cudaMalloc (a host framework that owns all
+ * device memory, or a process that must not grow its footprint after
+ * start-up): no grid plan and no workspace. Its scratch is a fixed 8 MiB
+ * file-scope device array (plus a 1024-entry twiddle table) that every GPU
+ * loading this library holds until exit. ns must be in [2, 1024]; larger
+ * grids are rejected with PT_ERR_ARG. The first call on each device resolves
+ * the arrays' addresses (cudaGetSymbolAddress) with that device current:
+ * make it before any stream capture. All calls share the arrays, so calls
+ * that overlap on the GPU race; nothing in them has to start at zero. */
+int pt_ifft2_noalloc(int ns, const float* in, float* out, int batch, void* stream);
+
 /* PhaseScreen.generate(count) (src/pyturb/fourier.py:233-282): coloured
  * complex noise x amplitude -> inverse FFT -> real parts are screens
  * [0, n_fft), imaginary parts screens [n_fft, 2 n_fft) (n_fft = ceil(count/2))

@@ -72,6 +72,7 @@ SIGNATURES = {
     "pt_grid_destroy": (i32, [vp]),
     "pt_grid_workspace_bytes": (sz, [vp, i32]),
     "pt_ifft2": (i32, [vp, vp, vp, i32, vp, sz, vp]),
+    "pt_ifft2_noalloc": (i32, [i32, vp, vp, i32, vp]),
     "pt_generate": (i32, [vp, i32, vp, vp, vp, vp, u64, u64, i32, i32, f32, i32, vp, vp, sz, vp]),
     "pt_layers_fill": (i32, [vp, i32, vp, vp, vp, vp, C.POINTER(C.c_uint64), vp, vp, vp]),
     "pt_frames": (i32, [vp, i32, vp, vp, i32, dptr, dptr, i32, i32, i32, f32, vp, vp, sz, vp]),

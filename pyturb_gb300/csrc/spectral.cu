@@ -1207,3 +1207,111 @@ extern "C" int pt_boil_step(const pt_grid* g, int L, float* spectra, float* sh_c
   }
   return check_launch("pt_boil_step");
 }
+
+// ================================================================ allocation-free inverse FFT
+// pt_ifft2_noalloc serves callers that cannot call cudaMalloc: code running
+// inside a host framework that owns all device memory, or a process that must
+// not grow its footprint after start-up. Its scratch is not a caller
+// workspace but a file-scope device array of fixed size, which every GPU that
+// loads this library holds until the process exits. Host code cannot use the
+// array's name as a device address, so the first call on each device, with
+// that device current, resolves the addresses with cudaGetSymbolAddress and
+// caches them; make that first call before any stream capture. All calls
+// share the arrays and the last call's contents stay in them; the row pass
+// overwrites every scratch element it later reads and the twiddle table is
+// rewritten by each call, so nothing has to start at zero. Calls that
+// overlap on the GPU (on different streams or threads) race on the arrays.
+#include <mutex>
+
+namespace pt {
+
+constexpr size_t kNoAllocScratchBytes = size_t(8) << 20;  // one 1024^2 complex image
+constexpr int kNoAllocMaxN = 1024;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+static __device__ __align__(256) float2 g_noalloc_tw[kNoAllocMaxN];
+
+struct NoAllocPtrs {
+  void* scratch;
+  void* tw;
+};
+constexpr int kNoAllocMaxDevices = 64;
+static std::mutex g_noalloc_mu;
+static NoAllocPtrs g_noalloc_ptrs[kNoAllocMaxDevices];
+static bool g_noalloc_ready[kNoAllocMaxDevices];
+
+static int noalloc_setup(NoAllocPtrs* out) {
+  int dev = 0;
+  if (int rc = check_cuda(cudaGetDevice(&dev), "pt_ifft2_noalloc: cudaGetDevice")) return rc;
+  if (dev < 0 || dev >= kNoAllocMaxDevices)
+    return fail(PT_ERR_UNSUPPORTED, "pt_ifft2_noalloc: device index beyond 63");
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (!g_noalloc_ready[dev]) {
+    NoAllocPtrs p{};
+    if (int rc = check_cuda(cudaGetSymbolAddress(&p.scratch, g_noalloc_scratch),
+                            "pt_ifft2_noalloc: cudaGetSymbolAddress(scratch)"))
+      return rc;
+    if (int rc = check_cuda(cudaGetSymbolAddress(&p.tw, g_noalloc_tw),
+                            "pt_ifft2_noalloc: cudaGetSymbolAddress(twiddles)"))
+      return rc;
+    g_noalloc_ptrs[dev] = p;
+    g_noalloc_ready[dev] = true;
+  }
+  *out = g_noalloc_ptrs[dev];
+  return PT_OK;
+}
+
+// exp(+2 pi i k / n) from the FP64 sincospi of the exact fraction k / n
+__global__ void k_noalloc_twiddles(float2* tw, int n) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  double s, c;
+  sincospi(2.0 * (double)k / (double)n, &s, &c);
+  tw[k] = make_float2((float)c, (float)s);
+}
+
+}  // namespace pt
+
+extern "C" int pt_ifft2_noalloc(int ns, const float* in, float* out, int batch, void* stream) {
+  if (ns < 2 || ns > kNoAllocMaxN)
+    return fail(PT_ERR_ARG, "pt_ifft2_noalloc: ns must be in [2, 1024] (fixed 8 MiB scratch)");
+  if (!in || !out || batch < 0) return fail(PT_ERR_ARG, "pt_ifft2_noalloc: bad arguments");
+  if (batch == 0) return PT_OK;
+  NoAllocPtrs p{};
+  if (int rc = noalloc_setup(&p)) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  pt_grid g{};  // a stack view over the static arrays: nothing is allocated
+  g.ns = ns;
+  g.dx = 1.0;
+  g.P = 0;
+  g.desc = make_fft_desc(ns);
+  g.tw = (float2*)p.tw;
+  float2* scratch = (float2*)p.scratch;
+  const size_t per = (size_t)ns * ns;
+  const int chunk = (int)std::max<size_t>(1, kNoAllocScratchBytes / (per * sizeof(float2)));
+  k_noalloc_twiddles<<<(ns + 127) / 128, 128, 0, s>>>(g.tw, ns);
+  count_launch();
+  const int rpc = rows_per_cta(ns), C = cols_per_cta(ns);
+  const size_t rs = rows_smem(ns, rpc), cs = cols_smem(ns, C, 0);
+  if (!pow2_fast(ns)) {
+    if (int rc = set_smem(k_rows, rs, "k_rows")) return rc;
+    if (int rc = set_smem(k_plain_cols, cs, "k_plain_cols")) return rc;
+  }
+  GenRowArgs none{};
+  for (int b0 = 0; b0 < batch; b0 += chunk) {
+    const int nb = std::min(chunk, batch - b0);
+    const float2* src = (const float2*)in + (size_t)b0 * per;
+    float2* dst = (float2*)out + (size_t)b0 * per;
+    if (pow2_fast(ns)) {
+      if (int rc = rows_reg(&g, src, 0, none, nb, scratch, s)) return rc;
+      if (int rc = plain_cols_reg(&g, scratch, nb, dst, s)) return rc;
+    } else {
+      k_rows<<<dim3((ns + rpc - 1) / rpc, nb), kThreads, rs, s>>>(g.desc, g.tw, rpc, src, 0, none,
+                                                                 scratch);
+      k_plain_cols<<<dim3((ns + C - 1) / C, nb), kThreads, cs, s>>>(g.desc, g.tw, scratch, C, dst);
+    }
+    count_launch(2);
+    if (int rc = check_launch("pt_ifft2_noalloc")) return rc;
+  }
+  return PT_OK;
+}
