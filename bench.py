@@ -311,16 +311,27 @@ def main() -> None:
     ns, L = N_PIX, 9
     frames_per_launch = FRAMES_PER_STEP * args.steps / max(1, nlaunch)
     pairs = frames_per_launch / 2.0
-    # algorithmic DRAM bytes per launch ("Roofline accounting")
+    blocks = np.ceil(frames_per_launch / 32.0)  # recurrence anchor blocks per launch
+    log2n = np.log2(ns)
+    # algorithmic bytes and FP32 flops per launch ("Roofline accounting")
     algo = {
-        "k_frame_rows": pairs * (L * ns * ns * 8 + ns * ns * 8),
-        "k_pair_cols": pairs * (ns * ns * 8 + 2 * N_PIX * N_PIX * 4),
-        "k_frame_phasors": frames_per_launch * L * ns * 2 * 8,
-    }.get(name, 0.0)
-    achieved = algo / (kms / nlaunch / 1000.0) / 1e9 if algo else None
+        "k_frame_rows_uniform": (blocks * L * ns * ns * 8 + pairs * ns * ns * 8,
+                                 frames_per_launch * (L * 8 * ns * ns)
+                                 + pairs * 5 * ns * ns * log2n),
+        "k_frame_rows": (pairs * (L * ns * ns * 8 + ns * ns * 8),
+                         frames_per_launch * L * 14 * ns * ns + pairs * 5 * ns * ns * log2n),
+        "k_pair_cols": (pairs * (ns * ns * 8 + 2 * N_PIX * N_PIX * 4),
+                        pairs * 5 * ns * ns * log2n + frames_per_launch * 4 * LEVELS * ns * ns),
+    }.get(name, (0.0, 0.0))
+    sec = kms / nlaunch / 1000.0
+    achieved = algo[0] / sec / 1e9 if algo[0] else None
+    fp32_peak = 152 * 128 * 2 * 2.07e9 / 1e12  # TFLOP/s, SIMT FP32 at max SM clock (nominal)
     roofline = {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": hbm,
                 "unit": "GB/s", "frac": (achieved / hbm) if achieved else None,
                 "traffic": None, "peak_source": f"MEASURED_PEAKS.json hbm_gbs ({peak_kind})",
+                "algorithmic_bytes_per_launch": algo[0],
+                "fp32_tflops": algo[1] / sec / 1e12 if algo[1] else None,
+                "fp32_frac_of_nominal": (algo[1] / sec / 1e12 / fp32_peak) if algo[1] else None,
                 "kernel_share": {k: round(v[1] / max(1e-9, sum(x[1] for x in prof.values())), 4)
                                  for k, v in prof.items()},
                 "kernel_ms_per_launch": {k: v[1] / v[0] for k, v in prof.items()}}

@@ -61,13 +61,45 @@ struct is_pow2_fft {
   static constexpr bool value = N >= 8 && N <= 4096 && (N & (N - 1)) == 0;
 };
 
+// Stage twiddles live in shared memory per stage, ordered [jm][r-1] with
+// jm = b mod Ns: consecutive butterflies read at a stride of R-1 float2
+// (7, 3 or 1), which is conflict-free per half-warp. Stage s starts at
+// tw_offset(N, s); the stages after the first fill fewer than N slots.
+template <int N>
+__host__ __device__ constexpr int tw_offset(int s) {
+  int off = 0, ns = 1;
+  for (int k = 0; k < s; ++k) {
+    const int r = Pow2Plan<N>::radix(k);
+    if (k > 0) off += ns * (r - 1);
+    ns *= r;
+  }
+  return off;
+}
+
+// Fill the per-stage tables from the N-entry table exp(+2 pi i k / N).
+template <int N>
+__device__ __forceinline__ void load_stage_tw(float2* stw, const float2* __restrict__ tw) {
+  int ns = Pow2Plan<N>::radix(0);
+  for (int s = 1; s < Pow2Plan<N>::stages; ++s) {
+    const int r = Pow2Plan<N>::radix(s);
+    const int twstep = N / (ns * r);
+    const int off = tw_offset<N>(s);
+    for (int i = threadIdx.x; i < ns * (r - 1); i += blockDim.x) {
+      const int jm = i / (r - 1), q = i % (r - 1) + 1;
+      stw[off + i] = tw[(q * jm * twstep) & (N - 1)];
+    }
+    ns *= r;
+  }
+}
+
 // Twiddle, butterflies of one stage on the thread's registers (in place:
-// output q of the butterfly in register slot i0 + (8/R) q).
-template <int N, int R, int Ns>
+// output q of the butterfly in register slot i0 + (8/R) q). `tw` here is the
+// per-stage table of load_stage_tw.
+template <int N, int R, int Ns, int S>
 __device__ __forceinline__ void reg_stage(float2 (&x)[8], int j, const float2* __restrict__ tw) {
   constexpr int T = N / 8;
   constexpr int B = 8 / R;                // butterflies per thread
-  constexpr int twstep = N / (Ns * R);
+  constexpr int off = tw_offset<N>(S);
 #pragma unroll
   for (int i0 = 0; i0 < B; ++i0) {
     const int b = j + T * i0;  // butterfly index (< N / R)
@@ -76,8 +108,9 @@ __device__ __forceinline__ void reg_stage(float2 (&x)[8], int j, const float2* _
 #pragma unroll
     for (int r = 0; r < R; ++r) v[r] = x[i0 + B * r];
     if (Ns > 1) {
+      const float2* t = tw + off + jm * (R - 1);
 #pragma unroll
-      for (int r = 1; r < R; ++r) v[r] = cmul(v[r], tw[(r * jm * twstep) & (N - 1)]);
+      for (int r = 1; r < R; ++r) v[r] = cmul(v[r], t[r - 1]);
     }
     if (R == 8) bfly8(v);
     else if (R == 4) bfly4(v);
@@ -113,7 +146,7 @@ struct RegStages {
   static __device__ __forceinline__ void run(float2 (&x)[8], int j, const float2* tw,
                                              const Lay& s) {
     constexpr int R = Pow2Plan<N>::radix(S);
-    reg_stage<N, R, Ns>(x, j, tw);
+    reg_stage<N, R, Ns, S>(x, j, tw);
     if constexpr (S + 1 < Pow2Plan<N>::stages) {
       reg_scatter<N, R, Ns>(x, j, s);
       __syncthreads();
@@ -126,8 +159,8 @@ struct RegStages {
 
 // Full transform of the thread's team. x in: element j + T i of the input;
 // x out: element j + T i of the output. `s` addresses this team's scratch
-// vector through its layout; tw is the N-entry twiddle table
-// exp(+2 pi i k / N). Every thread of the CTA must call this (it
+// vector through its layout; tw is the shared per-stage twiddle table filled
+// by load_stage_tw<N>. Every thread of the CTA must call this (it
 // synchronises the CTA), and the caller must synchronise between its own
 // last read of `s` and this call.
 template <int N, class Lay>

@@ -55,7 +55,7 @@ k_rows_reg(const float2* __restrict__ tw, const float2* __restrict__ in, int gen
   float2* stw = sm;
   const int v = threadIdx.x / T, j = threadIdx.x % T;
   const RowLayout s{sm + N + v * fft_padded(N)};
-  load_tw(stw, tw, N);
+  load_stage_tw<N>(stw, tw);
   const int kx = blockIdx.x * NV + v;
   const int img = blockIdx.y;
   const bool ok = kx < N;
@@ -100,7 +100,7 @@ k_plain_cols_reg(const float2* __restrict__ tw, const float2* __restrict__ work,
   float2* stw = sm;
   const int c = threadIdx.x % C, j = threadIdx.x / C;
   const ColLayout<C> s{sm + N + c};
-  load_tw(stw, tw, N);
+  load_stage_tw<N>(stw, tw);
   const int y = blockIdx.x * C + c;
   const int img = blockIdx.y;
   const bool ok = y < N;
@@ -133,7 +133,7 @@ k_pair_cols_reg(const float2* __restrict__ tw, const float2* __restrict__ work, 
   float2* mtab = buf + N * C;       // (2, 3P, C) or (2, P, C) (U, W) + (2, C) (K, 0)
   const int c = threadIdx.x % C, j = threadIdx.x / C;
   const ColLayout<C> s{buf + c};
-  load_tw(stw, tw, N);
+  load_stage_tw<N>(stw, tw);
   const int y = blockIdx.x * C + c;
   const int pl = blockIdx.y;
   const int pair = pair0 + pl;
@@ -227,10 +227,37 @@ k_pair_cols_reg(const float2* __restrict__ tw, const float2* __restrict__ work, 
 // Fused synthesis + row transform. Threads first own columns (E each) and
 // advance the layer recurrence two layers per packed register pair, writing
 // NV pair rows into shared memory; then NV teams transform those rows.
+// Separable anchor phasors Q(kx, ky) = Px(kx) Py(ky) per layer: px0/py0
+// (n_blocks, L, N) at each anchor block's first frame, rx/ry (L, N) per-frame
+// ratios; filled by k_uniform_tables from the exact fixed-point phases.
+struct UniformTables {
+  const float2* px0;
+  const float2* py0;
+  const float2* rx;
+  const float2* ry;
+};
+
+__global__ void k_uniform_tables(int N, int L, int nblocks, UniformParams up, float2* px0,
+                                 float2* py0, float2* rx, float2* ry) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const int bl = blockIdx.y;  // (block, layer) or the ratio row (block == nblocks)
+  if (k >= N) return;
+  const int b = bl / L, l = bl % L;
+  const uint64_t kk = (uint64_t)(int64_t)signed_freq(k, N);
+  if (b < nblocks) {
+    const uint64_t f0 = (uint64_t)b * kAnchor;
+    px0[(size_t)bl * N + k] = phasor_from_fixed(kk * (up.ux0[l] + f0 * up.dux[l]));
+    py0[(size_t)bl * N + k] = phasor_from_fixed(kk * (up.uy0[l] + f0 * up.duy[l]));
+  } else {
+    rx[(size_t)l * N + k] = phasor_from_fixed(kk * up.dux[l]);
+    ry[(size_t)l * N + k] = phasor_from_fixed(kk * up.duy[l]);
+  }
+}
+
 template <int LM, int N>
 __global__ void __launch_bounds__(N < 512 ? N : 512)
 k_frame_rows_uniform_reg(const float2* __restrict__ tw, const float2* __restrict__ spectra,
-                         int L, int F, UniformParams up, const float2* __restrict__ hn,
+                         int L, int F, UniformTables ut, const float2* __restrict__ hn,
                          float2* __restrict__ work) {
   constexpr int THREADS = N < 512 ? N : 512;
   constexpr int E = N / THREADS;  // columns per thread
@@ -240,16 +267,16 @@ k_frame_rows_uniform_reg(const float2* __restrict__ tw, const float2* __restrict
   extern __shared__ float2 sm[];
   float2* stw = sm;
   float2* rows = sm + N;  // NV * fft_padded(N)
-  load_tw(stw, tw, N);
+  load_stage_tw<N>(stw, tw);
   const int kx = blockIdx.x;
   const int fbeg = blockIdx.y * kAnchor;
-  const int kxs = signed_freq(kx, N), nkx = (N - kx) & (N - 1);
+  const int nkx = (N - kx) & (N - 1);
   // packed state: lanes (layer 2q, layer 2q+1)
   f2x Ax[E][LP], Ay[E][LP], Rx[E][LP], Ry[E][LP], NRy[E][LP];
 #pragma unroll
   for (int e = 0; e < E; ++e) {
     const int ky = threadIdx.x + e * THREADS;
-    const int kys = signed_freq(ky, N), nky = (N - ky) & (N - 1);
+    const int nky = (N - ky) & (N - 1);
 #pragma unroll
     for (int q = 0; q < LP; ++q) {
       float ax[2], ay[2], rx[2], ry[2];
@@ -262,9 +289,9 @@ k_frame_rows_uniform_reg(const float2* __restrict__ tw, const float2* __restrict
           const float2 sa = spectra[((size_t)l * N + kx) * N + ky];
           const float2 sb = spectra[((size_t)l * N + nkx) * N + nky];
           const float2 sh = make_float2(0.5f * (sa.x + sb.x), 0.5f * (sa.y - sb.y));
-          const float2 a = cmul(sh, phasor2(kxs, kys, up.ux0[l] + (uint64_t)fbeg * up.dux[l],
-                                            up.uy0[l] + (uint64_t)fbeg * up.duy[l]));
-          const float2 r = phasor2(kxs, kys, up.dux[l], up.duy[l]);
+          const size_t bl = (size_t)blockIdx.y * L + l;
+          const float2 a = cmul(cmul(sh, ut.px0[bl * N + kx]), ut.py0[bl * N + ky]);
+          const float2 r = cmul(ut.rx[(size_t)l * N + kx], ut.ry[(size_t)l * N + ky]);
           ax[h] = a.x;
           ay[h] = a.y;
           rx[h] = r.x;

@@ -725,7 +725,8 @@ static bool uniform_ok(const double* sx, const double* sy, int per_layer, int L,
 
 template <int LM>
 static int launch_uniform_t(const pt_grid* g, const float2* spectra, int L, int nf,
-                            const UniformParams& up, float2* hn, float2* img, cudaStream_t s) {
+                            const UniformParams& up, float2* hn, float2* ptab, float2* img,
+                            cudaStream_t s) {
   const int ns = g->ns;
   if ((ns & 1) == 0) {
     k_nyquist_h<<<dim3((2 * ns + 127) / 128, nf), 128, 0, s>>>(ns, spectra, L, nf, up, hn);
@@ -734,10 +735,16 @@ static int launch_uniform_t(const pt_grid* g, const float2* spectra, int L, int 
   const dim3 grid(ns, (nf + kAnchor - 1) / kAnchor);
   ProfScope ps("k_frame_rows_uniform", s);
   if (ns == 256 || ns == 512 || ns == 1024) {
+    const int nb = (nf + kAnchor - 1) / kAnchor;
+    UniformTables ut{ptab, ptab + (size_t)nb * L * ns, ptab + (size_t)2 * nb * L * ns,
+                     ptab + (size_t)(2 * nb + 1) * L * ns};
+    k_uniform_tables<<<dim3((ns + 127) / 128, (nb + 1) * L), 128, 0, s>>>(
+        ns, L, nb, up, (float2*)ut.px0, (float2*)ut.py0, (float2*)ut.rx, (float2*)ut.ry);
+    count_launch();
     auto go = [&](auto kern, int n, int threads, int nv) -> int {
       const size_t smem = (size_t)(n + nv * fft_padded(n)) * sizeof(float2);
       if (int rc = set_smem(kern, smem, "k_frame_rows_uniform_reg")) return rc;
-      kern<<<grid, threads, smem, s>>>(g->tw, spectra, L, nf, up, hn, img);
+      kern<<<grid, threads, smem, s>>>(g->tw, spectra, L, nf, ut, hn, img);
       return PT_OK;
     };
     if (ns == 256) return go(k_frame_rows_uniform_reg<LM, 256>, 256, 256, 8);
@@ -758,8 +765,8 @@ static int launch_uniform_t(const pt_grid* g, const float2* spectra, int L, int 
 }
 
 static int launch_uniform_rows(const pt_grid* g, const float2* spectra, int L, const double* sx,
-                               const double* sy, int f0, int nf, float2* hn, float2* img,
-                               cudaStream_t s) {
+                               const double* sy, int f0, int nf, float2* hn, float2* ptab,
+                               float2* img, cudaStream_t s) {
   const double df = 1.0 / (g->ns * g->dx);
   UniformParams up{};
   for (int l = 0; l < L; ++l) {
@@ -771,14 +778,14 @@ static int launch_uniform_rows(const pt_grid* g, const float2* spectra, int L, c
     up.dux[l] = host_fixed(dx * df);
     up.duy[l] = host_fixed(dy * df);
   }
-  if (L <= 1) return launch_uniform_t<1>(g, spectra, L, nf, up, hn, img, s);
-  if (L <= 2) return launch_uniform_t<2>(g, spectra, L, nf, up, hn, img, s);
-  if (L <= 3) return launch_uniform_t<3>(g, spectra, L, nf, up, hn, img, s);
-  if (L <= 4) return launch_uniform_t<4>(g, spectra, L, nf, up, hn, img, s);
-  if (L <= 6) return launch_uniform_t<6>(g, spectra, L, nf, up, hn, img, s);
-  if (L <= 9) return launch_uniform_t<9>(g, spectra, L, nf, up, hn, img, s);
-  if (L <= 12) return launch_uniform_t<12>(g, spectra, L, nf, up, hn, img, s);
-  return launch_uniform_t<16>(g, spectra, L, nf, up, hn, img, s);
+  if (L <= 1) return launch_uniform_t<1>(g, spectra, L, nf, up, hn, ptab, img, s);
+  if (L <= 2) return launch_uniform_t<2>(g, spectra, L, nf, up, hn, ptab, img, s);
+  if (L <= 3) return launch_uniform_t<3>(g, spectra, L, nf, up, hn, ptab, img, s);
+  if (L <= 4) return launch_uniform_t<4>(g, spectra, L, nf, up, hn, ptab, img, s);
+  if (L <= 6) return launch_uniform_t<6>(g, spectra, L, nf, up, hn, ptab, img, s);
+  if (L <= 9) return launch_uniform_t<9>(g, spectra, L, nf, up, hn, ptab, img, s);
+  if (L <= 12) return launch_uniform_t<12>(g, spectra, L, nf, up, hn, ptab, img, s);
+  return launch_uniform_t<16>(g, spectra, L, nf, up, hn, ptab, img, s);
 }
 
 // ---- power-of-two dispatch (runtime ns -> template N)
@@ -1134,8 +1141,8 @@ extern "C" int pt_frames(const pt_grid* g, int L, const float* spectra, const fl
       count_launch();
     }
     if (uniform_ok(sx, sy, per_layer, L, f0, nf, ns)) {
-      if (int rc = launch_uniform_rows(g, (const float2*)spectra, L, sx, sy, f0, nf, w.hn, w.img,
-                                       s))
+      if (int rc = launch_uniform_rows(g, (const float2*)spectra, L, sx, sy, f0, nf, w.hn, w.px,
+                                       w.img, s))
         return rc;
     } else {
       FrameRowArgs fa{(const float2*)spectra, w.px, w.py, J, nf, f0, per_layer};
