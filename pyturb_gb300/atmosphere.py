@@ -411,6 +411,58 @@ class Atmosphere:
                 self._t = float(times[i]) + dt
             done += k
 
+    def frames_host(self, dt: float, steps: int, wavelength: Optional[float] = None, out=None):
+        """All ``steps`` frames of :meth:`frames` delivered into host memory.
+
+        Returns a pinned CPU tensor ``(steps, n, n)`` (or fills ``out``, which
+        should be pinned for the copies to overlap). Chunks of ``frames_chunk``
+        frames are rendered into two alternating device buffers and copied to
+        the host on a side stream while the next chunk renders, so the run is
+        bounded by the slower of the GPU and the device-to-host link. Advances
+        the clock exactly as iterating :meth:`frames` does.
+        """
+        if dt <= 0:
+            raise ValueError("dt must be positive")
+        if steps < 1:
+            raise ValueError("steps must be >= 1")
+        torch = torch_module()
+        steps = int(steps)
+        if out is None:
+            out = torch.empty((steps, self.n, self.n), dtype=torch.float32, pin_memory=True)
+        if self.engine != "spectral" or self._boiling or self._lgs_mag is not None:
+            for i, (_t, f) in enumerate(self.frames(dt, steps, wavelength)):
+                out[i].copy_(f)
+            return out
+        dev = self._spec.grid.device
+        k = self.frames_chunk
+        bufs = [torch.empty((k, self.n, self.n), dtype=torch.float32, device=dev)
+                for _ in range(2)]
+        done_copy = [None, None]
+        main = torch.cuda.current_stream(dev)
+        side = torch.cuda.Stream(dev)
+        dt = float(dt)
+        t = self._t
+        for c, start in enumerate(range(0, steps, k)):
+            m = min(k, steps - start)
+            times = np.empty(m)
+            for i in range(m):  # the reference's clock: repeated float additions
+                times[i] = t
+                t += dt
+            b = c % 2
+            if done_copy[b] is not None:
+                main.wait_event(done_copy[b])
+            self.render(times, wavelength, out=bufs[b][:m])
+            ready = torch.cuda.Event()
+            ready.record(main)
+            with torch.cuda.stream(side):
+                side.wait_event(ready)
+                out[start:start + m].copy_(bufs[b][:m], non_blocking=True)
+                done_copy[b] = torch.cuda.Event()
+                done_copy[b].record(side)
+        side.synchronize()
+        self._t = t
+        return out
+
     def render(self, times: Sequence[float], wavelength: Optional[float] = None, out=None):
         """All on-axis frames at ``times`` in one call, ``(F, n, n)`` — each equal to
         ``opd(t)`` (spectral engine, frozen flow, no LGS). ``out`` may be a

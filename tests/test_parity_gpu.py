@@ -113,6 +113,22 @@ def test_frames_generator_equals_render_and_opd():
     assert a.time == pytest.approx(37e-3)
 
 
+def test_frames_host_equals_frames_generator():
+    import pyturb_gb300 as G
+    from pyturb_gb300.backend import to_numpy
+
+    warnings.simplefilter("ignore")
+    lys = [G.Layer(0, 0.7, 10, 30), G.Layer(5000, 0.3, 25, 200)]
+    kw = dict(r0=0.15, n=128, diameter=4.0, subharmonics=3, seed=2, frames_chunk=16)
+    a = G.Atmosphere(lys, **kw)
+    b = G.Atmosphere(lys, **kw)
+    host = a.frames_host(dt=1e-3, steps=53)
+    ref = np.stack([to_numpy(f) for _, f in b.frames(dt=1e-3, steps=53)])
+    assert host.device.type == "cpu" and host.shape == (53, 128, 128)
+    np.testing.assert_array_equal(host.numpy(), ref)
+    assert a.time == pytest.approx(b.time)
+
+
 def test_sample_config2_vs_oracle():
     import oracle
     import pyturb_gb300 as G
