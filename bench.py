@@ -199,21 +199,20 @@ def main() -> None:
     import warnings
 
     import pyturb_gb300 as G
-    from pyturb_gb300 import _lib
+    from pyturb_gb300 import _lib, replicas
 
     warnings.simplefilter("ignore")
     dev = torch.device("cuda", torch.cuda.current_device())
     layers = [G.Layer(h, f, v, d, L0) for h, f, v, d in layer_table()]
     atm = G.Atmosphere(layers, r0=R0, zenith_angle=ZENITH, diameter=DIAM, n=N_PIX,
-                       subharmonics=LEVELS, seed=1000 + rank, frames_chunk=64)
+                       subharmonics=LEVELS, seed=replicas.rank_seed(1000, rank, world),
+                       frames_chunk=64)
     out = torch.empty((FRAMES_PER_STEP, N_PIX, N_PIX), dtype=torch.float32, device=dev)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)  # > 129 MB L2
 
-    # each rank renders its own time window: rank r, step s starts at
-    # (r * 1e6 + s * FRAMES_PER_STEP) * DT
+    # each rank renders its own, disjoint time window
     def step_times(s: int) -> np.ndarray:
-        t0 = (rank * 1_000_000 + s * FRAMES_PER_STEP) * DT
-        return t0 + DT * np.arange(FRAMES_PER_STEP)
+        return replicas.time_window(rank, s, FRAMES_PER_STEP, DT)
 
     def barrier():
         if dist is not None:
@@ -249,11 +248,7 @@ def main() -> None:
     _lib.prof_enable(False)
     launches = _lib.launch_count() - launches0
     step_ms = [a.elapsed_time(b) for a, b in events]
-    total_ms = float(sum(step_ms))
-    if dist is not None:
-        t = torch.tensor([total_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = replicas.max_over_ranks(float(sum(step_ms)), dist, dev)
     frames_total = world * args.steps * FRAMES_PER_STEP
     value = frames_total / (total_ms / 1000.0)
 
@@ -267,11 +262,7 @@ def main() -> None:
         atm.frames_host(dt=DT, steps=FRAMES_PER_STEP, out=host)
         torch.cuda.synchronize()
         e2e_ms.append(1000.0 * (time.perf_counter() - t0))
-    e2e_step = min(e2e_ms[1:])
-    if dist is not None:
-        t = torch.tensor([e2e_step], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_step = float(t.item())
+    e2e_step = replicas.max_over_ranks(min(e2e_ms[1:]), dist, dev)
     e2e = {"value": world * FRAMES_PER_STEP / (e2e_step / 1000.0), "unit": "frames/s",
            "h2d_bytes_per_step": FRAMES_PER_STEP * 9 * 2 * 8,
            "d2h_bytes_per_step": FRAMES_PER_STEP * N_PIX * N_PIX * 4,

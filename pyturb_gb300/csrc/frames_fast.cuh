@@ -38,6 +38,8 @@ __device__ __forceinline__ f2x mul2(f2x a, f2x b) {
   asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
   return d;
 }
+// both lanes negated (sign bits flipped)
+__device__ __forceinline__ f2x neg2(f2x a) { return a ^ 0x8000000080000000ull; }
 __device__ __forceinline__ f2x add2(f2x a, f2x b) {
   f2x d;
   asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
@@ -224,9 +226,11 @@ k_pair_cols_reg(const float2* __restrict__ tw, const float2* __restrict__ work, 
 }
 
 // ------------------------------------------------------------------ uniform frames
-// Fused synthesis + row transform. Threads first own columns (E each) and
-// advance the layer recurrence two layers per packed register pair, writing
-// NV pair rows into shared memory; then NV teams transform those rows.
+// Fused synthesis + row transform. CTA = the row pair {kx, N - kx} of one
+// anchor block of frames. Threads first own columns (E each) and advance the
+// layer recurrence two layers per packed register pair, writing NV rows (NV/2
+// frame pairs, two mirrored rows each) into shared memory; then NV teams
+// transform those rows.
 // Separable anchor phasors Q(kx, ky) = Px(kx) Py(ky) per layer: px0/py0
 // (n_blocks, L, N) at each anchor block's first frame, rx/ry (L, N) per-frame
 // ratios; filled by k_uniform_tables from the exact fixed-point phases.
@@ -272,7 +276,7 @@ k_frame_rows_uniform_reg(const float2* __restrict__ tw, const float2* __restrict
   const int fbeg = blockIdx.y * kAnchor;
   const int nkx = (N - kx) & (N - 1);
   // packed state: lanes (layer 2q, layer 2q+1)
-  f2x Ax[E][LP], Ay[E][LP], Rx[E][LP], Ry[E][LP], NRy[E][LP];
+  f2x Ax[E][LP], Ay[E][LP], Rx[E][LP], Ry[E][LP];
 #pragma unroll
   for (int e = 0; e < E; ++e) {
     const int ky = threadIdx.x + e * THREADS;
@@ -302,14 +306,18 @@ k_frame_rows_uniform_reg(const float2* __restrict__ tw, const float2* __restrict
       Ay[e][q] = pk2(ay[0], ay[1]);
       Rx[e][q] = pk2(rx[0], rx[1]);
       Ry[e][q] = pk2(ry[0], ry[1]);
-      NRy[e][q] = pk2(-ry[0], -ry[1]);
     }
   }
+  // Hermitian symmetry H(-k) = conj H(k): this CTA synthesises row kx only and
+  // also emits the mirrored row N - kx (columns reversed), so the recurrence
+  // runs on half of the spectrum. Rows 0 and N/2 are their own mirrors.
+  const bool self = (kx == 0) || (kx == N / 2);
+  constexpr int PB = NV / 2;  // frame pairs per transform batch (two rows each)
   const int nfr = min(kAnchor, F - fbeg);
   const int npairs = (nfr + 1) / 2;
   const int v = threadIdx.x / T, j = threadIdx.x % T;
-  for (int pb = 0; pb < npairs; pb += NV) {
-    const int np = min(NV, npairs - pb);
+  for (int pb = 0; pb < npairs; pb += PB) {
+    const int np = min(PB, npairs - pb);
     for (int p = 0; p < np; ++p) {
       const bool two = 2 * (pb + p) + 1 < nfr;
 #pragma unroll
@@ -328,7 +336,7 @@ k_frame_rows_uniform_reg(const float2* __restrict__ tw, const float2* __restrict
                 hxa = add2(hxa, Ax[e][q]);
                 hya = add2(hya, Ay[e][q]);
               }
-              const f2x nx = fma2(Ax[e][q], Rx[e][q], mul2(Ay[e][q], NRy[e][q]));
+              const f2x nx = fma2(Ax[e][q], Rx[e][q], neg2(mul2(Ay[e][q], Ry[e][q])));
               const f2x ny = fma2(Ax[e][q], Ry[e][q], mul2(Ay[e][q], Rx[e][q]));
               Ax[e][q] = nx;
               Ay[e][q] = ny;
@@ -346,20 +354,28 @@ k_frame_rows_uniform_reg(const float2* __restrict__ tw, const float2* __restrict
           h[0] = hn[(size_t)fa * 2 * N + el];
           h[1] = two ? hn[(size_t)(fa + 1) * 2 * N + el] : make_float2(0.f, 0.f);
         }
-        const RowLayout rp{rows + p * fft_padded(N)};
-        rp[ky] = make_float2(h[0].x - h[1].y, h[0].y + h[1].x);
+        const RowLayout ra{rows + (2 * p) * fft_padded(N)};
+        ra[ky] = make_float2(h[0].x - h[1].y, h[0].y + h[1].x);
+        if (!self) {
+          // Y(-k) = conj H0(k) + i conj H1(k)
+          const RowLayout rb{rows + (2 * p + 1) * fft_padded(N)};
+          rb[(N - ky) & (N - 1)] = make_float2(h[0].x + h[1].y, h[1].x - h[0].y);
+        }
       }
     }
     __syncthreads();
+    const int pv = v >> 1, half = v & 1;  // team v: pair pv, row kx (0) or N - kx (1)
+    const bool active = pv < np && (half == 0 || !self);
     float2 x[8];
     const RowLayout s{rows + v * fft_padded(N)};
-    if (v < np) reg_gather8<N>(x, j, s);
+    if (active) reg_gather8<N>(x, j, s);
     __syncthreads();
     reg_fft<N>(x, j, stw, s);
-    if (v < np) {
-      const int pair = fbeg / 2 + pb + v;
+    if (active) {
+      const int pair = fbeg / 2 + pb + pv;
+      const int row = half ? nkx : kx;
 #pragma unroll
-      for (int i = 0; i < 8; ++i) work[((size_t)pair * N + kx) * N + j + T * i] = x[i];
+      for (int i = 0; i < 8; ++i) work[((size_t)pair * N + row) * N + j + T * i] = x[i];
     }
     __syncthreads();
   }

@@ -741,10 +741,11 @@ static int launch_uniform_t(const pt_grid* g, const float2* spectra, int L, int 
     k_uniform_tables<<<dim3((ns + 127) / 128, (nb + 1) * L), 128, 0, s>>>(
         ns, L, nb, up, (float2*)ut.px0, (float2*)ut.py0, (float2*)ut.rx, (float2*)ut.ry);
     count_launch();
+    const dim3 pgrid(ns / 2 + 1, nb);  // row pairs {kx, ns - kx}
     auto go = [&](auto kern, int n, int threads, int nv) -> int {
       const size_t smem = (size_t)(n + nv * fft_padded(n)) * sizeof(float2);
       if (int rc = set_smem(kern, smem, "k_frame_rows_uniform_reg")) return rc;
-      kern<<<grid, threads, smem, s>>>(g->tw, spectra, L, nf, ut, hn, img);
+      kern<<<pgrid, threads, smem, s>>>(g->tw, spectra, L, nf, ut, hn, img);
       return PT_OK;
     };
     if (ns == 256) return go(k_frame_rows_uniform_reg<LM, 256>, 256, 256, 8);
