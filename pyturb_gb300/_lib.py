@@ -68,6 +68,8 @@ SIGNATURES = {
     "pt_launch_count": (u64, []),
     "pt_prof_enable": (i32, [i32]),
     "pt_prof_report": (i32, [C.c_char_p, sz]),
+    "pt_device_error": (i32, [C.POINTER(C.c_int), i32]),
+    "pt_selftest_wait_timeout": (i32, [C.c_longlong, C.POINTER(C.c_int)]),
     "pt_grid_create": (i32, [C.POINTER(vp), i32, f64, i32, dptr]),
     "pt_grid_destroy": (i32, [vp]),
     "pt_grid_workspace_bytes": (sz, [vp, i32]),

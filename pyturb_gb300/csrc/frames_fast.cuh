@@ -233,30 +233,13 @@ k_pair_cols_reg(const float2* __restrict__ tw, const float2* __restrict__ work, 
 // transform those rows.
 // Separable anchor phasors Q(kx, ky) = Px(kx) Py(ky) per layer: px0/py0
 // (n_blocks, L, N) at each anchor block's first frame, rx/ry (L, N) per-frame
-// ratios; filled by k_uniform_tables from the exact fixed-point phases.
+// ratios; filled by k_uniform_prep from the exact fixed-point phases.
 struct UniformTables {
   const float2* px0;
   const float2* py0;
   const float2* rx;
   const float2* ry;
 };
-
-__global__ void k_uniform_tables(int N, int L, int nblocks, UniformParams up, float2* px0,
-                                 float2* py0, float2* rx, float2* ry) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  const int bl = blockIdx.y;  // (block, layer) or the ratio row (block == nblocks)
-  if (k >= N) return;
-  const int b = bl / L, l = bl % L;
-  const uint64_t kk = (uint64_t)(int64_t)signed_freq(k, N);
-  if (b < nblocks) {
-    const uint64_t f0 = (uint64_t)b * kAnchor;
-    px0[(size_t)bl * N + k] = phasor_from_fixed(kk * (up.ux0[l] + f0 * up.dux[l]));
-    py0[(size_t)bl * N + k] = phasor_from_fixed(kk * (up.uy0[l] + f0 * up.duy[l]));
-  } else {
-    rx[(size_t)l * N + k] = phasor_from_fixed(kk * up.dux[l]);
-    ry[(size_t)l * N + k] = phasor_from_fixed(kk * up.duy[l]);
-  }
-}
 
 template <int LM, int N>
 __global__ void __launch_bounds__(N < 512 ? N : 512)
@@ -378,5 +361,145 @@ k_frame_rows_uniform_reg(const float2* __restrict__ tw, const float2* __restrict
       for (int i = 0; i < 8; ++i) work[((size_t)pair * N + row) * N + j + T * i] = x[i];
     }
     __syncthreads();
+  }
+}
+
+// ------------------------------------------------------------------ uniform prep
+// Everything the uniform frame kernels need besides the spectra, in one launch
+// (block ranges select the role):
+//   tables  — separable anchor/ratio phasors (as k_uniform_tables);
+//   nyquist — exact Hermitian parts on the Nyquist cross for the anchor block
+//             of 32 frames, by the same geometric recurrence (one thread per
+//             cross element and block, 32 frame accumulators in registers);
+//   coef    — per frame, shifted subharmonic coefficients summed over layers
+//             and their grid mean (as k_frame_coef), with the shifts
+//             s0 + f delta formed in FP64.
+constexpr int kNyqGroup = 8;  // frames per Nyquist-cross thread (one exact anchor each)
+
+struct UniformPrep {
+  UniformParams up;
+  double s0x[kMaxUniformLayers], s0y[kMaxUniformLayers];
+  double dsx[kMaxUniformLayers], dsy[kMaxUniformLayers];
+  const float2* spectra;
+  const float2* sh_coef;  // (P, L, 3, 3)
+  const double* sh_freq;  // (P, 3)
+  const double* beta;     // (P, 3, 2)
+  float2* px0;
+  float2* py0;
+  float2* rx;
+  float2* ry;
+  float2* hn;    // (F, 2N)
+  float2* coef;  // (F, P, 9)
+  float* mean;   // (F)
+  int N, L, P, F, nb;
+  int blocks_tab, blocks_nyq;
+};
+
+__global__ void __launch_bounds__(256) k_uniform_prep(UniformPrep a) {
+  const int N = a.N, L = a.L;
+  int blk = blockIdx.x;
+  if (blk < a.blocks_tab) {  // ---- tables
+    const int idx = blk * blockDim.x + threadIdx.x;
+    if (idx >= (a.nb + 1) * L * N) return;
+    const int k = idx % N, bl = idx / N;
+    const int b = bl / L, l = bl % L;
+    const uint64_t kk = (uint64_t)(int64_t)signed_freq(k, N);
+    if (b < a.nb) {
+      const uint64_t f0 = (uint64_t)b * kAnchor;
+      a.px0[(size_t)bl * N + k] = phasor_from_fixed(kk * (a.up.ux0[l] + f0 * a.up.dux[l]));
+      a.py0[(size_t)bl * N + k] = phasor_from_fixed(kk * (a.up.uy0[l] + f0 * a.up.duy[l]));
+    } else {
+      a.rx[(size_t)l * N + k] = phasor_from_fixed(kk * a.up.dux[l]);
+      a.ry[(size_t)l * N + k] = phasor_from_fixed(kk * a.up.duy[l]);
+    }
+    return;
+  }
+  blk -= a.blocks_tab;
+  if (blk < a.blocks_nyq) {  // ---- Nyquist cross, kNyqGroup frames per thread
+    const int idx = blk * blockDim.x + threadIdx.x;
+    const int groups = (a.F + kNyqGroup - 1) / kNyqGroup;
+    if (idx >= 2 * N * groups) return;
+    const int e = idx % (2 * N), gi = idx / (2 * N);
+    const int kx = e < N ? N / 2 : e - N;
+    const int ky = e < N ? e : N / 2;
+    const int nkx = (N - kx) % N, nky = (N - ky) % N;
+    const int ka = signed_freq(kx, N), kb = signed_freq(ky, N);
+    const int na = signed_freq(nkx, N), nbf = signed_freq(nky, N);
+    const int fbeg = gi * kNyqGroup;
+    const int nfr = min(kNyqGroup, a.F - fbeg);
+    float2 h[kNyqGroup];
+#pragma unroll
+    for (int f = 0; f < kNyqGroup; ++f) h[f] = make_float2(0.f, 0.f);
+    // issue every layer's loads before any arithmetic (the loop below is a
+    // dependent chain; serial loads would dominate this short kernel)
+    float2 s1[kMaxUniformLayers], s2[kMaxUniformLayers];
+#pragma unroll
+    for (int l = 0; l < kMaxUniformLayers; ++l) {
+      if (l < L) {
+        s1[l] = a.spectra[((size_t)l * N + kx) * N + ky];
+        s2[l] = a.spectra[((size_t)l * N + nkx) * N + nky];
+      }
+    }
+#pragma unroll
+    for (int l = 0; l < kMaxUniformLayers; ++l) {
+      if (l >= L) break;
+      const uint64_t ux = a.up.ux0[l] + (uint64_t)fbeg * a.up.dux[l];
+      const uint64_t uy = a.up.uy0[l] + (uint64_t)fbeg * a.up.duy[l];
+      float2 x1 = cmul(s1[l], phasor2(ka, kb, ux, uy));
+      float2 x2 = cmul(s2[l], phasor2(na, nbf, ux, uy));
+      const float2 r1 = phasor2(ka, kb, a.up.dux[l], a.up.duy[l]);
+      const float2 r2 = phasor2(na, nbf, a.up.dux[l], a.up.duy[l]);
+#pragma unroll
+      for (int f = 0; f < kNyqGroup; ++f) {
+        h[f].x += 0.5f * (x1.x + x2.x);
+        h[f].y += 0.5f * (x1.y - x2.y);
+        x1 = cmul(x1, r1);
+        x2 = cmul(x2, r2);
+      }
+    }
+#pragma unroll
+    for (int f = 0; f < kNyqGroup; ++f)
+      if (f < nfr) a.hn[(size_t)(fbeg + f) * 2 * N + e] = h[f];
+    return;
+  }
+  blk -= a.blocks_nyq;
+  // ---- subharmonic coefficients of frame blk
+  __shared__ double part[8];
+  const int f = blk;
+  if (f >= a.F) return;
+  const int t = threadIdx.x;
+  double term = 0.0;
+  if (t < a.P * 9) {
+    const int p = t / 9, ij = t % 9, i = ij / 3, k = ij % 3;
+    const double fi = a.sh_freq[p * 3 + i], fk = a.sh_freq[p * 3 + k];
+    float2 acc = make_float2(0.f, 0.f);
+    float2 cf[kMaxUniformLayers];
+#pragma unroll
+    for (int l = 0; l < kMaxUniformLayers; ++l)
+      if (l < L) cf[l] = a.sh_coef[(((size_t)p * L + l) * 3 + i) * 3 + k];
+#pragma unroll
+    for (int l = 0; l < kMaxUniformLayers; ++l) {
+      if (l >= L) break;
+      const double sx = a.s0x[l] + (double)f * a.dsx[l];
+      const double sy = a.s0y[l] + (double)f * a.dsy[l];
+      double ph = fi * sx + fk * sy;
+      ph -= floor(ph);
+      float sn, cs;
+      sincospif(2.0f * (float)ph, &sn, &cs);
+      acc = cfma(cf[l], make_float2(cs, sn), acc);
+    }
+    a.coef[((size_t)f * a.P + p) * 9 + ij] = acc;
+    const double bir = a.beta[(p * 3 + i) * 2], bii = a.beta[(p * 3 + i) * 2 + 1];
+    const double bkr = a.beta[(p * 3 + k) * 2], bki = a.beta[(p * 3 + k) * 2 + 1];
+    const double br = bir * bkr - bii * bki, bi = bir * bki + bii * bkr;
+    term = (double)acc.x * br - (double)acc.y * bi;
+  }
+  for (int o = 16; o > 0; o >>= 1) term += __shfl_down_sync(0xffffffffu, term, o);
+  if ((t & 31) == 0) part[t >> 5] = term;
+  __syncthreads();
+  if (t == 0) {
+    double m = 0.0;
+    for (int w = 0; w < (int)(blockDim.x + 31) / 32; ++w) m += part[w];
+    a.mean[f] = (float)m;
   }
 }

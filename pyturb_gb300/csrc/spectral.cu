@@ -13,10 +13,13 @@
 // reference's own Re/Im pairing, frames are paired through their
 // Hermitian parts, H = (X(k) + conj X(-k)) / 2, so Re ifft2(X1) + i Re
 // ifft2(X2) = ifft2(H1 + i H2).
+#include <cuda.h>  // CUtensorMap (types only; the encoder comes from the runtime's entry point)
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
+#include <mutex>
 #include <vector>
 
 #include "common.cuh"
@@ -664,6 +667,7 @@ __global__ void k_lgs_zoom(int L, int ns, int n, int T, const int32_t* __restric
 }
 
 #include "frames_fast.cuh"  // power-of-two fast path kernels
+#include "cols_tma.cuh"     // TMA-fed column pass
 
 // ================================================================ host helpers
 static size_t rows_smem(int ns, int rpc) {
@@ -734,24 +738,7 @@ static int launch_uniform_t(const pt_grid* g, const float2* spectra, int L, int 
   }
   const dim3 grid(ns, (nf + kAnchor - 1) / kAnchor);
   ProfScope ps("k_frame_rows_uniform", s);
-  if (ns == 256 || ns == 512 || ns == 1024) {
-    const int nb = (nf + kAnchor - 1) / kAnchor;
-    UniformTables ut{ptab, ptab + (size_t)nb * L * ns, ptab + (size_t)2 * nb * L * ns,
-                     ptab + (size_t)(2 * nb + 1) * L * ns};
-    k_uniform_tables<<<dim3((ns + 127) / 128, (nb + 1) * L), 128, 0, s>>>(
-        ns, L, nb, up, (float2*)ut.px0, (float2*)ut.py0, (float2*)ut.rx, (float2*)ut.ry);
-    count_launch();
-    const dim3 pgrid(ns / 2 + 1, nb);  // row pairs {kx, ns - kx}
-    auto go = [&](auto kern, int n, int threads, int nv) -> int {
-      const size_t smem = (size_t)(n + nv * fft_padded(n)) * sizeof(float2);
-      if (int rc = set_smem(kern, smem, "k_frame_rows_uniform_reg")) return rc;
-      kern<<<pgrid, threads, smem, s>>>(g->tw, spectra, L, nf, ut, hn, img);
-      return PT_OK;
-    };
-    if (ns == 256) return go(k_frame_rows_uniform_reg<LM, 256>, 256, 256, 8);
-    if (ns == 512) return go(k_frame_rows_uniform_reg<LM, 512>, 512, 512, 8);
-    return go(k_frame_rows_uniform_reg<LM, 1024>, 1024, 512, 4);
-  }
+  (void)ptab;  // the power-of-two sizes 256/512/1024 take launch_uniform_reg_chunk instead
   const size_t smem = (size_t)(2 * kPairsPerFft * (ns + 1) + ns) * sizeof(float2);
   if (ns <= 512) {
     if (int rc = set_smem(k_frame_rows_uniform<LM, 1>, smem, "k_frame_rows_uniform")) return rc;
@@ -787,6 +774,80 @@ static int launch_uniform_rows(const pt_grid* g, const float2* spectra, int L, c
   if (L <= 9) return launch_uniform_t<9>(g, spectra, L, nf, up, hn, ptab, img, s);
   if (L <= 12) return launch_uniform_t<12>(g, spectra, L, nf, up, hn, ptab, img, s);
   return launch_uniform_t<16>(g, spectra, L, nf, up, hn, ptab, img, s);
+}
+
+// ---- uniform frames on the 256/512/1024 register path: one prep launch + rows
+template <int LM>
+static int uniform_reg_rows_t(const pt_grid* g, const float2* spectra, int L, int nf,
+                              const UniformTables& ut, const float2* hn, float2* img,
+                              cudaStream_t s) {
+  const int ns = g->ns;
+  const dim3 pgrid(ns / 2 + 1, (nf + kAnchor - 1) / kAnchor);  // row pairs {kx, ns - kx}
+  auto go = [&](auto kern, int threads, int nv) -> int {
+    const size_t smem = (size_t)(ns + nv * fft_padded(ns)) * sizeof(float2);
+    if (int rc = set_smem(kern, smem, "k_frame_rows_uniform_reg")) return rc;
+    ProfScope ps("k_frame_rows_uniform", s);
+    kern<<<pgrid, threads, smem, s>>>(g->tw, spectra, L, nf, ut, hn, img);
+    return PT_OK;
+  };
+  if (ns == 256) return go(k_frame_rows_uniform_reg<LM, 256>, 256, 8);
+  if (ns == 512) return go(k_frame_rows_uniform_reg<LM, 512>, 512, 8);
+  return go(k_frame_rows_uniform_reg<LM, 1024>, 512, 4);
+}
+
+static int launch_uniform_reg_chunk(const pt_grid* g, const float2* spectra, const float2* sh_coef,
+                                    int L, const double* sx, const double* sy, int f0, int nf,
+                                    const SpecWork& w, cudaStream_t s) {
+  const int ns = g->ns;
+  const double df = 1.0 / (ns * g->dx);
+  UniformPrep a{};
+  for (int l = 0; l < L; ++l) {
+    const double x0 = sx[(size_t)f0 * L + l], y0 = sy[(size_t)f0 * L + l];
+    const double dx = (sx[(size_t)(f0 + nf - 1) * L + l] - x0) / (nf - 1);
+    const double dy = (sy[(size_t)(f0 + nf - 1) * L + l] - y0) / (nf - 1);
+    a.up.ux0[l] = host_fixed(x0 * df);
+    a.up.uy0[l] = host_fixed(y0 * df);
+    a.up.dux[l] = host_fixed(dx * df);
+    a.up.duy[l] = host_fixed(dy * df);
+    a.s0x[l] = x0;
+    a.s0y[l] = y0;
+    a.dsx[l] = dx;
+    a.dsy[l] = dy;
+  }
+  const int nb = (nf + kAnchor - 1) / kAnchor;
+  float2* ptab = w.px;
+  a.px0 = ptab;
+  a.py0 = ptab + (size_t)nb * L * ns;
+  a.rx = ptab + (size_t)2 * nb * L * ns;
+  a.ry = ptab + (size_t)(2 * nb + 1) * L * ns;
+  a.spectra = spectra;
+  a.sh_coef = sh_coef;
+  a.sh_freq = g->sh_freq;
+  a.beta = g->beta;
+  a.hn = w.hn;
+  a.coef = w.coef;
+  a.mean = w.mean;
+  a.N = ns;
+  a.L = L;
+  a.P = g->P;
+  a.F = nf;
+  a.nb = nb;
+  a.blocks_tab = ((nb + 1) * L * ns + 255) / 256;
+  a.blocks_nyq = (2 * ns * ((nf + kNyqGroup - 1) / kNyqGroup) + 255) / 256;
+  {
+    ProfScope ps("k_uniform_prep", s);
+    k_uniform_prep<<<a.blocks_tab + a.blocks_nyq + nf, 256, 0, s>>>(a);
+  }
+  count_launch();
+  const UniformTables ut{a.px0, a.py0, a.rx, a.ry};
+  if (L <= 1) return uniform_reg_rows_t<1>(g, spectra, L, nf, ut, w.hn, w.img, s);
+  if (L <= 2) return uniform_reg_rows_t<2>(g, spectra, L, nf, ut, w.hn, w.img, s);
+  if (L <= 3) return uniform_reg_rows_t<3>(g, spectra, L, nf, ut, w.hn, w.img, s);
+  if (L <= 4) return uniform_reg_rows_t<4>(g, spectra, L, nf, ut, w.hn, w.img, s);
+  if (L <= 6) return uniform_reg_rows_t<6>(g, spectra, L, nf, ut, w.hn, w.img, s);
+  if (L <= 9) return uniform_reg_rows_t<9>(g, spectra, L, nf, ut, w.hn, w.img, s);
+  if (L <= 12) return uniform_reg_rows_t<12>(g, spectra, L, nf, ut, w.hn, w.img, s);
+  return uniform_reg_rows_t<16>(g, spectra, L, nf, ut, w.hn, w.img, s);
 }
 
 // ---- power-of-two dispatch (runtime ns -> template N)
@@ -853,8 +914,72 @@ static int pair_cols_reg_t(const pt_grid* g, const float2* work, int npair, int 
   return PT_OK;
 }
 
+// ---- TMA-fed column pass (N = 256, 512, 1024)
+typedef CUresult (*TensorMapEncodeFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                      const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                      const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                      CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static TensorMapEncodeFn tensor_map_encoder() {
+  static std::once_flag once;
+  static TensorMapEncodeFn fn = nullptr;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<TensorMapEncodeFn>(p);
+  });
+  return fn;
+}
+
+template <int N>
+static int pair_cols_tma_t(const pt_grid* g, const float2* work, int npair, int pair0,
+                           const PairStore& st, cudaStream_t s) {
+  using Cfg = TmaCfg<N>;
+  TensorMapEncodeFn enc = tensor_map_encoder();
+  if (!enc) return fail(PT_ERR_UNSUPPORTED, "cuTensorMapEncodeTiled unavailable");
+  // 2-D view of the (npair, N, N) complex workspace: x = column (inner), y = pair * N + row
+  CUtensorMap map;
+  const cuuint64_t dims[2] = {(cuuint64_t)N, (cuuint64_t)npair * N};
+  const cuuint64_t strides[1] = {(cuuint64_t)N * sizeof(float2)};
+  const cuuint32_t box[2] = {(cuuint32_t)Cfg::C, (cuuint32_t)Cfg::BOXR};
+  const cuuint32_t estr[2] = {1, 1};
+  const CUresult r = enc(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2, (void*)work, dims, strides, box,
+                         estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                         CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return fail(PT_ERR_CUDA, "cuTensorMapEncodeTiled failed");
+  const int P1 = std::max(g->P, 1);
+  const size_t smem =
+      (size_t)(3 * N * Cfg::C + N + 2 * 3 * P1 * Cfg::C) * sizeof(float2) + 2 * sizeof(uint64_t);
+  if (int rc = set_smem(k_pair_cols_tma<N>, smem, "k_pair_cols_tma")) return rc;
+  const int xb = N / Cfg::C;
+  const int groups = std::max(1, std::min(npair, (2 * 152 + xb - 1) / xb));
+  ProfScope ps("k_pair_cols", s);
+  k_pair_cols_tma<N><<<dim3(xb, groups), RegCfg<N>::THREADS, smem, s>>>(map, g->tw, npair, pair0,
+                                                                        st);
+  return PT_OK;
+}
+
+// The TMA-fed column pass is selected with PYTURB_GB300_COLS=tma (N = 256, 512,
+// 1024). Measured on the GB300 it trails the one-CTA-per-tile register pass,
+// whose 2048 short CTAs keep more loads in flight, so the latter is the default.
+static bool cols_tma_selected() {
+  static const bool on = [] {
+    const char* v = std::getenv("PYTURB_GB300_COLS");
+    return v && std::string(v) == "tma";
+  }();
+  return on;
+}
+
 static int pair_cols_reg(const pt_grid* g, const float2* work, int npair, int pair0,
                          const PairStore& st, cudaStream_t s) {
+  if (cols_tma_selected()) {
+    if (g->ns == 256) return pair_cols_tma_t<256>(g, work, npair, pair0, st, s);
+    if (g->ns == 512) return pair_cols_tma_t<512>(g, work, npair, pair0, st, s);
+    if (g->ns == 1024) return pair_cols_tma_t<1024>(g, work, npair, pair0, st, s);
+  }
   switch (g->ns) {
 #define PT_CASE(n) \
   case n: return pair_cols_reg_t<n>(g, work, npair, pair0, st, s);
@@ -865,6 +990,38 @@ static int pair_cols_reg(const pt_grid* g, const float2* work, int npair, int pa
 }
 
 }  // namespace pt
+
+using namespace pt;
+
+// Device error word set by bounded waits that ran out (0 = none).
+extern "C" int pt_device_error(int* out, int clear) {
+  if (!out) return fail(PT_ERR_ARG, "pt_device_error: out is NULL");
+  if (int rc = check_cuda(cudaDeviceSynchronize(), "pt_device_error: sync")) return rc;
+  if (int rc = check_cuda(cudaMemcpyFromSymbol(out, g_pt_device_error, sizeof(int)),
+                          "pt_device_error: read"))
+    return rc;
+  if (clear) {
+    const int zero = 0;
+    if (int rc = check_cuda(cudaMemcpyToSymbol(g_pt_device_error, &zero, sizeof(int)),
+                            "pt_device_error: clear"))
+      return rc;
+  }
+  return PT_OK;
+}
+
+extern "C" int pt_selftest_wait_timeout(long long limit, int* timed_out) {
+  if (!timed_out || limit < 1 || limit > (1ll << 24))
+    return fail(PT_ERR_ARG, "pt_selftest_wait_timeout: bad arguments");
+  int* d = nullptr;
+  if (int rc = check_cuda(cudaMalloc(&d, sizeof(int)), "pt_selftest_wait_timeout: cudaMalloc"))
+    return rc;
+  k_selftest_wait_timeout<<<1, 32>>>(limit, d);
+  int rc = check_launch("pt_selftest_wait_timeout");
+  if (!rc) rc = check_cuda(cudaMemcpy(timed_out, d, sizeof(int), cudaMemcpyDeviceToHost),
+                           "pt_selftest_wait_timeout: read");
+  cudaFree(d);
+  return rc;
+}
 
 using namespace pt;
 
@@ -1122,7 +1279,15 @@ extern "C" int pt_frames(const pt_grid* g, int L, const float* spectra, const fl
     pa.per_layer = per_layer;
     pa.frame0 = f0;
     pa.df = 1.0 / (ns * g->dx);
-    for (int fb = 0; fb < nf; fb += fsub) {
+    const bool uni = uniform_ok(sx, sy, per_layer, L, f0, nf, ns);
+    const bool uni_reg = uni && (ns == 256 || ns == 512 || ns == 1024);
+    if (uni_reg) {
+      // one prep launch (tables, Nyquist cross, subharmonics) + the fused rows kernel
+      if (int rc = launch_uniform_reg_chunk(g, (const float2*)spectra, (const float2*)sh_coef, L,
+                                            sx, sy, f0, nf, w, s))
+        return rc;
+    }
+    for (int fb = 0; fb < nf && !uni_reg; fb += fsub) {
       const int nb = std::min(fsub, nf - fb);
       ShiftParams sp;
       for (int f = 0; f < nb; ++f)
@@ -1136,12 +1301,14 @@ extern "C" int pt_frames(const pt_grid* g, int L, const float* spectra, const fl
         k_frame_coef<<<nb, 32 * ((P * 9 + 31) / 32), 0, s>>>(pa, sp, fb, nb);
         count_launch();
       }
-      if (uniform_ok(sx, sy, per_layer, L, f0, nf, ns)) continue;  // no phasor tables needed
+      if (uni) continue;  // no phasor tables needed
       ProfScope ps("k_frame_phasors", s);
       k_frame_phasors<<<dim3((ns + 255) / 256, nb * J), 256, 0, s>>>(pa, sp, fb);
       count_launch();
     }
-    if (uniform_ok(sx, sy, per_layer, L, f0, nf, ns)) {
+    if (uni_reg) {
+      // rows done above
+    } else if (uni) {
       if (int rc = launch_uniform_rows(g, (const float2*)spectra, L, sx, sy, f0, nf, w.hn, w.px,
                                        w.img, s))
         return rc;
