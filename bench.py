@@ -138,6 +138,85 @@ def cpu_reference(frames: int, mc_count: int, budget_s: float = 12.0):
     return fps, sps, cores, done, drawn
 
 
+def bench_generate(torch, G):
+    """PhaseScreen.generate(64) at 256^2 (D = 8 m, r0 = 0.15, L0 = 25, 3 levels): screens/s."""
+    gen = G.PhaseScreen(n=256, pixel_scale=8.0 / 256, r0=0.15, L0=25.0, subharmonics=3, seed=5)
+    out = torch.empty((64, 256, 256), dtype=torch.float32, device="cuda")
+    for _ in range(3):
+        gen._generate_into(out, 64, 0, 256, 1.0, False)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 50
+    e0.record()
+    for _ in range(reps):
+        gen._generate_into(out, 64, 0, 256, 1.0, False)
+    e1.record()
+    torch.cuda.synchronize()
+    return reps * 64 / (e0.elapsed_time(e1) / 1000.0)
+
+
+def bench_extrude(torch, G, steps: int = 128):
+    """Assemat-Wilson extrusion at n = 1024, 9 layers x 16 realisations = 144 ring
+    screens (one [A | B] GEMM per row step, M = W, N = 144, K = 3W), and the fused
+    9-layer bilinear readout of one realisation at 1024^2."""
+    from pyturb_gb300 import _lib
+    from pyturb_gb300.backend import NoiseStream, stream_handle
+    from pyturb_gb300.extrude import RingExtruder
+
+    tab = layer_table()
+    n = 1024
+    cos_z = np.cos(np.deg2rad(ZENITH))
+    frac = np.array(FRACTIONS) / np.sum(FRACTIONS)
+    r0s = [R0 * cos_z ** 0.6 * f ** (-0.6) for f in frac]
+    winds = [(v * np.cos(np.deg2rad(d)), v * np.sin(np.deg2rad(d))) for _, _, v, d in tab]
+    t0 = time.perf_counter()
+    ext = G.ExtrudedAtmosphere(n=n, pixel_scale=DIAM / n, layer_r0=r0s, layer_L0=[L0] * 9,
+                               layer_wind=winds, layer_altitude_los=[h / cos_z for h in HEIGHTS],
+                               interp="linear", seeds=list(range(9)))
+    setup_s = time.perf_counter() - t0
+    W, cap = ext.width, ext.capacity
+    R = 16
+    S = 9 * R
+    streams = [NoiseStream(100 + s, None) for s in range(S)]
+    ring = RingExtruder(W, 2, cap, [], [0] * S, [r ** (-5.0 / 6.0) for r in r0s] * R, streams,
+                        device_operator=ext._ring.M)
+    for s in range(S):  # every realisation starts from layer (s % 9)'s seeded rows
+        ring.buf[s].copy_(ext._ring.buf[s % 9])
+        ring.top[s] = ext._ring.top[s % 9]
+    ones = np.ones(S, dtype=np.int32)
+    for _ in range(3):
+        ring.extrude(ones)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    ring.extrude(steps * ones)
+    e1.record()
+    torch.cuda.synchronize()
+    step_s = e0.elapsed_time(e1) / 1000.0 / steps
+    flops = 2.0 * W * 3 * W * S
+    # readout: the 9 layers of one realisation, bilinear, at 1024^2
+    out = torch.empty((n, n), dtype=torch.float32, device="cuda")
+    ext.set_time(0.01)
+    params = ext.readout_params()
+    for _ in range(3):
+        ext.integrate(out=out)
+    torch.cuda.synchronize()
+    e0.record()
+    reps = 50
+    for _ in range(reps):
+        _lib.call("pt_readout", n, W, cap, 0, 9, params, ext._buf.data_ptr(), 1.0,
+                  out.data_ptr(), stream_handle())
+    e1.record()
+    torch.cuda.synchronize()
+    ro_s = e0.elapsed_time(e1) / 1000.0 / reps
+    return {"workload": f"n=1024, 9 layers x {R} realisations ({S} screens), W={W}, "
+                        f"stencil 2 rows, {steps} row steps timed; readout bilinear 9 layers",
+            "row_steps_per_s": 1.0 / step_s, "gemm_tflops": flops / step_s / 1e12,
+            "readout_frames_per_s": 1.0 / ro_s,
+            "readout_gbs_out": n * n * 4 / ro_s / 1e9, "host_setup_s": setup_s,
+            "note": "split-K SIMT FP32 GEMM (plain form)"}
+
+
 def run_reference(args, rank: int) -> None:
     if rank != 0:
         return
@@ -175,6 +254,7 @@ def main() -> None:
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extrude", action="store_true")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
 
@@ -340,6 +420,9 @@ def main() -> None:
         "clocks": clk,
         "wall_s_timed_region": wall,
     }
+    line["generate_256_screens_per_s"] = bench_generate(torch, G)
+    if not args.no_extrude:
+        line["extrude_1024"] = bench_extrude(torch, G)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         fps, sps, cores, done, drawn = cpu_reference(200, MC_BATCH, 12.0)
         line["cpu_baseline"] = {

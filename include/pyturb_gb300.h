@@ -171,6 +171,19 @@ typedef struct {
 
 size_t pt_extrude_workspace_bytes(int W, int m, int max_jobs_per_step);
 
+/* The same steps for S screens given as arrays (host): screen s extrudes
+ * counts[s] rows, its k-th at virtual row top[s] + k (ring row modulo cap,
+ * Philox counter = virtual row, key key[s]), scaled by bscale[s], operator
+ * group[s]; top[] is advanced in place. Injected noise, when given, holds W
+ * normals per row in step-major order (step k of screen s before step k of
+ * screen s+1, all step-k rows before step k+1). Replaces the per-row loop of
+ * _ExtrudeLayer._ensure (src/pyturb/extrude.py:446-449) for all layers and
+ * realisations at once. */
+int pt_extrude_batch(int W, int m, int cap, int n_groups, const float* M, float* buf, int S,
+                     const int32_t* group, const float* bscale, const uint64_t* key,
+                     int64_t* top, const int32_t* counts, const float* noise, void* work,
+                     size_t work_bytes, void* stream);
+
 int pt_extrude_rows(int W, int m, int cap, int n_groups, const float* M, float* buf,
                     int n_jobs, const pt_extrude_job* jobs, const float* noise, void* work,
                     size_t work_bytes, void* stream);

@@ -83,6 +83,8 @@ SIGNATURES = {
     "pt_extrude_workspace_bytes": (sz, [i32, i32, i32]),
     "pt_extrude_rows": (i32, [i32, i32, i32, i32, vp, vp, i32, C.POINTER(ExtrudeJob), vp, vp,
                               sz, vp]),
+    "pt_extrude_batch": (i32, [i32, i32, i32, i32, vp, vp, i32, vp, vp, vp, vp, vp, vp, vp, sz,
+                               vp]),
     "pt_readout": (i32, [i32, i32, i32, i32, i32, C.POINTER(ReadoutLayer), vp, f32, vp, vp]),
     "pt_rows_sample": (i32, [i32, i32, i32, i32, i32, f64, vp, vp, vp]),
 }

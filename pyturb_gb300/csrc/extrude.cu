@@ -338,6 +338,41 @@ extern "C" int pt_extrude_rows(int W, int m, int cap, int G, const float* M, flo
   return PT_OK;
 }
 
+extern "C" int pt_extrude_batch(int W, int m, int cap, int n_groups, const float* M, float* buf,
+                                int S, const int32_t* group, const float* bscale,
+                                const uint64_t* key, int64_t* top, const int32_t* counts,
+                                const float* noise, void* work, size_t work_bytes,
+                                void* stream) {
+  if (S < 1 || !group || !bscale || !key || !top || !counts)
+    return fail(PT_ERR_ARG, "pt_extrude_batch: bad screen arrays");
+  int steps = 0;
+  for (int s = 0; s < S; ++s) {
+    if (counts[s] < 0 || top[s] < 0) return fail(PT_ERR_ARG, "pt_extrude_batch: negative count");
+    steps = std::max(steps, (int)counts[s]);
+  }
+  std::vector<pt_extrude_job> jobs;
+  jobs.reserve((size_t)S * steps);
+  int64_t noff = 0;
+  for (int k = 0; k < steps; ++k)
+    for (int s = 0; s < S; ++s) {
+      if (k >= counts[s]) continue;
+      pt_extrude_job j{};
+      j.screen = s;
+      j.group = group[s];
+      j.head = (int32_t)(top[s] % cap);
+      j.step = k;
+      j.bscale = bscale[s];
+      j.key = key[s];
+      j.row = (uint64_t)top[s];
+      j.noise_off = noff;
+      noff += W;
+      top[s] += 1;
+      jobs.push_back(j);
+    }
+  return pt_extrude_rows(W, m, cap, n_groups, M, buf, (int)jobs.size(), jobs.data(), noise, work,
+                         work_bytes, stream);
+}
+
 extern "C" int pt_readout(int n, int W, int cap, int interp, int L, const pt_readout_layer* layers,
                           const float* buf, float scale, float* out, void* stream) {
   if (n < 1 || W < 1 || cap < 1 || L < 1) return fail(PT_ERR_ARG, "pt_readout: bad sizes");

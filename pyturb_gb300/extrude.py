@@ -123,22 +123,29 @@ class RingExtruder:
     s uses operator group ``groups[s]`` scaled by ``bscale[s]``."""
 
     def __init__(self, W: int, m: int, cap: int, operators: List[Tuple[np.ndarray, np.ndarray]],
-                 groups: Sequence[int], bscale: Sequence[float], streams: Sequence[NoiseStream]):
+                 groups: Sequence[int], bscale: Sequence[float], streams: Sequence[NoiseStream],
+                 device_operator=None):
         torch = torch_module()
         self.W, self.m, self.cap = int(W), int(m), int(cap)
         self.S = len(groups)
         self.groups = [int(g) for g in groups]
         self.bscale = [float(b) for b in bscale]
         self.streams = list(streams)
-        M = np.stack([np.concatenate([a, b], axis=1) for a, b in operators])  # (G, W, (m+1)W)
-        self.G = M.shape[0]
-        self.M = upload(M)
+        if device_operator is not None:  # an existing (G, W, (m+1)W) float32 CUDA tensor
+            self.M = device_operator
+        else:
+            M = np.stack([np.concatenate([a, b], axis=1) for a, b in operators])
+            self.M = upload(M)
+        self.G = int(self.M.shape[0])
         self.buf = torch.empty((self.S, self.cap, self.W), dtype=torch.float32,
                                device=cuda_device())
-        self.top = [0] * self.S  # rows extruded so far (relative virtual rows [0, top))
+        # rows extruded so far per screen (relative virtual rows [0, top))
+        self.top = np.zeros(self.S, dtype=np.int64)
+        self._group = np.asarray(self.groups, dtype=np.int32)
+        self._bscale = np.asarray(self.bscale, dtype=np.float32)
+        self._key = np.asarray([st.key for st in self.streams], dtype=np.uint64)
         self.work_bytes = 0
         self.work = None
-        self._jobs_cap = 0
 
     def _ensure_work(self, jobs_per_step: int) -> None:
         need = int(_lib.load().pt_extrude_workspace_bytes(self.W, self.m, max(1, jobs_per_step)))
@@ -154,40 +161,23 @@ class RingExtruder:
         self.top[s] = k
 
     def extrude(self, counts: Sequence[int]) -> None:
-        """Extrude ``counts[s]`` new rows on every screen s, in as many row steps
-        as the largest count; each step is one native call chain."""
-        steps = max(counts) if len(counts) else 0
+        """Extrude ``counts[s]`` new rows on every screen s (one native call:
+        as many row steps as the largest count, all screens of a step batched)."""
+        counts = np.ascontiguousarray(counts, dtype=np.int32).reshape(self.S)
+        steps = int(counts.max()) if counts.size else 0
         if steps <= 0:
             return
-        jobs = []
-        noise_rows = []
-        injected = any(st.injected for st in self.streams)
-        for k in range(steps):
-            for s in range(self.S):
-                if k >= counts[s]:
-                    continue
-                st = self.streams[s]
-                row = self.top[s]
-                j = _lib.ExtrudeJob()
-                j.screen = s
-                j.group = self.groups[s]
-                j.head = row % self.cap
-                j.step = k
-                j.bscale = self.bscale[s]
-                j.key = st.key
-                j.row = row
-                if injected:
-                    j.noise_off = len(noise_rows) * self.W
-                    noise_rows.append(st.draw((self.W,)))
-                jobs.append(j)
-                self.top[s] = row + 1
-        per_step = max(sum(1 for c in counts if c > k) for k in range(steps))
-        self._ensure_work(per_step)
-        arr = (_lib.ExtrudeJob * len(jobs))(*jobs)
-        noise = upload(np.stack(noise_rows)) if injected else None
-        _lib.call("pt_extrude_rows", self.W, self.m, self.cap, self.G, dptr(self.M),
-                  dptr(self.buf), len(jobs), arr, dptr(noise), dptr(self.work),
-                  self.work_bytes, stream_handle())
+        noise = None
+        if any(st.injected for st in self.streams):
+            rows = [self.streams[s].draw((self.W,))
+                    for k in range(steps) for s in range(self.S) if k < counts[s]]
+            noise = upload(np.stack(rows))
+        self._ensure_work(int((counts > 0).sum()))
+        ptr = lambda a: a.ctypes.data  # noqa: E731
+        _lib.call("pt_extrude_batch", self.W, self.m, self.cap, self.G, dptr(self.M),
+                  dptr(self.buf), self.S, ptr(self._group), ptr(self._bscale), ptr(self._key),
+                  ptr(self.top), ptr(counts), dptr(noise), dptr(self.work), self.work_bytes,
+                  stream_handle())
 
 
 class _LayerGeom:
