@@ -57,6 +57,20 @@ def peaks():
     return 6800.0, 1900.0, "fallback"
 
 
+def captured_traffic(kernel: str, frames_per_launch: float):
+    """DRAM bytes per launch of ``kernel`` from the committed ncu capture
+    (``profiles/dram_traffic.json``), scaled to ``frames_per_launch``; the
+    kernels' traffic grows in proportion to the frames a launch renders."""
+    p = ROOT / "profiles" / "dram_traffic.json"
+    if not p.exists():
+        return None
+    d = json.loads(p.read_text())
+    b = d.get("bytes_per_launch", {}).get(kernel)
+    if b is None:
+        return None
+    return float(b) * frames_per_launch / float(d["frames_per_launch"])
+
+
 class Clocks:
     """nvidia-smi SM clock / throttle sampling during the timed region."""
 
@@ -395,13 +409,24 @@ def main() -> None:
     fp32_peak = 152 * 128 * 2 * 2.07e9 / 1e12  # TFLOP/s, SIMT FP32 at max SM clock (nominal)
     roofline = {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": hbm,
                 "unit": "GB/s", "frac": (achieved / hbm) if achieved else None,
-                "traffic": None, "peak_source": f"MEASURED_PEAKS.json hbm_gbs ({peak_kind})",
+                "traffic": captured_traffic(name, frames_per_launch),
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one "
+                                  "64-frame launch (profiles/dram_traffic.json), scaled to "
+                                  "the frames per launch; L2-resident writes not counted",
+                "peak_source": f"MEASURED_PEAKS.json hbm_gbs ({peak_kind})",
                 "algorithmic_bytes_per_launch": algo[0],
                 "fp32_tflops": algo[1] / sec / 1e12 if algo[1] else None,
                 "fp32_frac_of_nominal": (algo[1] / sec / 1e12 / fp32_peak) if algo[1] else None,
                 "kernel_share": {k: round(v[1] / max(1e-9, sum(x[1] for x in prof.values())), 4)
                                  for k, v in prof.items()},
                 "kernel_ms_per_launch": {k: v[1] / v[0] for k, v in prof.items()}}
+    # the per-frame bytes of the reference's formulation (all L stored spectra read
+    # and one frame written per frame), over the whole step; the recurrence here
+    # does not re-read the spectra per frame, so this exceeds the DRAM traffic
+    ref_bpf = L * ns * ns * 8 + N_PIX * N_PIX * 4
+    roofline["reference_formulation"] = {
+        "bytes_per_frame": ref_bpf, "achieved_gbs": ref_bpf * value / world / 1e9,
+        "frac": ref_bpf * value / world / 1e9 / hbm}
 
     line = {
         "metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": world,
