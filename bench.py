@@ -231,6 +231,72 @@ def bench_extrude(torch, G, steps: int = 128):
             "note": "split-K SIMT FP32 GEMM (plain form)"}
 
 
+def bench_diff(torch, G, iters: int = 3):
+    """Differentiable readout: 9 layers of 768^2 screens (generate-coloured),
+    8 directions in a 60 arcsec disc + 1 LGS at 90 km, 512^2 pupil, batch 32,
+    64 frames at 1 ms; MSE to a target rendered with perturbed Cn2 weights and
+    winds; one Adam step on 9 weights + 18 wind components per iteration
+    (forward, loss, backward wrt screens, weights and winds, update)."""
+    from pyturb_gb300 import _lib
+    from pyturb_gb300.diff import DifferentiableReadout
+
+    B, L, S, n, T = 32, 9, 768, 512, 64
+    dx = DIAM / n
+    rng = np.random.default_rng(77)
+    rad = np.deg2rad(60.0 / 3600.0) * np.sqrt(rng.uniform(0, 1, 8))
+    ang = rng.uniform(0, 2 * np.pi, 8)
+    dirs = np.concatenate([np.stack([rad * np.cos(ang), rad * np.sin(ang)], 1), [[0.0, 0.0]]])
+    ro = DifferentiableReadout(n, S, dx, HEIGHTS, dirs, np.arange(T) * DT,
+                               source_altitudes=[None] * 8 + [90e3])
+    gen = G.PhaseScreen(n=S, pixel_scale=dx, r0=R0, L0=L0, subharmonics=LEVELS, seed=9)
+    screens = gen.generate(B * L).reshape(B, L, S, S).contiguous()
+    tab = layer_table()
+    v_true = torch.tensor([[v * np.cos(np.deg2rad(d)), v * np.sin(np.deg2rad(d))]
+                           for _, _, v, d in tab], dtype=torch.float64, device="cuda")
+    w_true = torch.tensor(np.sqrt(FRACTIONS), dtype=torch.float32, device="cuda")
+    with torch.no_grad():
+        target = ro(screens, w_true * torch.tensor(rng.uniform(0.8, 1.2, L), dtype=torch.float32,
+                                                    device="cuda"),
+                    v_true + torch.tensor(rng.normal(0, 1.0, (L, 2)), device="cuda"))
+    screens.requires_grad_(True)
+    w = w_true.clone().requires_grad_(True)
+    v = v_true.clone().requires_grad_(True)
+    opt = torch.optim.Adam([w, v], lr=0.01)
+
+    def step():
+        opt.zero_grad(set_to_none=True)
+        screens.grad = None
+        loss = torch.nn.functional.mse_loss(ro(screens, w, v), target)
+        loss.backward()
+        opt.step()
+        return loss
+
+    for _ in range(2):
+        step()
+    torch.cuda.synchronize()
+    _lib.prof_report()
+    _lib.prof_enable(True)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(iters):
+        loss = step()
+    e1.record()
+    torch.cuda.synchronize()
+    prof = _lib.prof_report()
+    _lib.prof_enable(False)
+    it_s = e0.elapsed_time(e1) / 1000.0 / iters
+    units = B * T  # (batch, frame) pairs per iteration
+    fwd_b = L * S * S * 4 + 9 * n * n * 4  # algorithmic bytes per (batch, frame), forward
+    k = {name: v[1] / v[0] / 1000.0 for name, v in prof.items()}
+    fwd_s = k.get("k_lr_forward", float("nan"))
+    return {"workload": "9 layers 768^2 x batch 32, 8 NGS dirs in 60\" + 1 LGS at 90 km, "
+                        "pupil 512^2, 64 frames, MSE + Adam on 9 weights + 18 winds",
+            "iter_ms": it_s * 1e3, "frames_per_s": units / it_s,
+            "kernel_ms": {name: v * 1e3 for name, v in k.items()},
+            "forward_gbs_algorithmic": units * fwd_b / fwd_s / 1e9,
+            "loss": float(loss.detach())}
+
+
 def run_reference(args, rank: int) -> None:
     if rank != 0:
         return
@@ -269,6 +335,7 @@ def main() -> None:
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extrude", action="store_true")
+    ap.add_argument("--no-diff", action="store_true")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
 
@@ -448,6 +515,8 @@ def main() -> None:
     line["generate_256_screens_per_s"] = bench_generate(torch, G)
     if not args.no_extrude:
         line["extrude_1024"] = bench_extrude(torch, G)
+    if not args.no_diff:
+        line["diff_readout_768"] = bench_diff(torch, G)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         fps, sps, cores, done, drawn = cpu_reference(200, MC_BATCH, 12.0)
         line["cpu_baseline"] = {

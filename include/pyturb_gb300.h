@@ -216,6 +216,39 @@ int pt_readout(int n, int W, int cap, int interp, int n_layers, const pt_readout
 int pt_rows_sample(int n, int cap, int interp, int anchor_phys, int row_max, double shift,
                    const float* buf, float* out, void* stream);
 
+/* ---- differentiable multi-layer readout --------------------------------
+ * out[b,t,d,i,j] = sum_l w[l] * bilerp(screens[b,l], u_r, u_c) with
+ * u_r = pos0[t,d,l,0] + mag[d,l] * i, u_c = pos0[t,d,l,1] + mag[d,l] * j,
+ * periodic on the S x S screen. The geometry is the LGS cone zoom of
+ * Atmosphere._build_lgs_zoom / _lgs_zoom (src/pyturb/atmosphere.py:581-616,
+ * 1048-1090) with the displacement of _integrate_lgs (atmosphere.py:1012-1022)
+ * applied as a bilinear shift. The reference has no adjoint: the gradient
+ * entry points have no counterpart there.
+ *
+ * Layouts: screens (B, L, S, S) f32; w (L,) f32; pos0 (T, D, L, 2) f64
+ * (device); mag (D, L) f64 (HOST, in [0.25, 4], mag*(n-1) + 2 < S);
+ * out / grad_out (B, T, D, n, n) f32. fix is a device workspace of
+ * 3*T*D*L int64 filled by pt_lr_fix: the positions in 32.32 fixed point, so
+ * the forward and the adjoints form identical taps. */
+int pt_lr_fix(int T, int D, int L, int S, int n, const double* pos0, const double* mag,
+              int64_t* fix, void* stream);
+int pt_lr_forward(int B, int L, int S, int T, int D, int n, const double* mag,
+                  const float* screens, const float* w, const int64_t* fix, float* out,
+                  void* stream);
+/* Number of floats in the partial-sum buffer of pt_lr_grad_params:
+ * (B, T*D, ceil(n/64), L, 3) = per (image, band of 64 rows, layer):
+ * [sum g*val, w*sum g*dval/du_r, w*sum g*dval/du_c]. Summing over b, t, d and
+ * bands gives dL/dw; summing over b and bands gives dL/dpos0. */
+size_t pt_lr_partial_count(int B, int L, int T, int D, int n);
+int pt_lr_grad_params(int B, int L, int S, int T, int D, int n, const double* mag,
+                      const float* screens, const float* w, const int64_t* fix,
+                      const float* grad_out, float* partial, void* stream);
+/* dL/dscreens (B, L, S, S): the transpose of the gather, as a deterministic
+ * gather over screen tiles (every element written once, no atomics). */
+int pt_lr_grad_screens(int B, int L, int S, int T, int D, int n, const double* mag,
+                       const float* w, const int64_t* fix, const float* grad_out,
+                       float* grad_screens, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -87,6 +87,11 @@ SIGNATURES = {
                                vp]),
     "pt_readout": (i32, [i32, i32, i32, i32, i32, C.POINTER(ReadoutLayer), vp, f32, vp, vp]),
     "pt_rows_sample": (i32, [i32, i32, i32, i32, i32, f64, vp, vp, vp]),
+    "pt_lr_fix": (i32, [i32, i32, i32, i32, i32, vp, dptr, vp, vp]),
+    "pt_lr_forward": (i32, [i32, i32, i32, i32, i32, i32, dptr, vp, vp, vp, vp, vp]),
+    "pt_lr_partial_count": (sz, [i32, i32, i32, i32, i32]),
+    "pt_lr_grad_params": (i32, [i32, i32, i32, i32, i32, i32, dptr, vp, vp, vp, vp, vp, vp]),
+    "pt_lr_grad_screens": (i32, [i32, i32, i32, i32, i32, i32, dptr, vp, vp, vp, vp, vp]),
 }
 
 
