@@ -249,6 +249,31 @@ int pt_lr_grad_screens(int B, int L, int S, int T, int D, int n, const double* m
                        const float* w, const int64_t* fix, const float* grad_out,
                        float* grad_screens, void* stream);
 
+/* ---- adjoint of the spectral frame synthesis ---------------------------
+ * No counterpart in the reference (it has no gradients). The forward is
+ * pt_frames without subharmonics, with per-layer weights folded into the
+ * spectra: y_f = scale * crop(Re IDFT(sum_l w_l S_l Phi_lf)), Phi_lf =
+ * exp(2 pi i (fx sx[f,l] + fy sy[f,l])) (Atmosphere._integrate,
+ * src/pyturb/atmosphere.py:882-938). Backward, for upstream g (F, n_out, n_out):
+ *  1. pt_synth_adj_pack: z (ceil(F/2), ns, ns) complex = scale * conj(g_2p +
+ *     i g_2p+1) zero-padded at (crop, crop);
+ *  2. pt_ifft2(grid, z, z, ceil(F/2), ...) in place (the forward DFT by
+ *     conjugation);
+ *  3. pt_synth_adj_phasors: ph (L, F, 2, ns) complex from DEVICE shifts
+ *     sx, sy (F, L) f64 [m], the forward's fixed-point ramps;
+ *  4. pt_synth_adj_spectra: dL/dS (L, ns, ns) complex (d/dRe + i d/dIm);
+ *  5. pt_synth_adj_params: out (L, F, 3) f64 = [dL/dw_l contribution of
+ *     frame f, dL/dsx[f,l], dL/dsy[f,l]]. */
+int pt_synth_adj_pack(int ns, int F, int crop, int n_out, float scale, const float* g, float* z,
+                      void* stream);
+int pt_synth_adj_phasors(int ns, double pixel_scale, int L, int F, const double* sx,
+                         const double* sy, float* ph, void* stream);
+int pt_synth_adj_spectra(int ns, int L, int F, const float* w, const float* Z, const float* ph,
+                         float* grad_spectra, void* stream);
+int pt_synth_adj_params(int ns, double pixel_scale, int L, int F, const float* w,
+                        const float* spectra, const float* Z, const float* ph, double* out,
+                        void* stream);
+
 #ifdef __cplusplus
 }
 #endif

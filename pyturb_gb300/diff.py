@@ -188,3 +188,150 @@ def fit_layers(readout: DifferentiableReadout, screens, target, weights0, winds0
         opt.step()
         losses.append(float(loss.detach()))
     return w.detach(), v.detach(), losses
+
+
+# ------------------------------------------------------------- spectral synthesis
+
+
+class _SynthFn:
+    """Holder for the spectral-synthesis autograd Function (built lazily)."""
+
+    fn = None
+
+    @classmethod
+    def get(cls):
+        if cls.fn is not None:
+            return cls.fn
+        import torch
+
+        class SpectralSynthesis(torch.autograd.Function):
+            @staticmethod
+            def forward(ctx, spectra, weights, shifts, grid, crop, n_out, scale):
+                L, ns, ns2 = spectra.shape
+                F = shifts.shape[0]
+                if ns2 != ns or ns != grid.ns or grid.P != 0:
+                    raise ValueError("spectral_synthesis: spectra must be (L, ns, ns) on a grid "
+                                     "without subharmonics")
+                if tuple(shifts.shape) != (F, L, 2) or shifts.dtype != torch.float64:
+                    raise ValueError("spectral_synthesis: shifts must be float64 (F, L, 2)")
+                if spectra.dtype != torch.complex64 or weights.dtype != torch.float32:
+                    raise ValueError("spectral_synthesis: complex64 spectra, float32 weights")
+                s = stream_handle()
+                grid.ensure_workspace(L)
+                sw = torch.view_as_real(spectra * weights.to(torch.complex64)[:, None, None])
+                sw = sw.contiguous()
+                sh = shifts.detach().cpu().numpy()
+                sx = np.ascontiguousarray(sh[..., 0])
+                sy = np.ascontiguousarray(sh[..., 1])
+                out = torch.empty((F, n_out, n_out), dtype=torch.float32, device=spectra.device)
+                _lib.call("pt_frames", grid.handle, L, _ptr(sw), None, F, _lib.as_dptr(sx),
+                          _lib.as_dptr(sy), 0, int(crop), int(n_out), float(scale), _ptr(out),
+                          _ptr(grid.work), grid.work_bytes, s)
+                ctx.save_for_backward(spectra, weights, shifts)
+                ctx.grid, ctx.crop, ctx.n_out, ctx.scale = grid, int(crop), int(n_out), float(scale)
+                return out
+
+            @staticmethod
+            def backward(ctx, g):
+                spectra, weights, shifts = ctx.saved_tensors
+                grid = ctx.grid
+                L, ns, _ = spectra.shape
+                F = shifts.shape[0]
+                dev = g.device
+                s = stream_handle()
+                g = g.contiguous()
+                P2 = (F + 1) // 2
+                z = torch.empty((P2, ns, ns, 2), dtype=torch.float32, device=dev)
+                _lib.call("pt_synth_adj_pack", ns, F, ctx.crop, ctx.n_out, ctx.scale, _ptr(g),
+                          _ptr(z), s)
+                _lib.call("pt_ifft2", grid.handle, _ptr(z), _ptr(z), P2, _ptr(grid.work),
+                          grid.work_bytes, s)
+                sx = shifts[..., 0].contiguous()
+                sy = shifts[..., 1].contiguous()
+                ph = torch.empty((L, F, 2, ns, 2), dtype=torch.float32, device=dev)
+                _lib.call("pt_synth_adj_phasors", ns, grid.dx, L, F, _ptr(sx), _ptr(sy), _ptr(ph), s)
+                w = weights.contiguous()
+                gS = gw = gsh = None
+                if ctx.needs_input_grad[0]:
+                    gSr = torch.empty((L, ns, ns, 2), dtype=torch.float32, device=dev)
+                    _lib.call("pt_synth_adj_spectra", ns, L, F, _ptr(w), _ptr(z), _ptr(ph),
+                              _ptr(gSr), s)
+                    gS = torch.view_as_complex(gSr)
+                if ctx.needs_input_grad[1] or ctx.needs_input_grad[2]:
+                    sr = torch.view_as_real(spectra.contiguous()).contiguous()
+                    part = torch.empty((L, F, 3), dtype=torch.float64, device=dev)
+                    _lib.call("pt_synth_adj_params", ns, grid.dx, L, F, _ptr(w), _ptr(sr), _ptr(z),
+                              _ptr(ph), _ptr(part), s)
+                    if ctx.needs_input_grad[1]:
+                        gw = part[..., 0].sum(dim=1).float()
+                    if ctx.needs_input_grad[2]:
+                        gsh = part[..., 1:].transpose(0, 1).contiguous()
+                return gS, gw, gsh, None, None, None, None
+
+        cls.fn = SpectralSynthesis
+        return cls.fn
+
+
+def spectral_synthesis(spectra, weights, shifts, grid, crop: int, n_out: int, scale: float = 1.0):
+    """``(F, n_out, n_out)`` frames ``scale * crop(Re IDFT(sum_l w_l S_l Phi_fl))`` (no
+    subharmonics), differentiable in ``spectra (L, ns, ns)`` complex64, ``weights (L,)``
+    and ``shifts (F, L, 2)`` float64 [m] (x along axis 0). ``grid`` is a
+    :class:`pyturb_gb300.fourier.Grid` built with no subharmonic levels."""
+    return _SynthFn.get().apply(spectra, weights, shifts, grid, int(crop), int(n_out),
+                                float(scale))
+
+
+class DifferentiableSpectralFrames:
+    """Spectral frozen-flow frames differentiable in the layer noise, the
+    per-layer weights (sqrt of the Cn2 fractions) and the winds.
+
+    The layers share one ``n_screen`` grid at ``pixel_scale`` and the von
+    Karman amplitude of ``r0`` / ``L0`` (``fourier.py:174-228`` of the
+    reference, without subharmonic levels); layer ``l``'s spectrum is
+    ``amplitude * noise[l]`` with ``noise`` complex N(0, 1). Frame ``(t, d)``
+    displaces layer ``l`` by ``v_l t + alt_l theta_d`` (``atmosphere.py:
+    1012-1015``) and is cropped to the central ``n x n`` pupil.
+    """
+
+    def __init__(self, n: int, n_screen: int, pixel_scale: float, r0: float, L0: float,
+                 altitudes: Sequence[float], times, directions=None, scale: float = 1.0,
+                 device: str = "gpu") -> None:
+        import torch
+
+        from .fourier import Grid, amplitude_table
+
+        check_device(device)
+        self.device = cuda_device()
+        self.n, self.n_screen = int(n), int(n_screen)
+        if not 1 <= self.n <= self.n_screen:
+            raise ValueError("need 1 <= n <= n_screen")
+        self.pixel_scale = float(pixel_scale)
+        self.altitudes = np.asarray(altitudes, np.float64).reshape(-1)
+        self.times = np.asarray(times, np.float64).reshape(-1)
+        dirs = np.zeros((1, 2)) if directions is None else np.asarray(directions, np.float64)
+        self.directions = dirs.reshape(-1, 2)
+        self.scale = float(scale)
+        self.crop = (self.n_screen - self.n) // 2
+        self.grid = Grid(self.n_screen, self.pixel_scale, np.zeros((0, 3)), n_layers=1)
+        amp = amplitude_table(self.n_screen, self.pixel_scale, r0, L0)
+        self.amplitude = torch.as_tensor(amp, dtype=torch.float32, device=self.device)
+        dev = self.device
+        self._t = torch.as_tensor(self.times, dtype=torch.float64, device=dev)
+        self._alt_th = torch.as_tensor(
+            self.altitudes[None, :, None] * self.directions[:, None, :], dtype=torch.float64,
+            device=dev)                                                     # (D, L, 2)
+
+    def shifts(self, winds):
+        """``(T * D, L, 2)`` float64 displacements [m] from ``winds (L, 2)``."""
+        v = winds.to(self.device, dtype=self._t.dtype)
+        disp = v[None, None] * self._t[:, None, None, None] + self._alt_th[None]
+        return disp.reshape(-1, self.altitudes.size, 2)
+
+    def spectra(self, noise):
+        """``amplitude * noise`` for complex ``noise (L, ns, ns)``."""
+        return noise * self.amplitude.to(noise.dtype)[None]
+
+    def __call__(self, noise, weights, winds):
+        """``(T * D, n, n)`` frames, frame index ``t * D + d``."""
+        return spectral_synthesis(self.spectra(noise), weights, self.shifts(winds), self.grid,
+                                  self.crop, self.n, self.scale)

@@ -127,6 +127,14 @@ class Grid:
         self.work_bytes = int(self._lib.pt_grid_workspace_bytes(handle, max(1, int(n_layers))))
         self.work = torch.empty(self.work_bytes, dtype=torch.uint8, device=self.device)
 
+    def ensure_workspace(self, n_layers: int) -> None:
+        """Grow the workspace to what ``n_layers`` layers need (never shrinks)."""
+        need = int(self._lib.pt_grid_workspace_bytes(self.handle, max(1, int(n_layers))))
+        if need > self.work_bytes:
+            torch = torch_module()
+            self.work = torch.empty(need, dtype=torch.uint8, device=self.device)
+            self.work_bytes = need
+
     def __del__(self) -> None:
         h = getattr(self, "handle", None)
         if h is not None and h.value:
