@@ -249,6 +249,14 @@ int pt_lr_grad_screens(int B, int L, int S, int T, int D, int n, const double* m
                        const float* w, const int64_t* fix, const float* grad_out,
                        float* grad_screens, void* stream);
 
+/* ---- tensor cores (tcgen05) ---------------------------------------------
+ * Self-test of the tcgen05 path, no counterpart in the reference: one tile
+ * D (128 x N) = A (128 x K) * B (N x K)^T with bf16 A, B (row-major, device)
+ * and fp32 D (row-major, device), through shared-memory descriptors, an fp32
+ * TMEM accumulator and tcgen05.ld. N, K multiples of 16 in [16, 256].
+ * Synchronises the stream; PT_ERR_CUDA if a bounded wait timed out. */
+int pt_tc_probe(int N, int K, const uint16_t* A, const uint16_t* B, float* D, void* stream);
+
 /* ---- adjoint of the spectral frame synthesis ---------------------------
  * No counterpart in the reference (it has no gradients). The forward is
  * pt_frames without subharmonics, with per-layer weights folded into the

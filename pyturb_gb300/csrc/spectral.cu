@@ -994,6 +994,10 @@ static int pair_cols_reg(const pt_grid* g, const float2* work, int npair, int pa
 using namespace pt;
 
 // Device error word set by bounded waits that ran out (0 = none).
+namespace pt {
+int tc_device_error(int* out, int clear);
+}
+
 extern "C" int pt_device_error(int* out, int clear) {
   if (!out) return fail(PT_ERR_ARG, "pt_device_error: out is NULL");
   if (int rc = check_cuda(cudaDeviceSynchronize(), "pt_device_error: sync")) return rc;
@@ -1006,6 +1010,9 @@ extern "C" int pt_device_error(int* out, int clear) {
                             "pt_device_error: clear"))
       return rc;
   }
+  int tcw = 0;  // the tensor-core kernels' own error word (separate module)
+  if (int rc = tc_device_error(&tcw, clear)) return rc;
+  *out |= tcw;
   return PT_OK;
 }
 
