@@ -208,6 +208,33 @@ def bench_extrude(torch, G, steps: int = 128):
     torch.cuda.synchronize()
     step_s = e0.elapsed_time(e1) / 1000.0 / steps
     flops = 2.0 * W * 3 * W * S
+    # the split-bf16 tensor-core forms from the same state
+    tc = {}
+    for form in ("bf16x2", "bf16x3"):
+        r2 = RingExtruder(W, 2, cap, [], [0] * S, [r ** (-5.0 / 6.0) for r in r0s] * R,
+                          [NoiseStream(100 + s, None) for s in range(S)],
+                          device_operator=ext._ring.M, form=form)
+        for s in range(S):
+            r2.buf[s].copy_(ext._ring.buf[s % 9])
+            r2.top[s] = ext._ring.top[s % 9]
+        for _ in range(3):
+            r2.extrude(ones)
+        torch.cuda.synchronize()
+        _lib.prof_report()
+        _lib.prof_enable(True)
+        e0.record()
+        r2.extrude(steps * ones)
+        e1.record()
+        torch.cuda.synchronize()
+        prof = _lib.prof_report()
+        _lib.prof_enable(False)
+        st = e0.elapsed_time(e1) / 1000.0 / steps
+        g = prof.get("k_tc_gemm", (1, float("nan")))
+        tc[form] = {"row_steps_per_s": 1.0 / st, "effective_tflops": flops / st / 1e12,
+                    "gemm_us": g[1] / g[0] * 1e3,
+                    "gemm_tflops_issued": flops * (3 if form == "bf16x2" else 6)
+                    / (g[1] / g[0] / 1e3) / 1e12}
+        del r2
     # readout: the 9 layers of one realisation, bilinear, at 1024^2
     out = torch.empty((n, n), dtype=torch.float32, device="cuda")
     ext.set_time(0.01)
@@ -228,7 +255,7 @@ def bench_extrude(torch, G, steps: int = 128):
             "row_steps_per_s": 1.0 / step_s, "gemm_tflops": flops / step_s / 1e12,
             "readout_frames_per_s": 1.0 / ro_s,
             "readout_gbs_out": n * n * 4 / ro_s / 1e9, "host_setup_s": setup_s,
-            "note": "split-K SIMT FP32 GEMM (plain form)"}
+            "note": "split-K SIMT FP32 GEMM (plain form)", "tensor_core": tc}
 
 
 def bench_diff(torch, G, iters: int = 3):

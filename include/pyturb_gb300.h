@@ -216,6 +216,26 @@ int pt_readout(int n, int W, int cap, int interp, int n_layers, const pt_readout
 int pt_rows_sample(int n, int cap, int interp, int anchor_phys, int row_max, double shift,
                    const float* buf, float* out, void* stream);
 
+/* ---- tensor-core form of the extrusion product --------------------------
+ * The split-precision form of pt_extrude_batch (same arguments and ring
+ * semantics, src/pyturb/extrude.py:424-456): the operator [A | B_unit] and
+ * the per-step operand [stencil ; bscale * beta] are split into `terms`
+ * bf16 terms (x = x_hi + x_lo (+ x_mid); 2 terms: 3 products, 3 terms: 6)
+ * and multiplied by tcgen05 MMAs into an fp32 accumulator in tensor memory.
+ * pt_extrude_tc_prepare converts the FP32 (G, W, (m+1)W) operator M once
+ * into `tiles` (pt_extrude_tc_operator_bytes bytes, 256-byte aligned); the
+ * workspace of pt_extrude_batch_tc is pt_extrude_tc_workspace_bytes (for the
+ * largest number of screens stepped at once), 256-byte aligned. No reference
+ * counterpart beyond the product it replaces. */
+size_t pt_extrude_tc_operator_bytes(int W, int m, int n_groups, int terms);
+int pt_extrude_tc_prepare(int W, int m, int n_groups, const float* M, int terms, void* tiles,
+                          size_t tiles_bytes, void* stream);
+size_t pt_extrude_tc_workspace_bytes(int W, int m, int max_jobs, int terms);
+int pt_extrude_batch_tc(int W, int m, int cap, int n_groups, const void* tiles, int terms,
+                        float* buf, int n_screens, const int32_t* group, const float* bscale,
+                        const uint64_t* key, int64_t* top, const int32_t* counts,
+                        const float* noise, void* work, size_t work_bytes, void* stream);
+
 /* ---- differentiable multi-layer readout --------------------------------
  * out[b,t,d,i,j] = sum_l w[l] * bilerp(screens[b,l], u_r, u_c) with
  * u_r = pos0[t,d,l,0] + mag[d,l] * i, u_c = pos0[t,d,l,1] + mag[d,l] * j,

@@ -93,6 +93,11 @@ SIGNATURES = {
     "pt_lr_grad_params": (i32, [i32, i32, i32, i32, i32, i32, dptr, vp, vp, vp, vp, vp, vp]),
     "pt_lr_grad_screens": (i32, [i32, i32, i32, i32, i32, i32, dptr, vp, vp, vp, vp, vp]),
     "pt_tc_probe": (i32, [i32, i32, vp, vp, vp, vp]),
+    "pt_extrude_tc_operator_bytes": (sz, [i32, i32, i32, i32]),
+    "pt_extrude_tc_prepare": (i32, [i32, i32, i32, vp, i32, vp, sz, vp]),
+    "pt_extrude_tc_workspace_bytes": (sz, [i32, i32, i32, i32]),
+    "pt_extrude_batch_tc": (i32, [i32, i32, i32, i32, vp, i32, vp, i32, vp, vp, vp, vp, vp, vp,
+                                  vp, sz, vp]),
     "pt_synth_adj_pack": (i32, [i32, i32, i32, i32, f32, vp, vp, vp]),
     "pt_synth_adj_phasors": (i32, [i32, f64, i32, i32, vp, vp, vp, vp]),
     "pt_synth_adj_spectra": (i32, [i32, i32, i32, vp, vp, vp, vp, vp]),

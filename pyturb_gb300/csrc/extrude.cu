@@ -21,7 +21,10 @@
 #include <map>
 #include <vector>
 
+#include <cuda_bf16.h>
+
 #include "common.cuh"
+#include "tc.cuh"
 
 namespace pt {
 uint64_t* launch_counter();
@@ -47,6 +50,27 @@ struct JobParams {
 };
 
 // X[j][k], k < mW: stencil rows; k >= mW: bscale * beta
+__device__ __forceinline__ float gather_value(int W, int m, int cap, const float* __restrict__ slab,
+                                              const GatherJob& jb, int k,
+                                              const float* __restrict__ noise) {
+  if (k < m * W) {
+    const int r = k / W, c = k % W;
+    int phys = jb.head - m + r;
+    if (phys < 0) phys += cap;
+    return slab[(size_t)phys * W + c];
+  }
+  const int c = k - m * W;
+  float z;
+  if (noise) {
+    z = noise[jb.noise_off + c];
+  } else {
+    // one Philox call yields a pair: even/odd columns share it
+    const float2 p = philox_cnormal(jb.key, (uint64_t)(c >> 1), jb.row, kDomainExtrude);
+    z = (c & 1) ? p.y : p.x;
+  }
+  return jb.bscale * z;
+}
+
 __global__ void k_extrude_gather(int W, int m, int cap, const float* __restrict__ buf,
                                  const JobParams jobs, int J, const float* __restrict__ noise,
                                  float* __restrict__ X) {
@@ -55,26 +79,33 @@ __global__ void k_extrude_gather(int W, int m, int cap, const float* __restrict_
   const GatherJob& jb = jobs.j[j];
   const int K = (m + 1) * W;
   const float* slab = buf + (size_t)jb.screen * cap * W;
-  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < K; k += gridDim.x * blockDim.x) {
-    float v;
-    if (k < m * W) {
-      const int r = k / W, c = k % W;
-      int phys = jb.head - m + r;
-      if (phys < 0) phys += cap;
-      v = slab[(size_t)phys * W + c];
-    } else {
-      const int c = k - m * W;
-      float z;
-      if (noise) {
-        z = noise[jb.noise_off + c];
-      } else {
-        // one Philox call yields a pair: even/odd columns share it
-        const float2 p = philox_cnormal(jb.key, (uint64_t)(c >> 1), jb.row, kDomainExtrude);
-        z = (c & 1) ? p.y : p.x;
-      }
-      v = jb.bscale * z;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < K; k += gridDim.x * blockDim.x)
+    X[(size_t)j * K + k] = gather_value(W, m, cap, slab, jb, k, noise);
+}
+
+// The same operand for the tensor-core form: split into `terms` bf16 terms and
+// stored as B tiles, tiles[(kc * terms + t) * NP * 128 + core(j, k % 64)],
+// zero for padding columns k >= K and rows j >= J.
+__global__ void k_tc_gather(int W, int m, int cap, const float* __restrict__ buf,
+                            const JobParams jobs, int J, int NP, int nkc, int terms,
+                            const float* __restrict__ noise, uint8_t* __restrict__ tiles) {
+  const int j = blockIdx.y;
+  const int K = (m + 1) * W;
+  const size_t tile = (size_t)NP * 128;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nkc * 64; k += gridDim.x * blockDim.x) {
+    float v = 0.f;
+    if (j < J && k < K) {
+      const GatherJob& jb = jobs.j[j];
+      v = gather_value(W, m, cap, buf + (size_t)jb.screen * cap * W, jb, k, noise);
     }
-    X[(size_t)j * K + k] = v;
+    uint8_t* blk = tiles + (size_t)(k / 64) * terms * tile;
+    const uint32_t off = tc::core_offset(j, k % 64, 64);
+    float r = v;
+    for (int t = 0; t < terms; ++t) {
+      const __nv_bfloat16 h = __float2bfloat16_rn(r);
+      *(uint16_t*)(blk + t * tile + off) = __bfloat16_as_ushort(h);
+      r -= __bfloat162float(h);
+    }
   }
 }
 
@@ -250,6 +281,15 @@ __global__ void k_rows_sample(int n, int cap, int anchor_phys, int row_max, int 
 
 static inline size_t al256(size_t x) { return (x + 255) & ~size_t(255); }
 
+// tensor-core launchers (extrude_tc.cu)
+int tc_max_jobs(int terms);
+size_t tc_operator_bytes(int W, int m, int G, int terms);
+size_t tc_btile_bytes(int W, int m, int J, int terms);
+size_t tc_partial_floats(int W, int m, int J, int terms);
+int tc_prepare_launch(int W, int m, int G, const float* M, int terms, void* tiles, cudaStream_t s);
+int tc_gemm_launch(int W, int m, int J, int terms, const uint8_t* At, const uint8_t* Bt,
+                   float* partial, int* nz_out, cudaStream_t s);
+
 static int split_for(int W, int J, int K) {
   const int ctas = ((W + kTM - 1) / kTM) * ((J + kTJ - 1) / kTJ);
   int s = std::max(1, std::min(kMaxSplit, (2 * 152 + ctas - 1) / ctas));
@@ -269,11 +309,21 @@ extern "C" size_t pt_extrude_workspace_bytes(int W, int m, int max_jobs) {
   return al256(J * K * sizeof(float)) + al256((size_t)kMaxSplit * J * W * sizeof(float));
 }
 
-extern "C" int pt_extrude_rows(int W, int m, int cap, int G, const float* M, float* buf,
-                               int n_jobs, const pt_extrude_job* jobs, const float* noise,
-                               void* work, size_t work_bytes, void* stream) {
-  if (W < 1 || m < 1 || cap < m + 1 || G < 1) return fail(PT_ERR_ARG, "pt_extrude_rows: bad sizes");
-  if (!M || !buf || (n_jobs > 0 && !jobs)) return fail(PT_ERR_ARG, "pt_extrude_rows: NULL pointer");
+// The operator of one form: FP32 [A | B] (SIMT GEMM) or its bf16 term tiles
+// (tensor cores, `terms` = 2 or 3).
+struct ExtrudeForm {
+  int terms;               // 0: FP32
+  const float* M;          // (G, W, K) FP32
+  const uint8_t* tiles;    // tensor-core operator tiles
+};
+
+static int extrude_jobs(const char* who, const ExtrudeForm& form, int W, int m, int cap, int G,
+                        float* buf, int n_jobs, const pt_extrude_job* jobs, const float* noise,
+                        void* work, size_t work_bytes, cudaStream_t s) {
+  if (W < 1 || m < 1 || cap < m + 1 || G < 1) return fail(PT_ERR_ARG, std::string(who) + ": bad sizes");
+  if ((form.terms == 0 && !form.M) || (form.terms != 0 && !form.tiles) || !buf ||
+      (n_jobs > 0 && !jobs))
+    return fail(PT_ERR_ARG, std::string(who) + ": NULL pointer");
   if (n_jobs == 0) return PT_OK;
   // group jobs by (step, group), validating order and ranges
   int max_j = 0;
@@ -281,24 +331,33 @@ extern "C" int pt_extrude_rows(int W, int m, int cap, int G, const float* M, flo
     int cur = 1, prev_step = jobs[0].step;
     for (int i = 0; i < n_jobs; ++i) {
       const pt_extrude_job& jb = jobs[i];
-      if (jb.group < 0 || jb.group >= G) return fail(PT_ERR_ARG, "pt_extrude_rows: job group out of range");
-      if (jb.head < 0 || jb.head >= cap) return fail(PT_ERR_ARG, "pt_extrude_rows: job head out of range");
-      if (jb.screen < 0) return fail(PT_ERR_ARG, "pt_extrude_rows: negative screen index");
+      if (jb.group < 0 || jb.group >= G)
+        return fail(PT_ERR_ARG, std::string(who) + ": job group out of range");
+      if (jb.head < 0 || jb.head >= cap)
+        return fail(PT_ERR_ARG, std::string(who) + ": job head out of range");
+      if (jb.screen < 0) return fail(PT_ERR_ARG, std::string(who) + ": negative screen index");
       if (i > 0) {
-        if (jb.step < prev_step) return fail(PT_ERR_ARG, "pt_extrude_rows: jobs must be sorted by step");
+        if (jb.step < prev_step)
+          return fail(PT_ERR_ARG, std::string(who) + ": jobs must be sorted by step");
         cur = (jb.step == prev_step) ? cur + 1 : 1;
       }
       prev_step = jb.step;
       max_j = std::max(max_j, cur);
     }
   }
-  const size_t need = pt_extrude_workspace_bytes(W, m, max_j);
-  if (!work || work_bytes < need) return fail(PT_ERR_ARG, "pt_extrude_rows: workspace too small");
+  const size_t need = form.terms ? pt_extrude_tc_workspace_bytes(W, m, max_j, form.terms)
+                                 : pt_extrude_workspace_bytes(W, m, max_j);
+  if (!work || work_bytes < need) return fail(PT_ERR_ARG, std::string(who) + ": workspace too small");
   const int K = (m + 1) * W;
-  const int jcap = std::min(max_j, kJobsPerLaunch);
+  const int per_launch = form.terms ? tc_max_jobs(form.terms) : kJobsPerLaunch;
+  const int jcap = std::min(max_j, per_launch);
+  // FP32: X (jcap, K) then partials; tensor cores: B tiles then partials
+  const size_t first = form.terms ? al256(tc_btile_bytes(W, m, jcap, form.terms))
+                                  : al256((size_t)jcap * K * sizeof(float));
   float* X = (float*)work;
-  float* partial = (float*)((char*)work + al256((size_t)jcap * K * sizeof(float)));
-  cudaStream_t s = (cudaStream_t)stream;
+  uint8_t* Bt = (uint8_t*)work;
+  float* partial = (float*)((char*)work + first);
+  const size_t op_group = form.terms ? tc_operator_bytes(W, m, 1, form.terms) : 0;
   std::vector<GatherJob> hj;
   int i = 0;
   while (i < n_jobs) {
@@ -313,24 +372,33 @@ extern "C" int pt_extrude_rows(int W, int m, int cap, int G, const float* M, flo
         const pt_extrude_job& jb = jobs[q];
         hj.push_back(GatherJob{jb.screen, jb.head, jb.bscale, jb.key, jb.row, (long long)jb.noise_off});
       }
-      for (size_t b = 0; b < hj.size(); b += kJobsPerLaunch) {
-        const int J = (int)std::min<size_t>(kJobsPerLaunch, hj.size() - b);
+      for (size_t b = 0; b < hj.size(); b += per_launch) {
+        const int J = (int)std::min<size_t>(per_launch, hj.size() - b);
         JobParams jp;
         for (int q = 0; q < J; ++q) jp.j[q] = hj[b + q];
-        k_extrude_gather<<<dim3(std::min((K + 255) / 256, 64), J), 256, 0, s>>>(W, m, cap, buf, jp,
-                                                                              J, noise, X);
-        const int nsplit = split_for(W, J, K);
-        const int kslice = ((K + nsplit - 1) / nsplit + kTK - 1) / kTK * kTK;
-        const int nz = (K + kslice - 1) / kslice;
-        const float* Mg = M + (size_t)kv.first * W * K;
-        {
+        int nz = 0;
+        if (form.terms == 0) {
+          k_extrude_gather<<<dim3(std::min((K + 255) / 256, 64), J), 256, 0, s>>>(W, m, cap, buf, jp,
+                                                                                J, noise, X);
+          const int nsplit = split_for(W, J, K);
+          const int kslice = ((K + nsplit - 1) / nsplit + kTK - 1) / kTK * kTK;
+          nz = (K + kslice - 1) / kslice;
+          const float* Mg = form.M + (size_t)kv.first * W * K;
           ProfScope ps("k_extrude_gemm", s);
           k_extrude_gemm<<<dim3((W + kTM - 1) / kTM, (J + kTJ - 1) / kTJ, nz), 256, 0, s>>>(
               W, K, J, kslice, Mg, X, partial);
+        } else {
+          const int NP = std::max(16, (J + 15) / 16 * 16);
+          const int nkc = (K + 63) / 64;
+          k_tc_gather<<<dim3(std::min((nkc * 64 + 255) / 256, 64), NP), 256, 0, s>>>(
+              W, m, cap, buf, jp, J, NP, nkc, form.terms, noise, Bt);
+          if (int rc = tc_gemm_launch(W, m, J, form.terms, form.tiles + (size_t)kv.first * op_group,
+                                      Bt, partial, &nz, s))
+            return rc;
         }
         k_extrude_reduce<<<dim3((W + 255) / 256, J), 256, 0, s>>>(W, J, cap, nz, partial, jp, buf);
-        count_launch_e(3);
-        if (int rc = check_launch("pt_extrude_rows")) return rc;
+        count_launch_e(form.terms ? 2 : 3);
+        if (int rc = check_launch(who)) return rc;
       }
     }
     i = e;
@@ -338,19 +406,26 @@ extern "C" int pt_extrude_rows(int W, int m, int cap, int G, const float* M, flo
   return PT_OK;
 }
 
-extern "C" int pt_extrude_batch(int W, int m, int cap, int n_groups, const float* M, float* buf,
-                                int S, const int32_t* group, const float* bscale,
-                                const uint64_t* key, int64_t* top, const int32_t* counts,
-                                const float* noise, void* work, size_t work_bytes,
-                                void* stream) {
+extern "C" int pt_extrude_rows(int W, int m, int cap, int G, const float* M, float* buf,
+                               int n_jobs, const pt_extrude_job* jobs, const float* noise,
+                               void* work, size_t work_bytes, void* stream) {
+  return extrude_jobs("pt_extrude_rows", ExtrudeForm{0, M, nullptr}, W, m, cap, G, buf, n_jobs,
+                      jobs, noise, work, work_bytes, (cudaStream_t)stream);
+}
+
+// Jobs of `counts[s]` row steps on every screen s, step-major (the order of
+// the noise rows), advancing top[s].
+static int batch_jobs(const char* who, int W, int cap, int S, const int32_t* group,
+                      const float* bscale, const uint64_t* key, int64_t* top,
+                      const int32_t* counts, std::vector<pt_extrude_job>& jobs) {
   if (S < 1 || !group || !bscale || !key || !top || !counts)
-    return fail(PT_ERR_ARG, "pt_extrude_batch: bad screen arrays");
+    return fail(PT_ERR_ARG, std::string(who) + ": bad screen arrays");
   int steps = 0;
   for (int s = 0; s < S; ++s) {
-    if (counts[s] < 0 || top[s] < 0) return fail(PT_ERR_ARG, "pt_extrude_batch: negative count");
+    if (counts[s] < 0 || top[s] < 0) return fail(PT_ERR_ARG, std::string(who) + ": negative count");
     steps = std::max(steps, (int)counts[s]);
   }
-  std::vector<pt_extrude_job> jobs;
+  jobs.clear();
   jobs.reserve((size_t)S * steps);
   int64_t noff = 0;
   for (int k = 0; k < steps; ++k)
@@ -369,8 +444,60 @@ extern "C" int pt_extrude_batch(int W, int m, int cap, int n_groups, const float
       top[s] += 1;
       jobs.push_back(j);
     }
-  return pt_extrude_rows(W, m, cap, n_groups, M, buf, (int)jobs.size(), jobs.data(), noise, work,
-                         work_bytes, stream);
+  return PT_OK;
+}
+
+extern "C" int pt_extrude_batch(int W, int m, int cap, int n_groups, const float* M, float* buf,
+                                int S, const int32_t* group, const float* bscale,
+                                const uint64_t* key, int64_t* top, const int32_t* counts,
+                                const float* noise, void* work, size_t work_bytes,
+                                void* stream) {
+  std::vector<pt_extrude_job> jobs;
+  if (int rc = batch_jobs("pt_extrude_batch", W, cap, S, group, bscale, key, top, counts, jobs))
+    return rc;
+  return extrude_jobs("pt_extrude_batch", ExtrudeForm{0, M, nullptr}, W, m, cap, n_groups, buf,
+                      (int)jobs.size(), jobs.data(), noise, work, work_bytes, (cudaStream_t)stream);
+}
+
+extern "C" size_t pt_extrude_tc_operator_bytes(int W, int m, int n_groups, int terms) {
+  if (W < 1 || m < 1 || n_groups < 1 || (terms != 2 && terms != 3)) return 0;
+  return tc_operator_bytes(W, m, n_groups, terms);
+}
+
+extern "C" int pt_extrude_tc_prepare(int W, int m, int n_groups, const float* M, int terms,
+                                     void* tiles, size_t tiles_bytes, void* stream) {
+  if (W < 1 || m < 1 || n_groups < 1) return fail(PT_ERR_ARG, "pt_extrude_tc_prepare: bad sizes");
+  if (terms != 2 && terms != 3) return fail(PT_ERR_ARG, "pt_extrude_tc_prepare: terms must be 2 or 3");
+  if (!M || !tiles) return fail(PT_ERR_ARG, "pt_extrude_tc_prepare: NULL pointer");
+  if (tiles_bytes < tc_operator_bytes(W, m, n_groups, terms))
+    return fail(PT_ERR_ARG, "pt_extrude_tc_prepare: tile buffer too small");
+  if (((uintptr_t)tiles & 255) != 0)
+    return fail(PT_ERR_ARG, "pt_extrude_tc_prepare: tiles must be 256-byte aligned");
+  return tc_prepare_launch(W, m, n_groups, M, terms, tiles, (cudaStream_t)stream);
+}
+
+extern "C" size_t pt_extrude_tc_workspace_bytes(int W, int m, int max_jobs, int terms) {
+  if (W < 1 || m < 1 || max_jobs < 1 || (terms != 2 && terms != 3)) return 0;
+  const int J = std::min(max_jobs, tc_max_jobs(terms));
+  return al256(tc_btile_bytes(W, m, J, terms)) + al256(tc_partial_floats(W, m, J, terms) * sizeof(float));
+}
+
+extern "C" int pt_extrude_batch_tc(int W, int m, int cap, int n_groups, const void* tiles,
+                                   int terms, float* buf, int S, const int32_t* group,
+                                   const float* bscale, const uint64_t* key, int64_t* top,
+                                   const int32_t* counts, const float* noise, void* work,
+                                   size_t work_bytes, void* stream) {
+  if (terms != 2 && terms != 3) return fail(PT_ERR_ARG, "pt_extrude_batch_tc: terms must be 2 or 3");
+  if (work && ((uintptr_t)work & 255) != 0)
+    return fail(PT_ERR_ARG, "pt_extrude_batch_tc: workspace must be 256-byte aligned");
+  if (tiles && ((uintptr_t)tiles & 255) != 0)
+    return fail(PT_ERR_ARG, "pt_extrude_batch_tc: tiles must be 256-byte aligned");
+  std::vector<pt_extrude_job> jobs;
+  if (int rc = batch_jobs("pt_extrude_batch_tc", W, cap, S, group, bscale, key, top, counts, jobs))
+    return rc;
+  return extrude_jobs("pt_extrude_batch_tc", ExtrudeForm{terms, nullptr, (const uint8_t*)tiles}, W,
+                      m, cap, n_groups, buf, (int)jobs.size(), jobs.data(), noise, work,
+                      work_bytes, (cudaStream_t)stream);
 }
 
 extern "C" int pt_readout(int n, int W, int cap, int interp, int L, const pt_readout_layer* layers,

@@ -122,10 +122,16 @@ class RingExtruder:
     ``screens`` independent ring buffers of ``cap`` rows x ``W`` columns; screen
     s uses operator group ``groups[s]`` scaled by ``bscale[s]``."""
 
+    FORMS = {"fp32": 0, "bf16x2": 2, "bf16x3": 3}
+
     def __init__(self, W: int, m: int, cap: int, operators: List[Tuple[np.ndarray, np.ndarray]],
                  groups: Sequence[int], bscale: Sequence[float], streams: Sequence[NoiseStream],
-                 device_operator=None):
+                 device_operator=None, form: str = "fp32"):
         torch = torch_module()
+        if form not in self.FORMS:
+            raise ValueError(f"form must be one of {sorted(self.FORMS)}, got {form!r}")
+        self.form = form
+        self.terms = self.FORMS[form]
         self.W, self.m, self.cap = int(W), int(m), int(cap)
         self.S = len(groups)
         self.groups = [int(g) for g in groups]
@@ -146,9 +152,22 @@ class RingExtruder:
         self._key = np.asarray([st.key for st in self.streams], dtype=np.uint64)
         self.work_bytes = 0
         self.work = None
+        self.tiles = None
+        if self.terms:
+            # the operator split into bf16 terms, tiled for the tensor cores (once)
+            nbytes = int(_lib.load().pt_extrude_tc_operator_bytes(self.W, self.m, self.G,
+                                                                  self.terms))
+            self.tiles = torch.empty(nbytes, dtype=torch.uint8, device=cuda_device())
+            _lib.call("pt_extrude_tc_prepare", self.W, self.m, self.G, dptr(self.M), self.terms,
+                      dptr(self.tiles), nbytes, stream_handle())
 
     def _ensure_work(self, jobs_per_step: int) -> None:
-        need = int(_lib.load().pt_extrude_workspace_bytes(self.W, self.m, max(1, jobs_per_step)))
+        lib = _lib.load()
+        if self.terms:
+            need = int(lib.pt_extrude_tc_workspace_bytes(self.W, self.m, max(1, jobs_per_step),
+                                                         self.terms))
+        else:
+            need = int(lib.pt_extrude_workspace_bytes(self.W, self.m, max(1, jobs_per_step)))
         if need > self.work_bytes:
             torch = torch_module()
             self.work = torch.empty(need, dtype=torch.uint8, device=cuda_device())
@@ -174,10 +193,16 @@ class RingExtruder:
             noise = upload(np.stack(rows))
         self._ensure_work(int((counts > 0).sum()))
         ptr = lambda a: a.ctypes.data  # noqa: E731
-        _lib.call("pt_extrude_batch", self.W, self.m, self.cap, self.G, dptr(self.M),
-                  dptr(self.buf), self.S, ptr(self._group), ptr(self._bscale), ptr(self._key),
-                  ptr(self.top), ptr(counts), dptr(noise), dptr(self.work), self.work_bytes,
-                  stream_handle())
+        if self.terms:
+            _lib.call("pt_extrude_batch_tc", self.W, self.m, self.cap, self.G, dptr(self.tiles),
+                      self.terms, dptr(self.buf), self.S, ptr(self._group), ptr(self._bscale),
+                      ptr(self._key), ptr(self.top), ptr(counts), dptr(noise), dptr(self.work),
+                      self.work_bytes, stream_handle())
+        else:
+            _lib.call("pt_extrude_batch", self.W, self.m, self.cap, self.G, dptr(self.M),
+                      dptr(self.buf), self.S, ptr(self._group), ptr(self._bscale),
+                      ptr(self._key), ptr(self.top), ptr(counts), dptr(noise), dptr(self.work),
+                      self.work_bytes, stream_handle())
 
 
 class _LayerGeom:
@@ -212,7 +237,10 @@ class _LayerGeom:
 class ExtrudedAtmosphere:
     """Multi-layer extrusion engine (``src/pyturb/extrude.py:499-915``).
 
-    Constructor as the reference's plus ``host_noise`` (parity mode).
+    Constructor as the reference's plus ``host_noise`` (parity mode) and
+    ``extrude_form``: ``"fp32"`` (FP32 SIMT products, the default),
+    ``"bf16x2"`` or ``"bf16x3"`` (operands split into 2 or 3 bf16 terms and
+    multiplied on the tensor cores with an fp32 accumulator).
     :meth:`integrate` returns a float32 CUDA tensor ``(n, n)``.
     """
 
@@ -224,7 +252,7 @@ class ExtrudedAtmosphere:
                  lgs_altitude_los: Optional[float] = None, device: str = "gpu",
                  dtype: Any = "float32", seeds: Optional[Sequence[Any]] = None,
                  tau_boil: Optional[Sequence[float]] = None, boil_seed: Optional[Any] = None,
-                 host_noise=None) -> None:
+                 host_noise=None, extrude_form: str = "fp32") -> None:
         config = ExtrusionConfig.create(
             n, pixel_scale, layer_r0, layer_L0, layer_wind, layer_altitude_los,
             field_of_view_pix, stencil_rows, interp, lgs_altitude_los, device, dtype, seeds,
@@ -270,7 +298,8 @@ class ExtrudedAtmosphere:
                                            config.field_of_view_pix):
             self.layers.append(_LayerGeom(self.n, W, self.dx, vx, vy, alt, self.m, mag, fov))
         bscale = [float(r0) ** (-5.0 / 6.0) for r0 in config.layer_r0]
-        self._ring = RingExtruder(W, self.m, self.capacity, operators, groups, bscale, streams)
+        self._ring = RingExtruder(W, self.m, self.capacity, operators, groups, bscale, streams,
+                                  form=extrude_form)
         # seed each ring with a von Karman screen from the layer's own stream
         for i, (r0, L0) in enumerate(zip(config.layer_r0, config.layer_L0)):
             gen = PhaseScreen(n=W, pixel_scale=self.dx, r0=float(r0), L0=float(L0),
