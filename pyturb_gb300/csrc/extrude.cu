@@ -84,27 +84,48 @@ __global__ void k_extrude_gather(int W, int m, int cap, const float* __restrict_
 }
 
 // The same operand for the tensor-core form: split into `terms` bf16 terms and
-// stored as B tiles, tiles[(kc * terms + t) * NP * 128 + core(j, k % 64)],
-// zero for padding columns k >= K and rows j >= J.
+// stored as B tiles, tiles[(kc * terms + t) * NP * Kc * 2 + core(j, k % Kc)]
+// (Kc = tc::kTcKc), zero for padding columns k >= K and rows j >= J. One
+// thread makes the 8 consecutive K values of one job that form a 16-byte row
+// of a core matrix; consecutive threads take consecutive K groups of the same
+// job, so a warp reads one contiguous stretch of that job's ring rows.
 __global__ void k_tc_gather(int W, int m, int cap, const float* __restrict__ buf,
                             const JobParams jobs, int J, int NP, int nkc, int terms,
                             const float* __restrict__ noise, uint8_t* __restrict__ tiles) {
-  const int j = blockIdx.y;
+  constexpr int Kc = tc::kTcKc;
   const int K = (m + 1) * W;
-  const size_t tile = (size_t)NP * 128;
-  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nkc * 64; k += gridDim.x * blockDim.x) {
-    float v = 0.f;
-    if (j < J && k < K) {
+  const size_t tile = (size_t)NP * Kc * 2;
+  const int groups = nkc * (Kc / 8);
+  const size_t total = (size_t)groups * NP;
+  for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+       t += (size_t)gridDim.x * blockDim.x) {
+    const int j = (int)(t / groups);
+    const int k0 = (int)(t % groups) * 8;
+    float v[8];
+    if (j < J) {
       const GatherJob& jb = jobs.j[j];
-      v = gather_value(W, m, cap, buf + (size_t)jb.screen * cap * W, jb, k, noise);
+      const float* slab = buf + (size_t)jb.screen * cap * W;
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const int k = k0 + q;
+        v[q] = k < K ? gather_value(W, m, cap, slab, jb, k, noise) : 0.f;
+      }
+    } else {
+#pragma unroll
+      for (int q = 0; q < 8; ++q) v[q] = 0.f;
     }
-    uint8_t* blk = tiles + (size_t)(k / 64) * terms * tile;
-    const uint32_t off = tc::core_offset(j, k % 64, 64);
-    float r = v;
-    for (int t = 0; t < terms; ++t) {
-      const __nv_bfloat16 h = __float2bfloat16_rn(r);
-      *(uint16_t*)(blk + t * tile + off) = __bfloat16_as_ushort(h);
-      r -= __bfloat162float(h);
+    uint8_t* blk = tiles + (size_t)(k0 / Kc) * terms * tile + tc::core_offset(j, k0 % Kc, Kc);
+    for (int tt = 0; tt < terms; ++tt) {
+      uint32_t w4[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const __nv_bfloat16 h0 = __float2bfloat16_rn(v[2 * q]);
+        const __nv_bfloat16 h1 = __float2bfloat16_rn(v[2 * q + 1]);
+        w4[q] = (uint32_t)__bfloat16_as_ushort(h0) | ((uint32_t)__bfloat16_as_ushort(h1) << 16);
+        v[2 * q] -= __bfloat162float(h0);
+        v[2 * q + 1] -= __bfloat162float(h1);
+      }
+      *(uint4*)(blk + tt * tile) = make_uint4(w4[0], w4[1], w4[2], w4[3]);
     }
   }
 }
@@ -165,7 +186,7 @@ __global__ void k_extrude_reduce(int W, int J, int cap, int nsplit, const float*
   const int j = blockIdx.y;
   if (r >= W || j >= J) return;
   float s = 0.f;
-  for (int z = 0; z < nsplit; ++z) s += partial[((size_t)z * J + j) * W + r];
+  for (int z = 0; z < nsplit; ++z) s += __ldcs(partial + ((size_t)z * J + j) * W + r);
   const GatherJob& jb = jobs.j[j];
   buf[((size_t)jb.screen * cap + jb.head) * W + r] = s;
 }
@@ -389,8 +410,9 @@ static int extrude_jobs(const char* who, const ExtrudeForm& form, int W, int m, 
               W, K, J, kslice, Mg, X, partial);
         } else {
           const int NP = std::max(16, (J + 15) / 16 * 16);
-          const int nkc = (K + 63) / 64;
-          k_tc_gather<<<dim3(std::min((nkc * 64 + 255) / 256, 64), NP), 256, 0, s>>>(
+          const int nkc = (K + tc::kTcKc - 1) / tc::kTcKc;
+          const size_t items = (size_t)nkc * (tc::kTcKc / 8) * NP;
+          k_tc_gather<<<(unsigned)std::min<size_t>((items + 255) / 256, 152 * 8), 256, 0, s>>>(
               W, m, cap, buf, jp, J, NP, nkc, form.terms, noise, Bt);
           if (int rc = tc_gemm_launch(W, m, J, form.terms, form.tiles + (size_t)kv.first * op_group,
                                       Bt, partial, &nz, s))

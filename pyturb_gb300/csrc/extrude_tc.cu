@@ -79,12 +79,13 @@ k_tc_probe(int N, int K, const uint16_t* __restrict__ A, const uint16_t* __restr
 
 // ------------------------------------------------------------------ extrusion GEMM
 // Operand tiles: 128 (A) or NP (B) rows x kTcKc columns of one bf16 term in
-// the core-matrix layout (SBO = kTcKc * 16 = 1024 B). The terms of one
+// the core-matrix layout (SBO = kTcKc * 16 B). The terms of one
 // (row tile, K chunk) are contiguous, so one bulk copy stages all of them.
-constexpr int kTcKc = 64;
+using tc::kTcKc;
 constexpr int kTcM = 128;
-constexpr int kTcTileA = kTcM * kTcKc * 2;  // 16 KB
+constexpr int kTcTileA = kTcM * kTcKc * 2;  // bytes of one A term tile
 constexpr size_t kTcSmemMax = 227 * 1024;
+constexpr int kTcMaxStages = 6;
 
 __device__ __forceinline__ void split_bf16(float x, int terms, uint16_t* t) {
   float r = x;
@@ -95,7 +96,7 @@ __device__ __forceinline__ void split_bf16(float x, int terms, uint16_t* t) {
   }
 }
 
-// tiles[(((g * MT + mt) * nkc + kc) * terms + t) * 16 KB + core(r % 128, k % 64)]
+// tiles[(((g * MT + mt) * nkc + kc) * terms + t) * kTcTileA + core(r % 128, k % kTcKc)]
 __global__ void k_tc_prepare(int W, int K, int G, int MT, int nkc, int terms,
                              const float* __restrict__ M, uint8_t* __restrict__ tiles) {
   const size_t cols = (size_t)nkc * kTcKc;
@@ -128,7 +129,7 @@ k_tc_gemm(int W, int J, int NP, int nkc, int cps, int stages, const uint8_t* __r
   constexpr int pa[6] = {0, 0, 1, 0, 2, 1};
   constexpr int pb[6] = {0, 1, 0, 2, 0, 1};
   extern __shared__ uint8_t smraw[];
-  __shared__ uint64_t full[4], empty[4], done;
+  __shared__ uint64_t full[kTcMaxStages], empty[kTcMaxStages], done;
   __shared__ uint32_t tslot;
   uint8_t* base = (uint8_t*)(((uintptr_t)smraw + 1023) & ~(uintptr_t)1023);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -151,30 +152,28 @@ k_tc_gemm(int W, int J, int NP, int nkc, int cps, int stages, const uint8_t* __r
   __syncthreads();
   tc::tc_fence_after();
   const uint32_t tmem = tslot;
+  // lane 0 of warp 0 drives the copies and MMAs; its warp-mates park at the
+  // __syncwarp below instead of spinning on `done` in the same warp
   if (tid == 0 && n > 0) {
     const uint8_t* a_src = At + ((size_t)mt * nkc) * TERMS * kTcTileA;
     const uint8_t* b_src = Bt;
+    // the operator is re-read every row step: keep it in L2 ahead of the
+    // per-step operand and partials
+    const uint64_t keep = tc::policy_evict_last();
     auto load = [&](int c) {  // chunk c (relative) into stage c % stages
       uint8_t* st = base + (size_t)(c % stages) * stage_bytes;
       uint64_t* fb = &full[c % stages];
       tc::mbar_expect_tx(fb, stage_bytes);
-      tc::bulk_g2s(st, a_src + (size_t)(kc0 + c) * TERMS * kTcTileA, bytesA, fb);
+      tc::bulk_g2s_hint(st, a_src + (size_t)(kc0 + c) * TERMS * kTcTileA, bytesA, fb, keep);
       tc::bulk_g2s(st + bytesA, b_src + (size_t)(kc0 + c) * bytesB, bytesB, fb);
     };
-    const int D = stages >= 3 ? stages - 2 : 1;  // chunks loaded ahead
-    for (int c = 0; c < min(D, n); ++c) load(c);
+    // all stages filled up front; afterwards the stage of chunk i - 1 is
+    // refilled with chunk i - 1 + stages once chunk i's MMAs are queued, so
+    // the wait for chunk i - 1 overlaps chunk i on the tensor pipe
+    for (int c = 0; c < min(stages, n); ++c) load(c);
     const uint32_t idesc = tc::idesc_bf16(kTcM, NP);
-    bool ok = true;
-    for (int i = 0; i < n && ok; ++i) {
-      const int c = i + D;
-      if (c < n) {
-        const int prev = c - stages;  // last chunk that used stage c % stages
-        if (prev >= 0) ok = tc::mbar_wait(&empty[prev % stages], (prev / stages) & 1, &g_tc_error);
-        if (!ok) break;
-        load(c);
-      }
-      ok = tc::mbar_wait(&full[i % stages], (i / stages) & 1, &g_tc_error);
-      if (!ok) break;
+    for (int i = 0; i < n; ++i) {
+      if (!tc::mbar_wait(&full[i % stages], (i / stages) & 1, &g_tc_error)) break;
       tc::tc_fence_after();
       const uint32_t sa = tc::smem_u32(base + (size_t)(i % stages) * stage_bytes);
       const uint32_t sb = sa + bytesA;
@@ -188,9 +187,15 @@ k_tc_gemm(int W, int J, int NP, int nkc, int cps, int stages, const uint8_t* __r
           tc::mma_bf16(tmem, ad, bd, idesc, (i | ks | p) ? 1u : 0u);
         }
       tc::mma_commit(&empty[i % stages]);
+      const int prev = i - 1, next = i - 1 + stages;
+      if (prev >= 0 && next < n) {
+        if (!tc::mbar_wait(&empty[prev % stages], (prev / stages) & 1, &g_tc_error)) break;
+        load(next);
+      }
     }
     tc::mma_commit(&done);
   }
+  if (warp == 0) __syncwarp();
   bool ok = n > 0 ? tc::mbar_wait(&done, 0, &g_tc_error) : true;
   ok = __all_sync(0xffffffffu, ok);
   tc::tc_fence_after();
@@ -204,7 +209,7 @@ k_tc_gemm(int W, int J, int NP, int nkc, int cps, int stages, const uint8_t* __r
 #pragma unroll
         for (int q = 0; q < 16; ++q) {
           const int j = c0 + q;
-          if (j < J) pz[(size_t)j * W + r] = n > 0 ? v[q] : 0.f;
+          if (j < J) __stcs(pz + (size_t)j * W + r, n > 0 ? v[q] : 0.f);  // read once
         }
       }
     }
@@ -230,8 +235,9 @@ TcShape tc_shape(int W, int m, int J, int terms) {
   t.cps = (t.nkc + want - 1) / want;
   t.nz = (t.nkc + t.cps - 1) / t.cps;
   t.stage_bytes = (size_t)terms * (kTcTileA + (size_t)t.NP * kTcKc * 2);
-  // 227 KB per CTA, less static shared memory and the 1 KB alignment pad
-  t.stages = (int)std::min<size_t>(4, (kTcSmemMax - 2048) / t.stage_bytes);
+  // one CTA per SM with as many stages as fit in 227 KB (less static shared
+  // memory and the 1 KB alignment pad)
+  t.stages = (int)std::min<size_t>(kTcMaxStages, (kTcSmemMax - 2048) / t.stage_bytes);
   return t;
 }
 int tc_max_jobs(int terms) { return terms == 2 ? 192 : 160; }
