@@ -132,6 +132,20 @@ int pt_frames(const pt_grid* grid, int n_layers, const float* spectra, const flo
               int n_frames, const double* sx, const double* sy, int per_layer, int crop,
               int n_out, float scale, float* out, void* work, size_t work_bytes, void* stream);
 
+/* The shift theorem applied to the stored layer state
+ * (FourierFlowScreen.translate, src/pyturb/flow.py:96-129; the phasors of
+ * Atmosphere._integrate, src/pyturb/atmosphere.py:904-916): spectra_out[l] =
+ * spectra_in[l] * exp(2 pi i (f_x sx[l] + f_y sy[l])) with the same exact
+ * fixed-point phases as pt_frames, and likewise the (P, L, 3, 3)
+ * subharmonic coefficients (NULL when P = 0). sx, sy: host FP64 (L) [m].
+ * Frames rendered from the output at displacement s equal frames of the
+ * input at sx + s, which lets a captured frame loop (a CUDA graph of
+ * pt_frames calls with fixed relative displacements) be replayed at any
+ * start time. n_layers <= 64; in and out may alias. */
+int pt_layers_translate(const pt_grid* grid, int n_layers, const float* spectra_in,
+                        const float* sh_in, const double* sx, const double* sy,
+                        float* spectra_out, float* sh_out, void* stream);
+
 /* Atmosphere._lgs_zoom (src/pyturb/atmosphere.py:1047-1090): separable
  * T-tap cone zoom of L (ns, ns) layer screens into one (n, n) pupil,
  * summed over layers, times scale. idx (L, T, n) int32, w (L, T, n) f32. */

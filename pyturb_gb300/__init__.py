@@ -8,7 +8,7 @@ C-ABI library ``libpyturb_gb300.so`` (``include/pyturb_gb300.h``). There is no
 CPU path: ``device="cpu"`` is refused and a missing GPU or library raises.
 """
 
-from .atmosphere import Atmosphere, ExtrudeBoilingPerformanceWarning, PeriodicWrapWarning
+from .atmosphere import Atmosphere, ExtrudeBoilingPerformanceWarning, FrameLoop, PeriodicWrapWarning
 from .backend import to_numpy
 from .extrude import ExtrudedAtmosphere, build_extrusion, phase_covariance
 from .flow import FourierFlowScreen
@@ -21,6 +21,7 @@ __version__ = "0.1.0"
 
 __all__ = [
     "Atmosphere",
+    "FrameLoop",
     "PeriodicWrapWarning",
     "ExtrudeBoilingPerformanceWarning",
     "PhaseScreen",

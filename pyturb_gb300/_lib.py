@@ -78,6 +78,7 @@ SIGNATURES = {
     "pt_generate": (i32, [vp, i32, vp, vp, vp, vp, u64, u64, i32, i32, f32, i32, vp, vp, sz, vp]),
     "pt_layers_fill": (i32, [vp, i32, vp, vp, vp, vp, C.POINTER(C.c_uint64), vp, vp, vp]),
     "pt_frames": (i32, [vp, i32, vp, vp, i32, dptr, dptr, i32, i32, i32, f32, vp, vp, sz, vp]),
+    "pt_layers_translate": (i32, [vp, i32, vp, vp, dptr, dptr, vp, vp, vp]),
     "pt_lgs_zoom": (i32, [i32, i32, i32, i32, vp, vp, vp, f32, vp, vp]),
     "pt_boil_step": (i32, [vp, i32, vp, vp, vp, vp, vp, vp, f64, vp, vp, u64, u64, vp]),
     "pt_extrude_workspace_bytes": (sz, [i32, i32, i32]),

@@ -32,7 +32,7 @@ from .fourier import PhaseScreen, amplitude_table, subharmonic_tables
 from .optics import ARCSEC_TO_RAD, output_scale, seeing_from_r0
 from .profiles import Layer
 
-__all__ = ["Atmosphere", "PeriodicWrapWarning", "ExtrudeBoilingPerformanceWarning"]
+__all__ = ["Atmosphere", "FrameLoop", "PeriodicWrapWarning", "ExtrudeBoilingPerformanceWarning"]
 
 
 class PeriodicWrapWarning(UserWarning):
@@ -477,6 +477,12 @@ class Atmosphere:
         return self._spec.frames(disp_x, disp_y, self.margin_pix, self.n,
                                  self._scale(wavelength), out=out)
 
+    def frame_loop(self, dt: float, steps: int, wavelength: Optional[float] = None) -> "FrameLoop":
+        """A :class:`FrameLoop`: the ``steps``-frame loop of :meth:`frames` at
+        spacing ``dt`` captured once as a CUDA graph, replayed at any start time
+        (spectral engine, frozen flow, no LGS)."""
+        return FrameLoop(self, dt, steps, wavelength)
+
     def evolve(self, dt: float, wavelength: Optional[float] = None):
         """Advance the clock by ``dt`` and return the new OPD
         (``src/pyturb/atmosphere.py:1156-1189``)."""
@@ -530,3 +536,74 @@ class Atmosphere:
         return (f"Atmosphere(layers={len(self.layers)}, r0={self.r0_los:.3f} m, "
                 f"seeing={self.seeing:.2f}\", n={self.n}, diameter={self.diameter} m, "
                 f"engine={self.engine!r}, device={self.device!r})")
+
+
+class FrameLoop:
+    """The frame loop of :meth:`Atmosphere.frames` captured as a CUDA graph.
+
+    The graph holds the chunked frame-synthesis launches for the relative
+    times ``0, dt, 2 dt, ...`` (the reference's clock of repeated additions,
+    ``src/pyturb/atmosphere.py:1128-1154``), reading a translated copy of the
+    layer state. :meth:`render` moves the stored spectra and subharmonic
+    coefficients to ``t0`` with one exact phase-ramp launch
+    (``pt_layers_translate``) and replays the graph, so a window of frames at
+    any start time costs two launches from the host. The frames equal
+    ``Atmosphere.render(t0 + relative times)`` to float32 rounding. The layer
+    state is read at replay time, so re-seeding the atmosphere between
+    replays renders new realisations of the same window.
+    """
+
+    def __init__(self, atm: "Atmosphere", dt: float, steps: int,
+                 wavelength: Optional[float] = None) -> None:
+        torch = torch_module()
+        if atm.engine != "spectral" or atm._boiling or atm._lgs_mag is not None:
+            raise ValueError("frame_loop needs the spectral engine without boiling or LGS")
+        if not dt > 0:
+            raise ValueError("dt must be positive")
+        if int(steps) < 1:
+            raise ValueError("steps must be >= 1")
+        self.atm, self.dt, self.steps = atm, float(dt), int(steps)
+        spec = atm._spec
+        self._spec = spec
+        self._P = spec.P
+        self.times = np.empty(self.steps)
+        t = 0.0
+        for i in range(self.steps):  # the reference's clock: repeated float additions
+            self.times[i] = t
+            t += self.dt
+        self._sx = np.ascontiguousarray(atm._vx[None, :] * self.times[:, None])
+        self._sy = np.ascontiguousarray(atm._vy[None, :] * self.times[:, None])
+        self._scale = atm._scale(wavelength)
+        self._spectra = spec.spectra.clone()
+        self._sh = spec.sh_coef.clone()
+        dev = spec.grid.device
+        self.out = torch.empty((self.steps, atm.n, atm.n), dtype=torch.float32, device=dev)
+        self._render_body()                      # first launches outside the capture
+        torch.cuda.synchronize(dev)
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.graph, capture_error_mode="relaxed"):
+            self._render_body()
+        torch.cuda.synchronize(dev)
+
+    def _render_body(self) -> None:
+        spec, atm, k = self._spec, self.atm, self.atm.frames_chunk
+        for c0 in range(0, self.steps, k):
+            m = min(k, self.steps - c0)
+            _lib.call("pt_frames", spec.grid.handle, spec.L, dptr(self._spectra),
+                      dptr(self._sh) if self._P else None, m,
+                      _lib.as_dptr(self._sx[c0:c0 + m]), _lib.as_dptr(self._sy[c0:c0 + m]), 0,
+                      int(atm.margin_pix), int(atm.n), float(self._scale), dptr(self.out[c0:c0 + m]),
+                      dptr(spec.grid.work), spec.grid.work_bytes, stream_handle())
+
+    def render(self, t0: float):
+        """Frames at ``t0 + times`` into :attr:`out` (returned), ``(steps, n, n)``."""
+        atm, spec = self.atm, self._spec
+        sx0 = np.ascontiguousarray(atm._vx * float(t0), dtype=np.float64)
+        sy0 = np.ascontiguousarray(atm._vy * float(t0), dtype=np.float64)
+        if not atm._wrap_warned:
+            atm._check_wrap(sx0[None, :] + self._sx[-1:], sy0[None, :] + self._sy[-1:])
+        _lib.call("pt_layers_translate", spec.grid.handle, spec.L, dptr(spec.spectra),
+                  dptr(spec.sh_coef) if self._P else None, _lib.as_dptr(sx0), _lib.as_dptr(sy0),
+                  dptr(self._spectra), dptr(self._sh) if self._P else None, stream_handle())
+        self.graph.replay()
+        return self.out

@@ -1497,3 +1497,82 @@ extern "C" int pt_ifft2_noalloc(int ns, const float* in, float* out, int batch, 
   }
   return PT_OK;
 }
+
+// ------------------------------------------------------------------ translate
+// Layer spectra and subharmonic coefficients moved by a displacement per
+// layer, out = in * exp(2 pi i (f_x sx[l] + f_y sy[l])): the shift theorem of
+// FourierFlowScreen.translate / Atmosphere._integrate (src/pyturb/flow.py:
+// 96-129, src/pyturb/atmosphere.py:904-916) applied to the stored state, so
+// that frames rendered from the result at displacement s equal frames of the
+// original at sx[l] + s. Main-grid phases are exact 64-bit fixed point
+// (k' frac(s df) mod 1, fftfreq signs); subharmonic phases are FP64 mod 1.
+namespace pt {
+constexpr int kMaxTranslateLayers = 64;
+struct TranslateArgs {
+  uint64_t ux[kMaxTranslateLayers], uy[kMaxTranslateLayers];
+  double sx[kMaxTranslateLayers], sy[kMaxTranslateLayers];
+};
+
+__global__ void k_translate_spectra(int ns, int L, TranslateArgs a, const float2* __restrict__ in,
+                                    float2* __restrict__ out) {
+  const size_t npix = (size_t)ns * ns;
+  const size_t total = npix * L;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const int l = (int)(i / npix);
+    const size_t k = i % npix;
+    const int kx = (int)(k / ns), ky = (int)(k % ns);
+    const int64_t sx = kx <= (ns - 1) / 2 ? kx : kx - ns;
+    const int64_t sy = ky <= (ns - 1) / 2 ? ky : ky - ns;
+    const uint64_t ph = (uint64_t)sx * a.ux[l] + (uint64_t)sy * a.uy[l];
+    out[i] = cmul(in[i], phasor_from_fixed(ph));
+  }
+}
+
+__global__ void k_translate_sh(int P, int L, TranslateArgs a, const double* __restrict__ sh_freq,
+                               const float2* __restrict__ in, float2* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= P * L * 9) return;
+  const int ij = i % 9, l = (i / 9) % L, p = i / (9 * L);
+  const double fi = sh_freq[p * 3 + ij / 3], fk = sh_freq[p * 3 + ij % 3];
+  double ph = fi * a.sx[l] + fk * a.sy[l];
+  ph -= floor(ph);
+  float sn, cs;
+  sincospif(2.0f * (float)ph, &sn, &cs);
+  out[i] = cmul(in[i], make_float2(cs, sn));
+}
+}  // namespace pt
+
+extern "C" int pt_layers_translate(const pt_grid* g, int L, const float* spectra_in,
+                                   const float* sh_in, const double* sx, const double* sy,
+                                   float* spectra_out, float* sh_out, void* stream) {
+  if (int rc = check_grid(g, "pt_layers_translate")) return rc;
+  if (L < 1 || L > kMaxTranslateLayers)
+    return fail(PT_ERR_ARG, "pt_layers_translate: n_layers must be in [1, 64]");
+  if (!spectra_in || !spectra_out || !sx || !sy)
+    return fail(PT_ERR_ARG, "pt_layers_translate: NULL pointer");
+  if (g->P > 0 && (!sh_in || !sh_out))
+    return fail(PT_ERR_ARG, "pt_layers_translate: subharmonic coefficients are NULL");
+  TranslateArgs a{};
+  const double df = 1.0 / (g->ns * g->dx);
+  for (int l = 0; l < L; ++l) {
+    if (!std::isfinite(sx[l]) || !std::isfinite(sy[l]))
+      return fail(PT_ERR_ARG, "pt_layers_translate: displacement is not finite");
+    a.ux[l] = host_fixed(sx[l] * df);
+    a.uy[l] = host_fixed(sy[l] * df);
+    a.sx[l] = sx[l];
+    a.sy[l] = sy[l];
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  const size_t total = (size_t)g->ns * g->ns * L;
+  k_translate_spectra<<<(unsigned)std::min<size_t>((total + 255) / 256, 152 * 16), 256, 0, s>>>(
+      g->ns, L, a, (const float2*)spectra_in, (float2*)spectra_out);
+  count_launch();
+  if (g->P > 0) {
+    const int n = g->P * L * 9;
+    k_translate_sh<<<(n + 127) / 128, 128, 0, s>>>(g->P, L, a, g->sh_freq,
+                                                   (const float2*)sh_in, (float2*)sh_out);
+    count_launch();
+  }
+  return check_launch("pt_layers_translate");
+}
