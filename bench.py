@@ -324,6 +324,41 @@ def bench_diff(torch, G, iters: int = 3):
             "loss": float(loss.detach())}
 
 
+def bench_ragged(torch, reps: int = 5):
+    """Ragged Monte-Carlo ensemble: 4096 screens with n drawn from {128, 256,
+    384, 512, 1024} (weights 4:4:2:2:1), L0 from {10, 25, 50} m, r0 ~ U[0.08,
+    0.25] m, dx = 1/64 m, 3 subharmonic levels, seeded; one pt_generate_scaled
+    call per (n, L0) group per ensemble."""
+    from pyturb_gb300 import _lib
+    from pyturb_gb300.ragged import RaggedEnsemble
+
+    rng = np.random.default_rng(55)
+    S = 4096
+    sizes = rng.choice([128, 256, 384, 512, 1024], size=S, p=np.array([4, 4, 2, 2, 1]) / 13.0)
+    L0s = rng.choice([10.0, 25.0, 50.0], size=S)
+    r0s = rng.uniform(0.08, 0.25, S)
+    ens = RaggedEnsemble(sizes, r0s, L0s, pixel_scale=1.0 / 64, subharmonics=3, seed=55)
+    for _ in range(2):
+        ens.generate()
+    torch.cuda.synchronize()
+    c0 = _lib.launch_count()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        ens.generate()
+    e1.record()
+    torch.cuda.synchronize()
+    sec = e0.elapsed_time(e1) / 1000.0 / reps
+    out_bytes = 4.0 * float(np.sum(sizes.astype(np.float64) ** 2))
+    hbm, _, _ = peaks()
+    return {"workload": "4096 screens, n in {128,256,384,512,1024} w 4:4:2:2:1, L0 in "
+                        "{10,25,50} m, r0 ~ U[0.08,0.25] m, dx 1/64 m, 3 subharmonic levels",
+            "screens_per_s": S / sec, "ms_per_ensemble": sec * 1e3,
+            "output_gb": out_bytes / 1e9, "output_gbs": out_bytes / sec / 1e9,
+            "output_frac_of_hbm": out_bytes / sec / 1e9 / hbm,
+            "groups": ens.n_groups, "launches_per_ensemble": (_lib.launch_count() - c0) // reps}
+
+
 def run_reference(args, rank: int) -> None:
     if rank != 0:
         return
@@ -582,6 +617,7 @@ def main() -> None:
         line["extrude_1024"] = bench_extrude(torch, G)
     if not args.no_diff:
         line["diff_readout_768"] = bench_diff(torch, G)
+    line["ragged_mc_4096"] = bench_ragged(torch)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         fps, sps, cores, done, drawn = cpu_reference(200, MC_BATCH, 12.0)
         line["cpu_baseline"] = {

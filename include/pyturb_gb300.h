@@ -109,6 +109,18 @@ int pt_generate(const pt_grid* grid, int count, const float* amplitude, const fl
                 int crop, int n_out, float scale, int accumulate, float* out, void* work,
                 size_t work_bytes, void* stream);
 
+/* pt_generate with one extra factor per screen (Philox noise, no
+ * accumulation): screen i is scaled by scale * screen_scale[i] (device f32,
+ * count entries). The von Karman amplitude is proportional to r0^(-5/6), so
+ * one unit-r0 grid serves every screen of a (size, L0) group of a ragged
+ * Monte-Carlo ensemble with screen_scale = r0_i^(-5/6): the ensemble of
+ * independent PhaseScreen(n_i, dx, r0_i, L0_i).generate() calls
+ * (src/pyturb/fourier.py:233-282) in one call per group. */
+int pt_generate_scaled(const pt_grid* grid, int count, const float* amplitude,
+                       const float* sh_amp, uint64_t seed, uint64_t call, int crop, int n_out,
+                       float scale, const float* screen_scale, float* out, void* work,
+                       size_t work_bytes, void* stream);
+
 /* FourierFlowScreen.reseed (src/pyturb/flow.py:71-94) for L layers at once:
  *   spectra[l] = (noise[l,0] + i noise[l,1]) * amplitude[l]   (L, ns, ns) complex
  *   sh_coef[p, l] = (sh_noise[l,p,0] + i sh_noise[l,p,1]) * sh_amp[p, l]  (P, L, 3, 3) complex

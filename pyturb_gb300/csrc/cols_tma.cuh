@@ -195,12 +195,12 @@ k_pair_cols_tma(const __grid_constant__ CUtensorMap map, const float2* __restric
         }
         const size_t o = (size_t)xo * st.n_out + yo;
         if (do_re) {
-          const float val = st.scale * (x[i].x + lre);
+          const float val = img_scale_of(st, img_re) * (x[i].x + lre);
           float* dst = st.out + (size_t)img_re * plane + o;
           *dst = st.accumulate ? *dst + val : val;
         }
         if (do_im) {
-          const float val = st.scale * (x[i].y + lim);
+          const float val = img_scale_of(st, img_im) * (x[i].y + lim);
           float* dst = st.out + (size_t)img_im * plane + o;
           *dst = st.accumulate ? *dst + val : val;
         }

@@ -372,7 +372,12 @@ struct PairStore {
   const float2* basis;  // (P, 3, ns)
   int P;
   int sym;  // symmetric subharmonic frequencies (see k_pair_cols_reg)
+  const float* img_scale;  // per output image factor on top of `scale` (NULL: none)
 };
+
+__device__ __forceinline__ float img_scale_of(const PairStore& st, int img) {
+  return st.img_scale ? st.scale * __ldg(st.img_scale + img) : st.scale;
+}
 
 __global__ void __launch_bounds__(kThreads)
 k_pair_cols(FftDesc d, const float2* __restrict__ tw, const float2* __restrict__ work, int C,
@@ -436,12 +441,12 @@ k_pair_cols(FftDesc d, const float2* __restrict__ tw, const float2* __restrict__
     }
     const size_t o = (size_t)xo * st.n_out + yo;
     if (do_re) {
-      const float val = st.scale * (v.x + (lre - mre));
+      const float val = img_scale_of(st, img_re) * (v.x + (lre - mre));
       float* dst = st.out + (size_t)img_re * plane + o;
       *dst = st.accumulate ? *dst + val : val;
     }
     if (do_im) {
-      const float val = st.scale * (v.y + (lim - mim));
+      const float val = img_scale_of(st, img_im) * (v.y + (lim - mim));
       float* dst = st.out + (size_t)img_im * plane + o;
       *dst = st.accumulate ? *dst + val : val;
     }
@@ -1142,11 +1147,11 @@ extern "C" int pt_ifft2(const pt_grid* g, const float* in, float* out, int batch
   return PT_OK;
 }
 
-extern "C" int pt_generate(const pt_grid* g, int count, const float* amplitude,
-                           const float* sh_amp, const float* noise, const float* sh_noise,
-                           uint64_t seed, uint64_t call, int crop, int n_out, float scale,
-                           int accumulate, float* out, void* work, size_t work_bytes,
-                           void* stream) {
+static int generate_impl(const pt_grid* g, int count, const float* amplitude,
+                         const float* sh_amp, const float* noise, const float* sh_noise,
+                         uint64_t seed, uint64_t call, int crop, int n_out, float scale,
+                         const float* screen_scale, int accumulate, float* out, void* work,
+                         size_t work_bytes, void* stream) {
   if (int rc = check_grid(g, "pt_generate")) return rc;
   const int ns = g->ns, P = g->P;
   if (count < 1) return fail(PT_ERR_ARG, "pt_generate: count must be >= 1");
@@ -1192,6 +1197,7 @@ extern "C" int pt_generate(const pt_grid* g, int count, const float* amplitude,
     st.basis = g->basis;
     st.P = P;
     st.sym = g->sym;
+    st.img_scale = screen_scale;
     if (P > 0) {
       const int n_re = std::min(nb, count - b0);
       const int n_im = std::max(0, std::min(nb, count - (n_fft + b0)));
@@ -1215,6 +1221,24 @@ extern "C" int pt_generate(const pt_grid* g, int count, const float* amplitude,
     if (int rc = check_launch("pt_generate")) return rc;
   }
   return PT_OK;
+}
+
+extern "C" int pt_generate(const pt_grid* g, int count, const float* amplitude,
+                           const float* sh_amp, const float* noise, const float* sh_noise,
+                           uint64_t seed, uint64_t call, int crop, int n_out, float scale,
+                           int accumulate, float* out, void* work, size_t work_bytes,
+                           void* stream) {
+  return generate_impl(g, count, amplitude, sh_amp, noise, sh_noise, seed, call, crop, n_out,
+                       scale, nullptr, accumulate, out, work, work_bytes, stream);
+}
+
+extern "C" int pt_generate_scaled(const pt_grid* g, int count, const float* amplitude,
+                                  const float* sh_amp, uint64_t seed, uint64_t call, int crop,
+                                  int n_out, float scale, const float* screen_scale, float* out,
+                                  void* work, size_t work_bytes, void* stream) {
+  if (!screen_scale) return fail(PT_ERR_ARG, "pt_generate_scaled: screen_scale is NULL");
+  return generate_impl(g, count, amplitude, sh_amp, nullptr, nullptr, seed, call, crop, n_out,
+                       scale, screen_scale, 0, out, work, work_bytes, stream);
 }
 
 extern "C" int pt_layers_fill(const pt_grid* g, int L, const float* amplitude,

@@ -111,7 +111,8 @@ def subharmonic_tables(n: int, dx: float, r0: float, L0: float, P: int,
 class Grid:
     """Owner of one native ``pt_grid`` plan plus a workspace sized for it."""
 
-    def __init__(self, ns: int, dx: float, sh_freq: np.ndarray, n_layers: int = 1) -> None:
+    def __init__(self, ns: int, dx: float, sh_freq: np.ndarray, n_layers: int = 1,
+                 workspace: bool = True) -> None:
         self._lib = _lib.load()
         torch = torch_module()
         self.device = cuda_device()
@@ -125,7 +126,9 @@ class Grid:
                   _lib.as_dptr(freq) if self.P else None)
         self.handle = handle
         self.work_bytes = int(self._lib.pt_grid_workspace_bytes(handle, max(1, int(n_layers))))
-        self.work = torch.empty(self.work_bytes, dtype=torch.uint8, device=self.device)
+        # without a workspace the owner passes a shared one to each call
+        self.work = (torch.empty(self.work_bytes, dtype=torch.uint8, device=self.device)
+                     if workspace else None)
 
     def ensure_workspace(self, n_layers: int) -> None:
         """Grow the workspace to what ``n_layers`` layers need (never shrinks)."""
