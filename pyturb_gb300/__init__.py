@@ -14,6 +14,7 @@ from .extrude import ExtrudedAtmosphere, build_extrusion, phase_covariance
 from .flow import FourierFlowScreen
 from .fourier import PhaseScreen
 from .infinite import InfinitePhaseScreen
+from .io import load, save
 from .optics import air_refractivity, r0_at_wavelength, seeing_from_r0, water_vapour_refractivity
 from .profiles import Layer
 
@@ -32,6 +33,8 @@ __all__ = [
     "phase_covariance",
     "build_extrusion",
     "to_numpy",
+    "save",
+    "load",
     "air_refractivity",
     "water_vapour_refractivity",
     "r0_at_wavelength",
