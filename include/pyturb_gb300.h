@@ -295,6 +295,29 @@ int pt_lr_grad_screens(int B, int L, int S, int T, int D, int n, const double* m
                        const float* w, const int64_t* fix, const float* grad_out,
                        float* grad_screens, void* stream);
 
+/* ---- validation diagnostics ---------------------------------------------
+ * pyturb.utils.structure_function (src/pyturb/utils.py:159-201): for a stack
+ * phase (count, ny, nx) f32 (device), D[s-1] = (<(phi[i+s,j] - phi[i,j])^2> +
+ * <(phi[i,j+s] - phi[i,j])^2>) / 2 for s = 1..max_sep (< min(ny, nx)), each
+ * mean over all valid pairs of the stack; D is a DEVICE f64 array. */
+size_t pt_structure_workspace_bytes(int count, int ny, int nx, int max_sep);
+int pt_structure_function(int count, int ny, int nx, const float* phase, int max_sep, double* D,
+                          void* work, size_t work_bytes, void* stream);
+/* out (J, R) = X (J, K) . M (R, K)^T, f32 device, row-major (the
+ * least-squares Zernike projection of pyturb.analysis.zernike_decompose,
+ * src/pyturb/analysis.py:129-162, with M the pseudo-inverse of the pupil
+ * design matrix built on the host). Split-K with a fixed-order reduce. */
+size_t pt_matmul_nt_workspace_bytes(int R, int K, int J);
+int pt_matmul_nt(int R, int K, int J, const float* M, const float* X, float* out, void* work,
+                 size_t work_bytes, void* stream);
+/* pyturb.analysis.temporal_psd (src/pyturb/analysis.py:183-208) for `count`
+ * series of length T = grid ns (device f32, samples contiguous): psd[f] for
+ * f = 0..T/2 (device f32) = mean over series of |DFT(x - mean x)|^2 * 2 dt / T.
+ * T <= 8192 (any factorisation). */
+size_t pt_temporal_psd_workspace_bytes(const pt_grid* grid, int count);
+int pt_temporal_psd(const pt_grid* grid, int count, const float* series, double dt, float* psd,
+                    void* work, size_t work_bytes, void* stream);
+
 /* ---- tensor cores (tcgen05) ---------------------------------------------
  * Self-test of the tcgen05 path, no counterpart in the reference: one tile
  * D (128 x N) = A (128 x K) * B (N x K)^T with bf16 A, B (row-major, device)

@@ -94,6 +94,12 @@ SIGNATURES = {
     "pt_lr_partial_count": (sz, [i32, i32, i32, i32, i32]),
     "pt_lr_grad_params": (i32, [i32, i32, i32, i32, i32, i32, dptr, vp, vp, vp, vp, vp, vp]),
     "pt_lr_grad_screens": (i32, [i32, i32, i32, i32, i32, i32, dptr, vp, vp, vp, vp, vp]),
+    "pt_structure_workspace_bytes": (sz, [i32, i32, i32, i32]),
+    "pt_structure_function": (i32, [i32, i32, i32, vp, i32, vp, vp, sz, vp]),
+    "pt_matmul_nt_workspace_bytes": (sz, [i32, i32, i32]),
+    "pt_matmul_nt": (i32, [i32, i32, i32, vp, vp, vp, vp, sz, vp]),
+    "pt_temporal_psd_workspace_bytes": (sz, [vp, i32]),
+    "pt_temporal_psd": (i32, [vp, i32, vp, f64, vp, vp, sz, vp]),
     "pt_tc_probe": (i32, [i32, i32, vp, vp, vp, vp]),
     "pt_extrude_tc_operator_bytes": (sz, [i32, i32, i32, i32]),
     "pt_extrude_tc_prepare": (i32, [i32, i32, i32, vp, i32, vp, sz, vp]),

@@ -428,6 +428,45 @@ static int extrude_jobs(const char* who, const ExtrudeForm& form, int W, int m, 
   return PT_OK;
 }
 
+namespace pt {
+__global__ void k_matmul_reduce(int R, int J, int nsplit, const float* __restrict__ partial,
+                                float* __restrict__ out) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y;
+  if (r >= R || j >= J) return;
+  float s = 0.f;
+  for (int z = 0; z < nsplit; ++z) s += partial[((size_t)z * J + j) * R + r];
+  out[(size_t)j * R + r] = s;
+}
+}  // namespace pt
+
+extern "C" size_t pt_matmul_nt_workspace_bytes(int R, int K, int J) {
+  if (R < 1 || K < 1 || J < 1) return 0;
+  return (size_t)kMaxSplit * J * R * sizeof(float);
+}
+
+extern "C" int pt_matmul_nt(int R, int K, int J, const float* M, const float* X, float* out,
+                            void* work, size_t work_bytes, void* stream) {
+  if (R < 1 || K < 1 || J < 1) return fail(PT_ERR_ARG, "pt_matmul_nt: bad sizes");
+  if (!M || !X || !out) return fail(PT_ERR_ARG, "pt_matmul_nt: NULL pointer");
+  if (!work || work_bytes < pt_matmul_nt_workspace_bytes(R, K, J))
+    return fail(PT_ERR_ARG, "pt_matmul_nt: workspace too small");
+  if ((J + kTJ - 1) / kTJ > 65535) return fail(PT_ERR_UNSUPPORTED, "pt_matmul_nt: J too large");
+  cudaStream_t s = (cudaStream_t)stream;
+  const int nsplit = split_for(R, J, K);
+  const int kslice = ((K + nsplit - 1) / nsplit + kTK - 1) / kTK * kTK;
+  const int nz = (K + kslice - 1) / kslice;
+  float* partial = (float*)work;
+  {
+    ProfScope ps("k_extrude_gemm", s);
+    k_extrude_gemm<<<dim3((R + kTM - 1) / kTM, (J + kTJ - 1) / kTJ, nz), 256, 0, s>>>(
+        R, K, J, kslice, M, X, partial);
+  }
+  k_matmul_reduce<<<dim3((R + 255) / 256, J), 256, 0, s>>>(R, J, nz, partial, out);
+  count_launch_e(2);
+  return check_launch("pt_matmul_nt");
+}
+
 extern "C" int pt_extrude_rows(int W, int m, int cap, int G, const float* M, float* buf,
                                int n_jobs, const pt_extrude_job* jobs, const float* noise,
                                void* work, size_t work_bytes, void* stream) {

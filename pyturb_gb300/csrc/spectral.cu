@@ -1600,3 +1600,85 @@ extern "C" int pt_layers_translate(const pt_grid* g, int L, const float* spectra
   }
   return check_launch("pt_layers_translate");
 }
+
+// ------------------------------------------------------------------ temporal PSD
+// pyturb.analysis.temporal_psd (src/pyturb/analysis.py:183-208): each series
+// (samples along the last axis) minus its mean, |DFT|^2 * 2 dt / T, averaged
+// over the series. The DFT is the grid's mixed-radix transform of length
+// ns = T (|X(f)|^2 of a real series is the same for either sign). CTA b sums
+// the power of series b, b + G, ... in shared memory; a second kernel sums
+// the G partials in a fixed order.
+namespace pt {
+__global__ void __launch_bounds__(kThreads)
+k_psd_series(FftDesc d, const float2* __restrict__ tw, int count,
+             const float* __restrict__ series, float* __restrict__ partial) {
+  extern __shared__ float2 sm[];
+  __shared__ double red[32];
+  const int T = d.n, H = T / 2 + 1;
+  float2* bufA = sm;
+  float2* bufB = sm + T;
+  float2* stw = sm + 2 * T;
+  float* acc = (float*)(stw + T);
+  for (int i = threadIdx.x; i < T; i += blockDim.x) stw[i] = tw[i];
+  for (int f = threadIdx.x; f < H; f += blockDim.x) acc[f] = 0.f;
+  for (int s = blockIdx.x; s < count; s += gridDim.x) {
+    const float* x = series + (size_t)s * T;
+    double m = 0.0;
+    for (int i = threadIdx.x; i < T; i += blockDim.x) m += x[i];
+    for (int o = 16; o > 0; o >>= 1) m += __shfl_xor_sync(0xffffffffu, m, o);
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+    __syncthreads();
+    double tot = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tot += red[w];
+    const float mean = (float)(tot / T);
+    for (int i = threadIdx.x; i < T; i += blockDim.x) bufA[i] = make_float2(x[i] - mean, 0.f);
+    __syncthreads();
+    const float2* res = fft_smem(bufA, bufB, d, stw, 1, T, 1, false);
+    __syncthreads();
+    for (int f = threadIdx.x; f < H; f += blockDim.x) {
+      const float2 v = res[f];
+      acc[f] += v.x * v.x + v.y * v.y;
+    }
+    __syncthreads();
+  }
+  for (int f = threadIdx.x; f < H; f += blockDim.x) partial[(size_t)blockIdx.x * H + f] = acc[f];
+}
+
+__global__ void k_psd_reduce(int H, int G, double scale, const float* __restrict__ partial,
+                             float* __restrict__ psd) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= H) return;
+  double s = 0.0;
+  for (int b = 0; b < G; ++b) s += partial[(size_t)b * H + f];
+  psd[f] = (float)(s * scale);
+}
+
+static int psd_blocks(int count) { return std::max(1, std::min(count, 2 * 152)); }
+}  // namespace pt
+
+extern "C" size_t pt_temporal_psd_workspace_bytes(const pt_grid* g, int count) {
+  if (!g || count < 1) return 0;
+  return (size_t)psd_blocks(count) * (g->ns / 2 + 1) * sizeof(float);
+}
+
+extern "C" int pt_temporal_psd(const pt_grid* g, int count, const float* series, double dt,
+                               float* psd, void* work, size_t work_bytes, void* stream) {
+  if (int rc = check_grid(g, "pt_temporal_psd")) return rc;
+  if (count < 1 || !(dt > 0)) return fail(PT_ERR_ARG, "pt_temporal_psd: bad count or dt");
+  if (!series || !psd) return fail(PT_ERR_ARG, "pt_temporal_psd: NULL pointer");
+  if (!work || work_bytes < pt_temporal_psd_workspace_bytes(g, count))
+    return fail(PT_ERR_ARG, "pt_temporal_psd: workspace too small");
+  const int T = g->ns, H = T / 2 + 1, G = psd_blocks(count);
+  const size_t smem = (size_t)3 * T * sizeof(float2) + (size_t)H * sizeof(float);
+  if (smem > 220 * 1024) return fail(PT_ERR_UNSUPPORTED, "pt_temporal_psd: series longer than 8192");
+  if (int rc = set_smem(k_psd_series, smem, "k_psd_series")) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  {
+    ProfScope ps("k_psd_series", s);
+    k_psd_series<<<G, kThreads, smem, s>>>(g->desc, g->tw, count, series, (float*)work);
+  }
+  k_psd_reduce<<<(H + 127) / 128, 128, 0, s>>>(H, G, 2.0 * dt / T / count, (const float*)work, psd);
+  count_launch(2);
+  return check_launch("pt_temporal_psd");
+}
