@@ -242,6 +242,18 @@ int pt_readout(int n, int W, int cap, int interp, int n_layers, const pt_readout
 int pt_rows_sample(int n, int cap, int interp, int anchor_phys, int row_max, double shift,
                    const float* buf, float* out, void* stream);
 
+/* Extrusion boiling helpers (ExtrudedAtmosphere.boil_step,
+ * src/pyturb/extrude.py:661-753). pt_fill_normals: out (rows, cols) device
+ * f32 = row_scale[r] (host, rows <= 64) * Philox N(0, 1) keyed by (key, call):
+ * the white noise under the seed rows S . white of the fresh windows.
+ * pt_ring_blend: ring rows phys0, phys0 + 1, ... (mod cap) of one (cap, W)
+ * screen become a * buf + b * fresh (fresh: (h, W) device f32), the AR(1)
+ * blend buf[lo:hi] = a buf + b fresh on the modular ring. */
+int pt_fill_normals(uint64_t key, uint64_t call, int rows, int cols, const float* row_scale,
+                    float* out, void* stream);
+int pt_ring_blend(int W, int cap, float* screen, int phys0, int h, float a, float b,
+                  const float* fresh, void* stream);
+
 /* ---- tensor-core form of the extrusion product --------------------------
  * The split-precision form of pt_extrude_batch (same arguments and ring
  * semantics, src/pyturb/extrude.py:424-456): the operator [A | B_unit] and

@@ -49,6 +49,22 @@ def build_extrusion(width, m, dx, L0, r0=1.0):
     return a, v * np.sqrt(np.clip(w, 0.0, None))
 
 
+def seed_factor(width, m, dx, L0, r0=1.0):
+    """``S`` with ``S S^T = C_zz`` of the m stencil rows, the seed of boiling's
+    fresh windows (``src/pyturb/extrude.py:290-303``): Cholesky of the
+    symmetrised covariance, an eigen square root if that fails."""
+    yz, xz = np.mgrid[0:m, 0:width]
+    st = np.column_stack((xz.ravel(), yz.ravel())).astype(float)
+    czz = phase_covariance(np.hypot(st[:, None, 0] - st[None, :, 0],
+                                    st[:, None, 1] - st[None, :, 1]) * dx, r0, L0)
+    czz = (czz + czz.T) / 2.0
+    try:
+        return np.linalg.cholesky(czz)
+    except np.linalg.LinAlgError:
+        w, v = np.linalg.eigh(czz)
+        return v * np.sqrt(np.clip(w, 0.0, None))
+
+
 def compact_row_ring(buf, base, fill, m, first_readable_row):
     """``src/pyturb/ring.py:9-28``."""
     target = int(floor(first_readable_row)) - 1
@@ -113,7 +129,7 @@ class OracleExtruded:
 
     def __init__(self, n, pixel_scale, layer_r0, layer_L0, layer_wind, layer_altitude_los,
                  field_of_view_pix=0.0, stencil_rows=2, interp="cubic", lgs_altitude_los=None,
-                 seeds=None, rng_factory=np.random.default_rng):
+                 seeds=None, rng_factory=np.random.default_rng, tau_boil=None, boil_seed=None):
         self.n, self.dx, self.interp, self.m = int(n), float(pixel_scale), interp, stencil_rows
         L = len(layer_r0)
         fov = ([float(field_of_view_pix)] * L if np.ndim(field_of_view_pix) == 0
@@ -141,6 +157,43 @@ class OracleExtruded:
             a, b = cache[key]
             self.layers.append(_Layer(self.n, self.W, self.dx, r0, L0, vx, vy, alt, self.m,
                                       rng_factory(sd), a, b, self.cap, mag, fv))
+        # boiling (src/pyturb/extrude.py:472-496, 643-650, 695-753, the NumPy path)
+        self.tau = [float("inf")] * L if tau_boil is None else [
+            float("inf") if t is None else float(t) for t in tau_boil]
+        self.boiling = any(np.isfinite(t) for t in self.tau)
+        if self.boiling:
+            seeds_by_L0 = {}
+            for ly, r0, L0 in zip(self.layers, layer_r0, layer_L0):
+                key = round(float(L0), 9)
+                if key not in seeds_by_L0:
+                    seeds_by_L0[key] = seed_factor(self.W, self.m, self.dx, L0)
+                ly.seed = seeds_by_L0[key] * r0 ** (-5.0 / 6.0)
+            self.boil_rng = rng_factory(boil_seed)
+
+    def boil_step(self, dt):
+        """Blend every boiling layer's readable rows toward an independent
+        fresh window: ``buf[lo:hi] = a buf + b fresh``, a = exp(-dt/tau)."""
+        if not self.boiling:
+            return
+        regions = []
+        for i, ly in enumerate(self.layers):
+            if not np.isfinite(self.tau[i]):
+                continue
+            a = float(np.exp(-dt / self.tau[i]))
+            b = float(np.sqrt(max(0.0, 1.0 - a * a)))
+            lo = max(0, int(np.floor(ly.amin + ly.travel)) - ly.base - 3)
+            hi = ly.fill
+            if hi > lo:
+                regions.append((ly, lo, hi, a, b))
+        W, m = self.W, self.m
+        for ly, lo, hi, a, b in regions:
+            h = hi - lo
+            fresh = np.empty((h, W))
+            seed = (ly.seed @ self.boil_rng.standard_normal(m * W)).reshape(m, W)
+            fresh[:min(m, h)] = seed[:min(m, h)]
+            for k in range(m, h):
+                fresh[k] = ly.a @ fresh[k - m:k].ravel() + ly.b @ self.boil_rng.standard_normal(W)
+            ly.buf[lo:hi] = a * ly.buf[lo:hi] + b * fresh
 
     def set_time(self, t):
         for ly in self.layers:

@@ -101,6 +101,8 @@ SIGNATURES = {
     "pt_temporal_psd_workspace_bytes": (sz, [vp, i32]),
     "pt_temporal_psd": (i32, [vp, i32, vp, f64, vp, vp, sz, vp]),
     "pt_tc_probe": (i32, [i32, i32, vp, vp, vp, vp]),
+    "pt_fill_normals": (i32, [u64, u64, i32, i32, C.POINTER(f32), vp, vp]),
+    "pt_ring_blend": (i32, [i32, i32, vp, i32, i32, f32, f32, vp, vp]),
     "pt_extrude_tc_operator_bytes": (sz, [i32, i32, i32, i32]),
     "pt_extrude_tc_prepare": (i32, [i32, i32, i32, vp, i32, vp, sz, vp]),
     "pt_extrude_tc_workspace_bytes": (sz, [i32, i32, i32, i32]),

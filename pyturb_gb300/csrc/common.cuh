@@ -115,6 +115,7 @@ enum NoiseDomain : uint32_t {
   kDomainLayerSub = 0x44u,    // frozen-flow layer subharmonics
   kDomainExtrude = 0x55u,     // extrusion row noise
   kDomainBoil = 0x66u,        // boiling AR(1) innovations
+  kDomainBoilSeed = 0x77u,    // seed rows of extrusion boiling's fresh windows
 };
 
 // Complex N(0,1)+iN(0,1) pair for element `idx` of stream (`key`, `call`, `domain`).

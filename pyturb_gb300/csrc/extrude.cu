@@ -440,6 +440,68 @@ __global__ void k_matmul_reduce(int R, int J, int nsplit, const float* __restric
 }
 }  // namespace pt
 
+namespace pt {
+constexpr int kMaxBoilRows = 64;
+struct RowScales {
+  float v[kMaxBoilRows];
+};
+// out[r][c] = scale[r] * N(0, 1), Philox keyed by (key, r * cols + c, call).
+__global__ void k_fill_normals(uint64_t key, uint64_t call, int rows, int cols, RowScales sc,
+                               float* __restrict__ out) {
+  const size_t total = (size_t)rows * cols;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; 2 * i < total;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const float2 z = philox_cnormal(key, i, call, kDomainBoilSeed);
+    const size_t e = 2 * i;
+    out[e] = sc.v[e / cols] * z.x;
+    if (e + 1 < total) out[e + 1] = sc.v[(e + 1) / cols] * z.y;
+  }
+}
+
+// ring rows phys0, phys0 + 1, ... (mod cap) of one screen: buf = a buf + b fresh
+__global__ void k_ring_blend(int W, int cap, float* __restrict__ screen, int phys0, int h, float a,
+                             float b, const float* __restrict__ fresh) {
+  const size_t total = (size_t)h * W;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const int r = (int)(i / W), c = (int)(i % W);
+    int p = phys0 + r;
+    if (p >= cap) p -= cap;
+    float* d = screen + (size_t)p * W + c;
+    *d = fmaf(a, *d, b * fresh[i]);
+  }
+}
+}  // namespace pt
+
+extern "C" int pt_fill_normals(uint64_t key, uint64_t call, int rows, int cols,
+                               const float* row_scale, float* out, void* stream) {
+  if (rows < 1 || cols < 1 || rows > kMaxBoilRows)
+    return fail(PT_ERR_ARG, "pt_fill_normals: rows must be in [1, 64], cols >= 1");
+  if (!row_scale || !out) return fail(PT_ERR_ARG, "pt_fill_normals: NULL pointer");
+  RowScales sc{};
+  for (int r = 0; r < rows; ++r) sc.v[r] = row_scale[r];
+  const size_t pairs = ((size_t)rows * cols + 1) / 2;
+  cudaStream_t s = (cudaStream_t)stream;
+  k_fill_normals<<<(unsigned)std::min<size_t>((pairs + 255) / 256, 1024), 256, 0, s>>>(
+      key, call, rows, cols, sc, out);
+  count_launch_e();
+  return check_launch("pt_fill_normals");
+}
+
+extern "C" int pt_ring_blend(int W, int cap, float* screen, int phys0, int h, float a, float b,
+                             const float* fresh, void* stream) {
+  if (W < 1 || cap < 1 || h < 0 || h > cap || phys0 < 0 || phys0 >= cap)
+    return fail(PT_ERR_ARG, "pt_ring_blend: bad sizes");
+  if (!screen || (h > 0 && !fresh)) return fail(PT_ERR_ARG, "pt_ring_blend: NULL pointer");
+  if (h == 0) return PT_OK;
+  const size_t total = (size_t)h * W;
+  cudaStream_t s = (cudaStream_t)stream;
+  k_ring_blend<<<(unsigned)std::min<size_t>((total + 255) / 256, 4096), 256, 0, s>>>(
+      W, cap, screen, phys0, h, a, b, fresh);
+  count_launch_e();
+  return check_launch("pt_ring_blend");
+}
+
 extern "C" size_t pt_matmul_nt_workspace_bytes(int R, int K, int J) {
   if (R < 1 || K < 1 || J < 1) return 0;
   return (size_t)kMaxSplit * J * R * sizeof(float);

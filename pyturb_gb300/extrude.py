@@ -94,6 +94,37 @@ def build_extrusion(width: int, stencil_rows: int, pixel_scale: float, L0: float
     return a, b
 
 
+def seed_factor(width: int, stencil_rows: int, pixel_scale: float, L0: float) -> np.ndarray:
+    """FP64 ``S`` with ``S S^T = C_zz`` (unit r0) for the m stencil rows: the
+    seed of boiling's fresh windows (``src/pyturb/extrude.py:290-303``),
+    Cholesky of the symmetrised covariance or an eigen square root."""
+    m, n = int(stencil_rows), int(width)
+    yz, xz = np.mgrid[0:m, 0:n]
+    st = np.column_stack((xz.ravel(), yz.ravel())).astype(np.float64)
+    sep = np.hypot(st[:, None, 0] - st[None, :, 0], st[:, None, 1] - st[None, :, 1])
+    c_zz = phase_covariance(sep * pixel_scale, 1.0, L0)
+    c_zz = (c_zz + c_zz.T) / 2.0
+    try:
+        return np.linalg.cholesky(c_zz)
+    except np.linalg.LinAlgError:
+        w, v = np.linalg.eigh(c_zz)
+        return v * np.sqrt(np.clip(w, 0.0, None))
+
+
+class _RowQueue:
+    """A noise stream that hands out pre-drawn rows (the boil stream's draws,
+    taken in the reference's order and replayed to a scratch extrusion)."""
+
+    key = 0
+
+    def __init__(self, injected: bool) -> None:
+        self.injected = injected
+        self.rows: list = []
+
+    def draw(self, shape):
+        return self.rows.pop(0)
+
+
 def along_extent_and_span(n: int, vx: float, vy: float, mag: float,
                           fov_margin_pix: float) -> Tuple[float, int]:
     """A layer's along-wind half extent and buffer span (``src/pyturb/extrude.py:222-247``)."""
@@ -257,10 +288,6 @@ class ExtrudedAtmosphere:
             n, pixel_scale, layer_r0, layer_L0, layer_wind, layer_altitude_los,
             field_of_view_pix, stencil_rows, interp, lgs_altitude_los, device, dtype, seeds,
             tau_boil, boil_seed)
-        if any(np.isfinite(t) for t in config.tau_boil):
-            raise NotImplementedError(
-                "boiling on engine='extrude' is not implemented on the GPU backend yet; "
-                "use engine='spectral' boiling")
         self.config = config
         self.n = config.grid.n
         self.dx = config.grid.pixel_scale
@@ -307,6 +334,23 @@ class ExtrudedAtmosphere:
             init = gen.generate()
             self._ring.seed_rows(i, init[: self.layers[i].span])
             del gen
+        # boiling (src/pyturb/extrude.py:472-496, 586-650, 695-753)
+        self._tau = [float(t) for t in config.tau_boil]
+        self.boiling = any(np.isfinite(t) for t in self._tau)
+        if self.boiling:
+            self._boil_layers = [i for i, t in enumerate(self._tau) if np.isfinite(t)]
+            self._host_boil = host_noise is not None
+            self._boil = NoiseStream(config.boil_seed, host_noise)
+            seeds = [seed_factor(W, self.m, self.dx, a_L0) for a_L0 in
+                     sorted(op_index, key=op_index.get)]
+            self._S = upload(np.stack(seeds))                     # (G, mW, mW)
+            self._groups = groups
+            self._bscale = bscale
+            self._queues = [_RowQueue(self._host_boil) for _ in self._boil_layers]
+            self._scratch = RingExtruder(
+                W, self.m, self.capacity + self.m, [], [groups[i] for i in self._boil_layers],
+                [bscale[i] for i in self._boil_layers], self._queues,
+                device_operator=self._ring.M, form=extrude_form)
 
     @property
     def _buf(self):
@@ -337,8 +381,67 @@ class ExtrudedAtmosphere:
         self._ring.extrude(counts)
 
     def boil_step(self, dt: float) -> None:
-        """Frozen flow only on this backend (boiling is refused at construction)."""
-        return None
+        """One AR(1) boiling step (``src/pyturb/extrude.py:715-753``): every
+        boiling layer's readable rows ``[lo, hi)`` become ``a buf + b fresh``,
+        ``a = exp(-dt/tau)``, with ``fresh`` an independent window seeded by
+        ``S white`` and extruded with the layer's own operator. With host noise
+        the boil stream is consumed in the reference's order (per layer: the
+        ``m W`` seed normals, then ``W`` per extruded row)."""
+        if not self.boiling:
+            return
+        torch = torch_module()
+        W, m, cap = self.width, self.m, self.capacity
+        regions = []
+        for q, i in enumerate(self._boil_layers):
+            ly = self.layers[i]
+            a = float(np.exp(-dt / self._tau[i]))
+            b = float(np.sqrt(max(0.0, 1.0 - a * a)))
+            lo = max(0, int(np.floor(ly.along_min + ly.travel)) - ly.base - 3)
+            hi = ly.fill
+            if hi > lo:
+                regions.append((q, i, lo, hi, a, b))
+        if not regions:
+            return
+        scr = self._scratch
+        scales = np.asarray([self._bscale[i] for _, i, *_ in regions], dtype=np.float32)
+        dev = scr.buf.device
+        if self._host_boil:
+            whites = []
+            for (q, i, lo, hi, a, b), sc in zip(regions, scales):
+                whites.append(self._boil.draw((m * W,)) * float(sc))
+                self._queues[q].rows = [self._boil.draw((W,)) for _ in range(m, hi - lo)]
+            X = upload(np.stack(whites))
+        else:
+            call = self._boil.next_call()
+            X = torch.empty((len(regions), m * W), dtype=torch.float32, device=dev)
+            _lib.call("pt_fill_normals", self._boil.key, call, len(regions), m * W,
+                      scales.ctypes.data_as(C.POINTER(C.c_float)), dptr(X), stream_handle())
+            for q, *_ in regions:  # fresh Philox rows for every step's scratch extrusion
+                scr._key[q] = np.uint64((self._boil.key ^ (0x9E3779B97F4A7C15 * (call + 1))
+                                         ^ (q + 1) * 0xBF58476D1CE4E5B9) & 0xFFFFFFFFFFFFFFFF)
+        # seed rows S_g (r0^-5/6 white) for every region, one GEMM per operator group
+        seeds = torch.empty((len(regions), m * W), dtype=torch.float32, device=dev)
+        lib = _lib.load()
+        for g in sorted({self._groups[i] for _, i, *_ in regions}):
+            idx = [k for k, (_, i, *_r) in enumerate(regions) if self._groups[i] == g]
+            Xg = X[idx].contiguous()
+            out = torch.empty_like(Xg)
+            nbytes = int(lib.pt_matmul_nt_workspace_bytes(m * W, m * W, len(idx)))
+            work = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+            _lib.call("pt_matmul_nt", m * W, m * W, len(idx), dptr(self._S[g]), dptr(Xg),
+                      dptr(out), dptr(work), nbytes, stream_handle())
+            seeds[idx] = out
+        counts = np.zeros(scr.S, dtype=np.int32)
+        for k, (q, i, lo, hi, a, b) in enumerate(regions):
+            h = hi - lo
+            scr.seed_rows(q, seeds[k].view(m, W)[:min(m, h)])
+            counts[q] = max(0, h - m)
+        scr.extrude(counts)
+        for q, i, lo, hi, a, b in regions:
+            ly = self.layers[i]
+            phys0 = (ly.base + lo - ly.v0) % cap
+            _lib.call("pt_ring_blend", W, cap, dptr(self._ring.buf[i]), int(phys0), hi - lo,
+                      a, b, dptr(scr.buf[q]), stream_handle())
 
     def readout_params(self, thx: float = 0.0, thy: float = 0.0):
         arr = (_lib.ReadoutLayer * len(self.layers))()

@@ -132,6 +132,8 @@ def ext_layer_args(m, field_of_view=0.0, lgs_altitude=None):
     master = np.random.SeedSequence(m["seed"])
     children = master.spawn(len(lys))
     seeds = [int(c.spawn(3)[2].generate_state(1)[0]) for c in children]
+    master.spawn(1)  # the spectral engine's boil stream
+    ext_boil_seed = int(master.spawn(1)[0].generate_state(1)[0])
     alt = [ly.altitude * air for ly in lys]
     wind = [(ly.wind_speed * np.cos(np.deg2rad(ly.wind_direction)),
              ly.wind_speed * np.sin(np.deg2rad(ly.wind_direction))) for ly in lys]
@@ -140,7 +142,7 @@ def ext_layer_args(m, field_of_view=0.0, lgs_altitude=None):
                 layer_L0=[ly.L0 for ly in lys], layer_wind=wind, layer_altitude_los=alt,
                 field_of_view_pix=[a * np.tan(field_of_view * arc) / dx for a in alt],
                 lgs_altitude_los=None if lgs_altitude is None else lgs_altitude * air,
-                seeds=seeds)
+                seeds=seeds, boil_seed=ext_boil_seed)
 
 
 def _oracle_ext(name, meta):
@@ -153,6 +155,16 @@ def _oracle_ext(name, meta):
         e.set_time(m["t"])
         return np.stack([e.integrate(np.tan(a * arc), np.tan(b * arc))
                          for a, b in m["directions"]]) * (500e-9 / (2 * np.pi))
+    if name == "ext_boil":
+        m = meta[name]
+        e = O.OracleExtruded(interp="linear", tau_boil=m["tau_boil"], **ext_layer_args(m))
+        out, t = [], 0.0
+        for _ in range(m["steps"]):  # Atmosphere.frames: frame, then the boil step
+            e.set_time(t)
+            out.append(e.integrate() * (500e-9 / (2 * np.pi)))
+            e.boil_step(m["dt"])
+            t += m["dt"]
+        return np.stack(out)
     m = meta["ext"]
     interp = name.split("_", 1)[1]
     e = O.OracleExtruded(interp=interp, **ext_layer_args(m))
@@ -270,6 +282,11 @@ def _gpu_ext(name, meta):
                          field_of_view=m["field_of_view"], lgs_altitude=m["lgs_altitude"],
                          host_noise=rng, **kw(m))
         return np_(a.opd(m["t"], directions=m["directions"]))
+    if name == "ext_boil":
+        m = meta[name]
+        a = G.Atmosphere(_gpu_layers(m["profile"]), engine="extrude", interp="linear",
+                         tau_boil=m["tau_boil"], host_noise=rng, **kw(m))
+        return np.stack([np_(f) for _, f in a.frames(dt=m["dt"], steps=m["steps"])])
     m = meta["ext"]
     interp = name.split("_", 1)[1]
     a = G.Atmosphere(_gpu_layers(m["profile"]), engine="extrude", interp=interp,
@@ -280,7 +297,7 @@ def _gpu_ext(name, meta):
 CASES = ["gen_64", "gen_48", "gen_37", "gen_64_nosh", "gen_32_kolmo", "gen_60_vk", "flow_64",
          "atm_frames", "atm_frames_t", "atm_opd_t0.5", "atm_opd_wl", "atm_sample", "atm_dirs",
          "atm2_sample", "atm2_opd_wl", "atm_lgs_cubic", "atm_lgs_linear", "atm_lgs_lanczos",
-         "atm_boil", "ext_cubic", "ext_linear", "ext_lanczos", "ext_dirs_lgs", "inf_cubic",
+         "atm_boil", "ext_cubic", "ext_linear", "ext_lanczos", "ext_dirs_lgs", "ext_boil", "inf_cubic",
          "inf_linear", "inf_lanczos"]
 
 

@@ -114,6 +114,13 @@ def main() -> None:
                                 interp=interp, **ext_kw)
         cases[f"ext_{interp}"] = np.stack([f for _, f in atm.frames(dt=0.04, steps=8)])
     meta["ext"] = dict(kind="extrude", profile=PROFILE, dt=0.04, steps=8, **ext_kw)
+    # boiling on the extrusion engine: two boiling layers and one frozen
+    tau = [0.08, float("inf"), 0.2]
+    atm = pyturb.Atmosphere(layers(PROFILE), dtype="float64", engine="extrude", interp="linear",
+                            tau_boil=tau, **ext_kw)
+    cases["ext_boil"] = np.stack([f for _, f in atm.frames(dt=0.04, steps=6)])
+    meta["ext_boil"] = dict(kind="extrude", profile=PROFILE, dt=0.04, steps=6, tau_boil=tau,
+                            **ext_kw)
     atm = pyturb.Atmosphere(layers(PROFILE), dtype="float64", engine="extrude",
                             field_of_view=30.0, lgs_altitude=90e3, **ext_kw)
     cases["ext_dirs_lgs"] = np.asarray(atm.opd(0.05, directions=[(0.0, 0.0), (20.0, -10.0)]))
