@@ -167,7 +167,10 @@ k_pair_cols_reg(const float2* __restrict__ tw, const float2* __restrict__ work, 
   for (int i = 0; i < 8; ++i)
     x[i] = ok ? work[((size_t)pl * N + j + T * i) * N + y] : make_float2(0.f, 0.f);
   __syncthreads();
-  // per-column symmetric-basis constants, read by this thread only
+  // per-column symmetric-basis constants: K (this thread's registers) and,
+  // per level, (U_re, W_re, U_im, W_im) in a shared float4 table read once per
+  // output element (the FFT's own barriers order these writes before use)
+  float4* utab = (float4*)(mtab + 2 * 3 * P * C);
   float k0 = 0.f, k1 = 0.f;
   if (st.sym) {
     for (int p = 0; p < P; ++p) {
@@ -176,6 +179,12 @@ k_pair_cols_reg(const float2* __restrict__ tw, const float2* __restrict__ work, 
     }
     if (P > 0 && do_re) k0 -= st.mean[row_re];
     if (P > 0 && do_im) k1 -= st.mean[row_im];
+    for (int i = threadIdx.x; i < P * C; i += blockDim.x) {
+      const int p = i / C, cc = i % C;
+      const float2 m00 = mtab[(0 * 3 * P + 3 * p) * C + cc], m02 = mtab[(0 * 3 * P + 3 * p + 2) * C + cc];
+      const float2 m10 = mtab[(1 * 3 * P + 3 * p) * C + cc], m12 = mtab[(1 * 3 * P + 3 * p + 2) * C + cc];
+      utab[i] = make_float4(m00.x + m02.x, m02.y - m00.y, m10.x + m12.x, m12.y - m10.y);
+    }
   }
   reg_fft<N>(x, j, stw, s);
   if (!ok) return;
@@ -184,6 +193,7 @@ k_pair_cols_reg(const float2* __restrict__ tw, const float2* __restrict__ work, 
   if (yo < 0 || yo >= st.n_out) return;
   const float mre = (P > 0 && do_re) ? st.mean[row_re] : 0.f;
   const float mim = (P > 0 && do_im) ? st.mean[row_im] : 0.f;
+  const float sre = img_scale_of(st, img_re), sim = img_scale_of(st, img_im);
 #pragma unroll
   for (int i = 0; i < 8; ++i) {
     const int xr = j + T * i;
@@ -194,11 +204,10 @@ k_pair_cols_reg(const float2* __restrict__ tw, const float2* __restrict__ work, 
       lre = k0;
       lim = k1;
       for (int p = 0; p < P; ++p) {
-        const float2 b = st.basis[(size_t)(3 * p) * N + xr];
-        const float2 m00 = mtab[(0 * 3 * P + 3 * p) * C + c], m02 = mtab[(0 * 3 * P + 3 * p + 2) * C + c];
-        const float2 m10 = mtab[(1 * 3 * P + 3 * p) * C + c], m12 = mtab[(1 * 3 * P + 3 * p + 2) * C + c];
-        lre = fmaf(b.x, m00.x + m02.x, fmaf(b.y, m02.y - m00.y, lre));
-        lim = fmaf(b.x, m10.x + m12.x, fmaf(b.y, m12.y - m10.y, lim));
+        const float2 b = __ldg(st.basis + (size_t)(3 * p) * N + xr);
+        const float4 u = utab[p * C + c];
+        lre = fmaf(b.x, u.x, fmaf(b.y, u.y, lre));
+        lim = fmaf(b.x, u.z, fmaf(b.y, u.w, lim));
       }
     } else {
       lre = -mre;
@@ -213,12 +222,12 @@ k_pair_cols_reg(const float2* __restrict__ tw, const float2* __restrict__ work, 
     }
     const size_t o = (size_t)xo * st.n_out + yo;
     if (do_re) {
-      const float val = img_scale_of(st, img_re) * (x[i].x + lre);
+      const float val = sre * (x[i].x + lre);
       float* dst = st.out + (size_t)img_re * plane + o;
       *dst = st.accumulate ? *dst + val : val;
     }
     if (do_im) {
-      const float val = img_scale_of(st, img_im) * (x[i].y + lim);
+      const float val = sim * (x[i].y + lim);
       float* dst = st.out + (size_t)img_im * plane + o;
       *dst = st.accumulate ? *dst + val : val;
     }
