@@ -267,8 +267,11 @@ k_frame_rows_uniform_reg(const float2* __restrict__ tw, const float2* __restrict
   const int kx = blockIdx.x;
   const int fbeg = blockIdx.y * kAnchor;
   const int nkx = (N - kx) & (N - 1);
-  // packed state: lanes (layer 2q, layer 2q+1)
-  f2x Ax[E][LP], Ay[E][LP], Rx[E][LP], Ry[E][LP];
+  // packed state: lanes (layer 2q, layer 2q+1). With one column per thread
+  // -Ry is kept beside Ry so the complex step needs no separate negation
+  // (two columns per thread would spill it).
+  constexpr bool kNegR = E == 1;
+  f2x Ax[E][LP], Ay[E][LP], Rx[E][LP], Ry[E][LP], NRy[kNegR ? E : 1][kNegR ? LP : 1];
 #pragma unroll
   for (int e = 0; e < E; ++e) {
     const int ky = threadIdx.x + e * THREADS;
@@ -298,6 +301,7 @@ k_frame_rows_uniform_reg(const float2* __restrict__ tw, const float2* __restrict
       Ay[e][q] = pk2(ay[0], ay[1]);
       Rx[e][q] = pk2(rx[0], rx[1]);
       Ry[e][q] = pk2(ry[0], ry[1]);
+      if constexpr (kNegR) NRy[e][q] = pk2(-ry[0], -ry[1]);
     }
   }
   // Hermitian symmetry H(-k) = conj H(k): this CTA synthesises row kx only and
@@ -328,7 +332,9 @@ k_frame_rows_uniform_reg(const float2* __restrict__ tw, const float2* __restrict
                 hxa = add2(hxa, Ax[e][q]);
                 hya = add2(hya, Ay[e][q]);
               }
-              const f2x nx = fma2(Ax[e][q], Rx[e][q], neg2(mul2(Ay[e][q], Ry[e][q])));
+              f2x nx;
+              if constexpr (kNegR) nx = fma2(Ax[e][q], Rx[e][q], mul2(Ay[e][q], NRy[e][q]));
+              else nx = fma2(Ax[e][q], Rx[e][q], neg2(mul2(Ay[e][q], Ry[e][q])));
               const f2x ny = fma2(Ax[e][q], Ry[e][q], mul2(Ay[e][q], Rx[e][q]));
               Ax[e][q] = nx;
               Ay[e][q] = ny;
