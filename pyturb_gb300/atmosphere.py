@@ -477,11 +477,12 @@ class Atmosphere:
         return self._spec.frames(disp_x, disp_y, self.margin_pix, self.n,
                                  self._scale(wavelength), out=out)
 
-    def frame_loop(self, dt: float, steps: int, wavelength: Optional[float] = None) -> "FrameLoop":
+    def frame_loop(self, dt: float, steps: int, wavelength: Optional[float] = None,
+                   branches: int = 4) -> "FrameLoop":
         """A :class:`FrameLoop`: the ``steps``-frame loop of :meth:`frames` at
         spacing ``dt`` captured once as a CUDA graph, replayed at any start time
         (spectral engine, frozen flow, no LGS)."""
-        return FrameLoop(self, dt, steps, wavelength)
+        return FrameLoop(self, dt, steps, wavelength, branches)
 
     def evolve(self, dt: float, wavelength: Optional[float] = None):
         """Advance the clock by ``dt`` and return the new OPD
@@ -554,8 +555,10 @@ class FrameLoop:
     """
 
     def __init__(self, atm: "Atmosphere", dt: float, steps: int,
-                 wavelength: Optional[float] = None) -> None:
+                 wavelength: Optional[float] = None, branches: int = 4) -> None:
         torch = torch_module()
+        if not 1 <= int(branches) <= 8:
+            raise ValueError("branches must be in [1, 8]")
         if atm.engine != "spectral" or atm._boiling or atm._lgs_mag is not None:
             raise ValueError("frame_loop needs the spectral engine without boiling or LGS")
         if not dt > 0:
@@ -578,6 +581,13 @@ class FrameLoop:
         self._sh = spec.sh_coef.clone()
         dev = spec.grid.device
         self.out = torch.empty((self.steps, atm.n, atm.n), dtype=torch.float32, device=dev)
+        # `branches` graph branches: chunk c goes to stream c % branches with its
+        # own workspace, so one chunk's latency-bound launches overlap another's
+        self.branches = int(branches)
+        self._work = [spec.grid.work] + [
+            torch.empty(spec.grid.work_bytes, dtype=torch.uint8, device=dev)
+            for _ in range(self.branches - 1)]
+        self._side = [torch.cuda.Stream(dev) for _ in range(self.branches - 1)]
         self._render_body()                      # first launches outside the capture
         torch.cuda.synchronize(dev)
         self.graph = torch.cuda.CUDAGraph()
@@ -586,14 +596,22 @@ class FrameLoop:
         torch.cuda.synchronize(dev)
 
     def _render_body(self) -> None:
+        torch = torch_module()
         spec, atm, k = self._spec, self.atm, self.atm.frames_chunk
-        for c0 in range(0, self.steps, k):
+        main = torch.cuda.current_stream()
+        streams = [main] + self._side
+        for sd in self._side:
+            sd.wait_stream(main)
+        for c, c0 in enumerate(range(0, self.steps, k)):
             m = min(k, self.steps - c0)
+            b = c % self.branches
             _lib.call("pt_frames", spec.grid.handle, spec.L, dptr(self._spectra),
                       dptr(self._sh) if self._P else None, m,
                       _lib.as_dptr(self._sx[c0:c0 + m]), _lib.as_dptr(self._sy[c0:c0 + m]), 0,
                       int(atm.margin_pix), int(atm.n), float(self._scale), dptr(self.out[c0:c0 + m]),
-                      dptr(spec.grid.work), spec.grid.work_bytes, stream_handle())
+                      dptr(self._work[b]), spec.grid.work_bytes, streams[b].cuda_stream)
+        for sd in self._side:
+            main.wait_stream(sd)
 
     def render(self, t0: float):
         """Frames at ``t0 + times`` into :attr:`out` (returned), ``(steps, n, n)``."""
