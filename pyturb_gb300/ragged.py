@@ -7,8 +7,10 @@ The reference draws such an ensemble as independent
 ``r0^(-5/6)`` (``fourier.py:131-228``), so the screens of one (n, dx, L0) group
 share a unit-r0 grid plan and filter and take ``r0_i^(-5/6)`` as a per-screen
 factor in the fused column epilogue (``pt_generate_scaled``). The screens are
-packed into one float32 buffer, group after group, sharing one workspace;
-:meth:`RaggedEnsemble.screen` returns screen ``i`` in the caller's order.
+packed into one float32 buffer, group after group; the groups are spread over
+a few streams with a workspace each, so the small groups' latency-bound
+launches overlap. :meth:`RaggedEnsemble.screen` returns screen ``i`` in the
+caller's order.
 """
 
 from __future__ import annotations
@@ -50,7 +52,7 @@ class RaggedEnsemble:
 
     def __init__(self, sizes: Sequence[int], r0, L0, pixel_scale=1.0 / 64,
                  subharmonics: int = 3, power_law: float = 11.0 / 3.0, seed=None,
-                 device: str = "gpu") -> None:
+                 device: str = "gpu", streams: int = 4) -> None:
         torch = torch_module()
         check_device(device)
         sizes = np.asarray(sizes, dtype=np.int64).reshape(-1)
@@ -83,19 +85,39 @@ class RaggedEnsemble:
                 pos += int(sizes[i]) ** 2
         dev = cuda_device()
         self.buffer = torch.empty(pos, dtype=torch.float32, device=dev)
+        # groups run on `streams` streams (largest groups first, round robin),
+        # each stream with its own workspace, so small groups overlap
+        if not 1 <= int(streams) <= 16:
+            raise ValueError("streams must be in [1, 16]")
         self.work_bytes = max(g.grid.work_bytes for g in self.groups)
-        self.work = torch.empty(self.work_bytes, dtype=torch.uint8, device=dev)
+        self.n_streams = min(int(streams), len(self.groups))
+        self._works = [torch.empty(self.work_bytes, dtype=torch.uint8, device=dev)
+                       for _ in range(self.n_streams)]
+        self.work = self._works[0]
+        self._side = [torch.cuda.Stream(dev) for _ in range(self.n_streams - 1)]
+        self._order = sorted(range(len(self.groups)),
+                             key=lambda k: -len(self.groups[k].members) * self.groups[k].n ** 2)
         self._rng = NoiseStream(seed, None)
         self._keys = [self._rng.next_key() for _ in self.groups]
 
     def generate(self):
-        """Draw a new ensemble into :attr:`buffer` and return it."""
+        """Draw a new ensemble into :attr:`buffer` and return it (ordered on the
+        current stream: later work on it sees the whole ensemble)."""
+        torch = torch_module()
         call = self._rng.next_call()
-        for g, off, key in zip(self.groups, self._group_off, self._keys):
+        main = torch.cuda.current_stream()
+        streams = [main] + self._side
+        for sd in self._side:
+            sd.wait_stream(main)
+        for slot, k in enumerate(self._order):
+            g, off, key = self.groups[k], self._group_off[k], self._keys[k]
+            b = slot % self.n_streams
             _lib.call("pt_generate_scaled", g.grid.handle, len(g.members), dptr(g.amplitude),
                       dptr(g.sh_amp), key, call, 0, g.n, 1.0, dptr(g.scale),
-                      self.buffer.data_ptr() + 4 * off, dptr(self.work), self.work_bytes,
-                      stream_handle())
+                      self.buffer.data_ptr() + 4 * off, dptr(self._works[b]), self.work_bytes,
+                      streams[b].cuda_stream)
+        for sd in self._side:
+            main.wait_stream(sd)
         return self.buffer
 
     def screen(self, i: int):
