@@ -337,7 +337,8 @@ def bench_ragged(torch, reps: int = 5):
     sizes = rng.choice([128, 256, 384, 512, 1024], size=S, p=np.array([4, 4, 2, 2, 1]) / 13.0)
     L0s = rng.choice([10.0, 25.0, 50.0], size=S)
     r0s = rng.uniform(0.08, 0.25, S)
-    ens = RaggedEnsemble(sizes, r0s, L0s, pixel_scale=1.0 / 64, subharmonics=3, seed=55)
+    ens = RaggedEnsemble(sizes, r0s, L0s, pixel_scale=1.0 / 64, subharmonics=3, seed=55,
+                         autotune=True)  # tuned at construction, outside the timing
     for _ in range(2):
         ens.generate()
     torch.cuda.synchronize()

@@ -69,6 +69,18 @@ int pt_grid_create(pt_grid** out, int ns, double pixel_scale, int n_levels,
                    const double* sh_freq);
 int pt_grid_destroy(pt_grid* grid);
 
+/* Tuning knobs of a grid (no reference counterpart; read and set by the
+ * package's autotuner). pt_grid_radices reports the stage radices of the
+ * mixed-radix transform (used for sizes other than powers of two up to
+ * 4096); pt_grid_set_radices replaces them with any factorisation of ns into
+ * n_stages radices >= 2 (n_stages <= 23; radices other than 2, 3, 4, 5, 7, 8
+ * run as direct-sum stages). pt_grid_set_cols_variant picks the column pass
+ * of power-of-two grids: 0 register-fed (default), 1 TMA-fed. Results do not
+ * depend on either choice beyond float32 rounding. */
+int pt_grid_radices(const pt_grid* grid, int* n_stages, int* radices);
+int pt_grid_set_radices(pt_grid* grid, int n_stages, const int* radices);
+int pt_grid_set_cols_variant(pt_grid* grid, int variant);
+
 /* Workspace needed by pt_generate / pt_frames / pt_ifft2 on this grid
  * (largest over the three, for the chunk sizes the library uses). */
 size_t pt_grid_workspace_bytes(const pt_grid* grid, int n_layers);

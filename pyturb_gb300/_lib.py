@@ -73,6 +73,9 @@ SIGNATURES = {
     "pt_grid_create": (i32, [C.POINTER(vp), i32, f64, i32, dptr]),
     "pt_grid_destroy": (i32, [vp]),
     "pt_grid_workspace_bytes": (sz, [vp, i32]),
+    "pt_grid_radices": (i32, [vp, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "pt_grid_set_radices": (i32, [vp, i32, C.POINTER(C.c_int)]),
+    "pt_grid_set_cols_variant": (i32, [vp, i32]),
     "pt_ifft2": (i32, [vp, vp, vp, i32, vp, sz, vp]),
     "pt_ifft2_noalloc": (i32, [i32, vp, vp, i32, vp]),
     "pt_generate": (i32, [vp, i32, vp, vp, vp, vp, u64, u64, i32, i32, f32, i32, vp, vp, sz, vp]),

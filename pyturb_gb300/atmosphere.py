@@ -478,10 +478,19 @@ class Atmosphere:
                                  self._scale(wavelength), out=out)
 
     def frame_loop(self, dt: float, steps: int, wavelength: Optional[float] = None,
-                   branches: int = 4) -> "FrameLoop":
+                   branches=4) -> "FrameLoop":
         """A :class:`FrameLoop`: the ``steps``-frame loop of :meth:`frames` at
         spacing ``dt`` captured once as a CUDA graph, replayed at any start time
-        (spectral engine, frozen flow, no LGS)."""
+        (spectral engine, frozen flow, no LGS). ``branches="auto"`` times 1-4
+        concurrent branches once (cached on disk per device and sizes)."""
+        if branches == "auto":
+            from .tuning import choose
+
+            loop = FrameLoop(self, dt, steps, wavelength, 1)
+            choose(f"frame_loop|branches|ns={self.n_screen}|L={len(self.layers)}|"
+                   f"steps={int(steps)}|chunk={self.frames_chunk}", [1, 2, 3, 4],
+                   loop.capture, lambda: loop.render(0.0), warmup=1, reps=3)
+            return loop
         return FrameLoop(self, dt, steps, wavelength, branches)
 
     def evolve(self, dt: float, wavelength: Optional[float] = None):
@@ -581,13 +590,27 @@ class FrameLoop:
         self._sh = spec.sh_coef.clone()
         dev = spec.grid.device
         self.out = torch.empty((self.steps, atm.n, atm.n), dtype=torch.float32, device=dev)
-        # `branches` graph branches: chunk c goes to stream c % branches with its
-        # own workspace, so one chunk's latency-bound launches overlap another's
-        self.branches = int(branches)
-        self._work = [spec.grid.work] + [
-            torch.empty(spec.grid.work_bytes, dtype=torch.uint8, device=dev)
-            for _ in range(self.branches - 1)]
-        self._side = [torch.cuda.Stream(dev) for _ in range(self.branches - 1)]
+        self._work = [spec.grid.work]
+        self._side = []
+        self.graph = None
+        self.capture(branches)
+
+    def capture(self, branches: int) -> None:
+        """(Re)capture the graph with ``branches`` branches: chunk c goes to
+        stream c % branches with its own workspace, so one chunk's
+        latency-bound launches overlap another's."""
+        torch = torch_module()
+        branches = int(branches)
+        if not 1 <= branches <= 8:
+            raise ValueError("branches must be in [1, 8]")
+        dev = self._spec.grid.device
+        self.branches = branches
+        while len(self._work) < branches:
+            self._work.append(torch.empty(self._spec.grid.work_bytes, dtype=torch.uint8,
+                                          device=dev))
+        while len(self._side) < branches - 1:
+            self._side.append(torch.cuda.Stream(dev))
+        self.graph = None
         self._render_body()                      # first launches outside the capture
         torch.cuda.synchronize(dev)
         self.graph = torch.cuda.CUDAGraph()
@@ -599,8 +622,9 @@ class FrameLoop:
         torch = torch_module()
         spec, atm, k = self._spec, self.atm, self.atm.frames_chunk
         main = torch.cuda.current_stream()
-        streams = [main] + self._side
-        for sd in self._side:
+        side = self._side[:self.branches - 1]
+        streams = [main] + side
+        for sd in side:
             sd.wait_stream(main)
         for c, c0 in enumerate(range(0, self.steps, k)):
             m = min(k, self.steps - c0)
@@ -610,7 +634,7 @@ class FrameLoop:
                       _lib.as_dptr(self._sx[c0:c0 + m]), _lib.as_dptr(self._sy[c0:c0 + m]), 0,
                       int(atm.margin_pix), int(atm.n), float(self._scale), dptr(self.out[c0:c0 + m]),
                       dptr(self._work[b]), spec.grid.work_bytes, streams[b].cuda_stream)
-        for sd in self._side:
+        for sd in side:
             main.wait_stream(sd)
 
     def render(self, t0: float):

@@ -40,6 +40,7 @@ struct pt_grid {
   double* sh_freq;  // (P, 3)
   double* beta;     // (P, 3, 2) grid mean of each basis row
   int sym;          // every level's frequencies are {-a, 0, +a}
+  int cols_variant; // power-of-two column pass: 0 register-fed, 1 TMA-fed
 };
 
 namespace pt {
@@ -970,17 +971,18 @@ static int pair_cols_tma_t(const pt_grid* g, const float2* work, int npair, int 
 // The TMA-fed column pass is selected with PYTURB_GB300_COLS=tma (N = 256, 512,
 // 1024). Measured on the GB300 it trails the one-CTA-per-tile register pass,
 // whose 2048 short CTAs keep more loads in flight, so the latter is the default.
-static bool cols_tma_selected() {
-  static const bool on = [] {
-    const char* v = std::getenv("PYTURB_GB300_COLS");
-    return v && std::string(v) == "tma";
+// default column-pass variant of new grids (PYTURB_GB300_COLS=tma selects TMA)
+static int default_cols_variant() {
+  static const int v = [] {
+    const char* e = std::getenv("PYTURB_GB300_COLS");
+    return (e && std::string(e) == "tma") ? 1 : 0;
   }();
-  return on;
+  return v;
 }
 
 static int pair_cols_reg(const pt_grid* g, const float2* work, int npair, int pair0,
                          const PairStore& st, cudaStream_t s) {
-  if (cols_tma_selected()) {
+  if (g->cols_variant == 1) {
     if (g->ns == 256) return pair_cols_tma_t<256>(g, work, npair, pair0, st, s);
     if (g->ns == 512) return pair_cols_tma_t<512>(g, work, npair, pair0, st, s);
     if (g->ns == 1024) return pair_cols_tma_t<1024>(g, work, npair, pair0, st, s);
@@ -1050,6 +1052,7 @@ extern "C" int pt_grid_create(pt_grid** out, int ns, double dx, int P, const dou
   g->ns = ns;
   g->dx = dx;
   g->P = P;
+  g->cols_variant = default_cols_variant();
   g->desc = make_fft_desc(ns);
   if (g->desc.nstages >= kMaxStages) {
     delete g;
@@ -1095,6 +1098,38 @@ extern "C" int pt_grid_create(pt_grid** out, int ns, double dx, int P, const dou
     return rc;
   }
   *out = g;
+  return PT_OK;
+}
+
+extern "C" int pt_grid_radices(const pt_grid* g, int* n_stages, int* radices) {
+  if (int rc = check_grid(g, "pt_grid_radices")) return rc;
+  if (!n_stages || !radices) return fail(PT_ERR_ARG, "pt_grid_radices: NULL pointer");
+  *n_stages = g->desc.nstages;
+  for (int i = 0; i < g->desc.nstages; ++i) radices[i] = g->desc.radix[i];
+  return PT_OK;
+}
+
+extern "C" int pt_grid_set_radices(pt_grid* g, int n_stages, const int* radices) {
+  if (int rc = check_grid(g, "pt_grid_set_radices")) return rc;
+  if (!radices || n_stages < 1 || n_stages >= kMaxStages)
+    return fail(PT_ERR_ARG, "pt_grid_set_radices: n_stages must be in [1, 23]");
+  long long prod = 1;
+  for (int i = 0; i < n_stages; ++i) {
+    if (radices[i] < 2) return fail(PT_ERR_ARG, "pt_grid_set_radices: every radix must be >= 2");
+    prod *= radices[i];
+    if (prod > g->ns) break;
+  }
+  if (prod != g->ns) return fail(PT_ERR_ARG, "pt_grid_set_radices: radices must multiply to ns");
+  g->desc.nstages = n_stages;
+  for (int i = 0; i < n_stages; ++i) g->desc.radix[i] = radices[i];
+  return PT_OK;
+}
+
+extern "C" int pt_grid_set_cols_variant(pt_grid* g, int variant) {
+  if (int rc = check_grid(g, "pt_grid_set_cols_variant")) return rc;
+  if (variant != 0 && variant != 1)
+    return fail(PT_ERR_ARG, "pt_grid_set_cols_variant: variant must be 0 (register) or 1 (TMA)");
+  g->cols_variant = variant;
   return PT_OK;
 }
 

@@ -212,6 +212,25 @@ class PhaseScreen:
                   int(crop), int(n_out), float(scale), int(bool(accumulate)), dptr(out),
                   dptr(self._grid.work), self._grid.work_bytes, stream_handle())
 
+    def autotune(self, count: int) -> dict:
+        """Tune this screen's transform schedule for batches of ``count``
+        (radix plan or column variant, cached on disk per device, size and
+        batch; results are unchanged beyond float32 rounding). The noise
+        stream is left where it was. Needs in-kernel noise."""
+        if self._rng.injected:
+            raise ValueError("autotune needs in-kernel noise (host_noise draws cannot be replayed)")
+        from .tuning import tune_grid
+
+        torch = torch_module()
+        count = int(count)
+        out = torch.empty((count, self.n, self.n), dtype=torch.float32, device=self._grid.device)
+        call = self._rng.call
+        try:
+            return tune_grid(self._grid, lambda: self._generate_into(out, count, 0, self.n, 1.0,
+                                                                     False), count)
+        finally:
+            self._rng.call = call
+
     def generate(self, count: Optional[int] = None):
         """``count`` independent screens ``(count, n, n)`` (or one ``(n, n)``)."""
         squeeze = count is None

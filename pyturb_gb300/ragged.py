@@ -48,11 +48,13 @@ class RaggedEnsemble:
     ``subharmonics`` levels of 3x3 low-order modes.
 
     :meth:`generate` draws a new ensemble (in-kernel Philox keyed by ``seed``,
-    a fresh counter per call) into :attr:`buffer`."""
+    a fresh counter per call) into :attr:`buffer`. ``autotune=True`` times
+    each group's radix plan or column variant once (cached on disk per
+    device, size and batch; see :mod:`pyturb_gb300.tuning`)."""
 
     def __init__(self, sizes: Sequence[int], r0, L0, pixel_scale=1.0 / 64,
                  subharmonics: int = 3, power_law: float = 11.0 / 3.0, seed=None,
-                 device: str = "gpu", streams: int = 4) -> None:
+                 device: str = "gpu", streams: int = 4, autotune: bool = False) -> None:
         torch = torch_module()
         check_device(device)
         sizes = np.asarray(sizes, dtype=np.int64).reshape(-1)
@@ -99,6 +101,22 @@ class RaggedEnsemble:
                              key=lambda k: -len(self.groups[k].members) * self.groups[k].n ** 2)
         self._rng = NoiseStream(seed, None)
         self._keys = [self._rng.next_key() for _ in self.groups]
+        self.tuning = {}
+        if autotune:  # per group: radix plan or column variant, cached per (n, batch)
+            from .tuning import tune_grid
+
+            for k, g in enumerate(self.groups):
+                self.tuning[(g.n, g.dx, g.L0)] = tune_grid(
+                    g.grid, lambda k=k: self._launch_group(k, 0, self._works[0],
+                                                           torch.cuda.current_stream()),
+                    len(g.members), workload="ragged")
+
+    def _launch_group(self, k: int, call: int, work, stream) -> None:
+        g, off, key = self.groups[k], self._group_off[k], self._keys[k]
+        _lib.call("pt_generate_scaled", g.grid.handle, len(g.members), dptr(g.amplitude),
+                  dptr(g.sh_amp), key, call, 0, g.n, 1.0, dptr(g.scale),
+                  self.buffer.data_ptr() + 4 * off, dptr(work), self.work_bytes,
+                  stream.cuda_stream)
 
     def generate(self):
         """Draw a new ensemble into :attr:`buffer` and return it (ordered on the
@@ -110,12 +128,8 @@ class RaggedEnsemble:
         for sd in self._side:
             sd.wait_stream(main)
         for slot, k in enumerate(self._order):
-            g, off, key = self.groups[k], self._group_off[k], self._keys[k]
             b = slot % self.n_streams
-            _lib.call("pt_generate_scaled", g.grid.handle, len(g.members), dptr(g.amplitude),
-                      dptr(g.sh_amp), key, call, 0, g.n, 1.0, dptr(g.scale),
-                      self.buffer.data_ptr() + 4 * off, dptr(self._works[b]), self.work_bytes,
-                      streams[b].cuda_stream)
+            self._launch_group(k, call, self._works[b], streams[b])
         for sd in self._side:
             main.wait_stream(sd)
         return self.buffer
