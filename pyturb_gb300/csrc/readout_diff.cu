@@ -303,11 +303,18 @@ k_lr_grad_screens(int L, int S, int T, int D, int n, int tiles, int ymax,
           }
           ry[p] = (int)(ya - ylo);
         }
-        // stage the pupil block
+        // stage the pupil block with asynchronous copies (all of a thread's
+        // loads in flight at once, one wait)
         for (int yy = warp; yy < ny; yy += 8) {
           const float* src = gi + (size_t)(ylo + yy) * n + xlo;
-          for (int xx = lane; xx < nx; xx += 32) gsm[yy * ymax + xx] = __ldg(src + xx);
+          for (int xx = lane; xx < nx; xx += 32) {
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(
+                             (uint32_t)__cvta_generic_to_shared(gsm + yy * ymax + xx)),
+                         "l"(src + xx)
+                         : "memory");
+          }
         }
+        asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
         __syncthreads();
         // column pass: h[yy][pc] = sum_k cwt[k] g[yy][cx0 + k]
         int ci[KM];
