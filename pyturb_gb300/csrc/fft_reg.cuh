@@ -140,19 +140,31 @@ __device__ __forceinline__ void reg_gather8(float2 (&x)[8], int j, const Lay& s)
   for (int i = 0; i < 8; ++i) x[i] = s[j + (N / 8) * i];
 }
 
-template <int N, int S, int Ns, class Lay>
+// Barrier policies of the exchanges: the whole CTA, or only the team that
+// owns the exchanged vector (a named barrier; the team is whole warps).
+struct CtaSync {
+  __device__ __forceinline__ void operator()() const { __syncthreads(); }
+};
+struct TeamSync {
+  int id, threads;  // barrier 1..15, thread count (a multiple of 32)
+  __device__ __forceinline__ void operator()() const {
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(threads) : "memory");
+  }
+};
+
+template <int N, int S, int Ns, class Lay, class Sync>
 struct RegStages {
   // run stages S.. ; x holds the inputs of stage S at positions j + T i
   static __device__ __forceinline__ void run(float2 (&x)[8], int j, const float2* tw,
-                                             const Lay& s) {
+                                             const Lay& s, const Sync& sync) {
     constexpr int R = Pow2Plan<N>::radix(S);
     reg_stage<N, R, Ns, S>(x, j, tw);
     if constexpr (S + 1 < Pow2Plan<N>::stages) {
       reg_scatter<N, R, Ns>(x, j, s);
-      __syncthreads();
+      sync();
       reg_gather8<N>(x, j, s);
-      __syncthreads();
-      RegStages<N, S + 1, Ns * R, Lay>::run(x, j, tw, s);
+      sync();
+      RegStages<N, S + 1, Ns * R, Lay, Sync>::run(x, j, tw, s, sync);
     }
   }
 };
@@ -160,12 +172,13 @@ struct RegStages {
 // Full transform of the thread's team. x in: element j + T i of the input;
 // x out: element j + T i of the output. `s` addresses this team's scratch
 // vector through its layout; tw is the shared per-stage twiddle table filled
-// by load_stage_tw<N>. Every thread of the CTA must call this (it
-// synchronises the CTA), and the caller must synchronise between its own
-// last read of `s` and this call.
-template <int N, class Lay>
-__device__ __forceinline__ void reg_fft(float2 (&x)[8], int j, const float2* tw, const Lay& s) {
-  RegStages<N, 0, 1, Lay>::run(x, j, tw, s);
+// by load_stage_tw<N>. Every thread the barrier policy covers must call this
+// (CtaSync: the whole CTA; TeamSync: the team), and the caller must
+// synchronise those threads between its own last read of `s` and this call.
+template <int N, class Lay, class Sync = CtaSync>
+__device__ __forceinline__ void reg_fft(float2 (&x)[8], int j, const float2* tw, const Lay& s,
+                                        const Sync& sync = Sync{}) {
+  RegStages<N, 0, 1, Lay, Sync>::run(x, j, tw, s, sync);
 }
 
 }  // namespace pt

@@ -366,9 +366,11 @@ k_frame_rows_uniform_reg(const float2* __restrict__ tw, const float2* __restrict
     const bool active = pv < np && (half == 0 || !self);
     float2 x[8];
     const RowLayout s{rows + v * fft_padded(N)};
+    // the team's own row from here on: team barriers, not CTA barriers
+    const TeamSync team{1 + v, T};
     if (active) reg_gather8<N>(x, j, s);
-    __syncthreads();
-    reg_fft<N>(x, j, stw, s);
+    team();
+    reg_fft<N>(x, j, stw, s, team);
     if (active) {
       const int pair = fbeg / 2 + pb + pv;
       const int row = half ? nkx : kx;
