@@ -130,6 +130,31 @@ __device__ __forceinline__ float2 philox_cnormal(uint64_t key, uint64_t idx, uin
   return box_muller(r.x, r.y);
 }
 
+// Both complex pairs of one Philox call: (x, y) -> lo, (z, w) -> hi. The screen
+// noise of a row of length N uses counter (row * H + ky mod H), H = ceil(N/2),
+// lo for ky < H and hi for ky >= H, so the elements ky and ky + H share a
+// call (the register FFT path owns both in one thread).
+__device__ __forceinline__ void philox_cnormal2(uint64_t key, uint64_t idx, uint64_t call,
+                                                uint32_t domain, float2& lo, float2& hi) {
+  u32x4 c;
+  c.x = (uint32_t)idx;
+  c.y = (uint32_t)(idx >> 32);
+  c.z = (uint32_t)call;
+  c.w = ((uint32_t)(call >> 32) & 0x00FFFFFFu) | (domain << 24);
+  const u32x4 r = philox4x32_10(c, key);
+  lo = box_muller(r.x, r.y);
+  hi = box_muller(r.z, r.w);
+}
+__device__ __forceinline__ float2 screen_normal(uint64_t key, uint64_t row, int ky, int N,
+                                                uint64_t call) {
+  const int H = (N + 1) / 2;
+  const bool upper = ky >= H;
+  float2 lo, hi;
+  philox_cnormal2(key, row * (uint64_t)H + (uint64_t)(upper ? ky - H : ky), call, kDomainScreen,
+                  lo, hi);
+  return upper ? hi : lo;
+}
+
 // ---------------------------------------------------------------- fixed point phase
 // Shift-theorem phases are formed as k * u (mod 1) with u = frac(s * df)
 // held as a 64-bit binary fraction, so the product wraps exactly and the

@@ -62,27 +62,35 @@ k_rows_reg(const float2* __restrict__ tw, const float2* __restrict__ in, int gen
   const int img = blockIdx.y;
   const bool ok = kx < N;
   float2 x[8];
+  if (ok && gen && !ga.noise) {
+    // one Philox call per element pair (ky, ky + N/2): elements i and i + 4
+    const uint64_t row = (uint64_t)(ga.img0 + img) * N + kx;
 #pragma unroll
-  for (int i = 0; i < 8; ++i) {
-    const int ky = j + T * i;
-    float2 val = make_float2(0.f, 0.f);
-    if (ok) {
-      if (gen) {
-        const size_t e = ((size_t)(ga.img0 + img) * N + kx) * N + ky;
-        float2 z;
-        if (ga.noise) {
-          const size_t plane = (size_t)ga.n_fft * N * N;
-          z = make_float2(ga.noise[e], ga.noise[plane + e]);
-        } else {
-          z = philox_cnormal(ga.seed, e, ga.call, kDomainScreen);
-        }
-        const float amp = ga.amplitude[(size_t)kx * N + ky];
-        val = make_float2(z.x * amp, z.y * amp);
-      } else {
-        val = in[((size_t)img * N + kx) * N + ky];
-      }
+    for (int i = 0; i < 4; ++i) {
+      float2 lo, hi;
+      philox_cnormal2(ga.seed, row * (N / 2) + j + T * i, ga.call, kDomainScreen, lo, hi);
+      const float a0 = ga.amplitude[(size_t)kx * N + j + T * i];
+      const float a1 = ga.amplitude[(size_t)kx * N + j + T * (i + 4)];
+      x[i] = make_float2(lo.x * a0, lo.y * a0);
+      x[i + 4] = make_float2(hi.x * a1, hi.y * a1);
     }
-    x[i] = val;
+  } else {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int ky = j + T * i;
+      float2 val = make_float2(0.f, 0.f);
+      if (ok) {
+        if (gen) {
+          const size_t e = ((size_t)(ga.img0 + img) * N + kx) * N + ky;
+          const size_t plane = (size_t)ga.n_fft * N * N;
+          const float amp = ga.amplitude[(size_t)kx * N + ky];
+          val = make_float2(ga.noise[e] * amp, ga.noise[plane + e] * amp);
+        } else {
+          val = in[((size_t)img * N + kx) * N + ky];
+        }
+      }
+      x[i] = val;
+    }
   }
   __syncthreads();  // twiddles loaded
   reg_fft<N>(x, j, stw, s);

@@ -135,7 +135,7 @@ k_rows(FftDesc d, const float2* __restrict__ tw, int rpc, const float2* __restri
           const size_t plane = (size_t)ga.n_fft * ns * ns;
           z = make_float2(ga.noise[e], ga.noise[plane + e]);
         } else {
-          z = philox_cnormal(ga.seed, e, ga.call, kDomainScreen);
+          z = screen_normal(ga.seed, (uint64_t)(ga.img0 + img) * ns + kx, ky, ns, ga.call);
         }
         const float amp = ga.amplitude[(size_t)kx * ns + ky];
         v = make_float2(z.x * amp, z.y * amp);
