@@ -56,6 +56,14 @@ static inline int image_chunk(int ns) {
   size_t c = (size_t)(64u << 20) / per;
   return (int)std::max<size_t>(1, std::min<size_t>(32, c));
 }
+// Transforms per chunk of generate / ifft2: up to 256 as long as the row-pass
+// intermediate of a chunk stays within 64 MB (L2-resident between the passes),
+// so small screens run as a few large launches.
+static inline int gen_chunk(int ns) {
+  size_t per = (size_t)ns * ns * sizeof(float2);
+  size_t c = (size_t)(64u << 20) / per;
+  return (int)std::max<size_t>(1, std::min<size_t>(256, c));
+}
 static inline int rows_per_cta(int ns) { return std::max(1, std::min(8, 1024 / ns)); }
 static inline int cols_per_cta(int ns) { return std::max(1, std::min(16, 4096 / ns)); }
 
@@ -78,7 +86,7 @@ struct SpecWork {
 };
 
 static SpecWork carve(const pt_grid* g, int L, void* base) {
-  const int ns = g->ns, ch = image_chunk(ns), P = std::max(1, g->P);
+  const int ns = g->ns, ch = image_chunk(ns), gch = gen_chunk(ns), P = std::max(1, g->P);
   const int F = 2 * ch;
   const int J = std::max(1, L);
   size_t off = 0;
@@ -89,9 +97,9 @@ static SpecWork carve(const pt_grid* g, int L, void* base) {
     off += align256(bytes);
     return p;
   };
-  w.img = (float2*)take((size_t)ch * ns * ns * sizeof(float2));
-  w.coef = (float2*)take((size_t)F * P * 9 * sizeof(float2));
-  w.mean = (float*)take((size_t)F * sizeof(float));
+  w.img = (float2*)take((size_t)std::max(ch, gch) * ns * ns * sizeof(float2));
+  w.coef = (float2*)take((size_t)2 * std::max(ch, gch) * P * 9 * sizeof(float2));
+  w.mean = (float*)take((size_t)2 * std::max(ch, gch) * sizeof(float));
   w.px = (float2*)take((size_t)F * J * ns * sizeof(float2));
   w.py = (float2*)take((size_t)F * J * ns * sizeof(float2));
   w.hn = (float2*)take((size_t)F * 2 * ns * sizeof(float2));
@@ -1159,7 +1167,7 @@ extern "C" int pt_ifft2(const pt_grid* g, const float* in, float* out, int batch
   SpecWork w = carve(g, 1, work);
   if (!work || work_bytes < w.bytes) return fail(PT_ERR_ARG, "pt_ifft2: workspace too small");
   cudaStream_t s = (cudaStream_t)stream;
-  const int ns = g->ns, ch = image_chunk(ns), rpc = rows_per_cta(ns), C = cols_per_cta(ns);
+  const int ns = g->ns, ch = gen_chunk(ns), rpc = rows_per_cta(ns), C = cols_per_cta(ns);
   const size_t rs = rows_smem(ns, rpc), cs = cols_smem(ns, C, 0);
   if (int rc = set_smem(k_rows, rs, "k_rows")) return rc;
   if (int rc = set_smem(k_plain_cols, cs, "k_plain_cols")) return rc;
@@ -1202,7 +1210,7 @@ static int generate_impl(const pt_grid* g, int count, const float* amplitude,
   if (!work || work_bytes < w.bytes) return fail(PT_ERR_ARG, "pt_generate: workspace too small");
   cudaStream_t s = (cudaStream_t)stream;
   const int n_fft = (count + 1) / 2;
-  const int ch = image_chunk(ns), rpc = rows_per_cta(ns), C = cols_per_cta(ns);
+  const int ch = gen_chunk(ns), rpc = rows_per_cta(ns), C = cols_per_cta(ns);
   const size_t rs = rows_smem(ns, rpc), cs = cols_smem(ns, C, P);
   if (int rc = set_smem(k_rows, rs, "k_rows")) return rc;
   if (int rc = set_smem(k_pair_cols, cs, "k_pair_cols")) return rc;

@@ -44,6 +44,25 @@ def test_generate_config1_shape_vs_oracle():
     assert cases.rel_l2(got2, o.generate(3)) < TOL
 
 
+@pytest.mark.parametrize("n,count", [(1024, 19), (64, 601)])
+def test_generate_chunk_boundaries_vs_oracle(n, count):
+    """Batches spanning several internal chunks (8 transforms per chunk at
+    1024^2, 256 at 64^2), odd counts so the last transform carries one screen."""
+    import oracle
+    import pyturb_gb300 as G
+    from pyturb_gb300.backend import to_numpy
+
+    kw = dict(n=n, pixel_scale=4.0 / n, r0=0.1, L0=20.0, subharmonics=2)
+    g = G.PhaseScreen(seed=9, host_noise=np.random.default_rng, **kw)
+    got = to_numpy(g.generate(count))
+    ref = oracle.OraclePhaseScreen(kw["n"], kw["pixel_scale"], kw["r0"], kw["L0"], 2,
+                                   rng=np.random.default_rng(9)).generate(count)
+    assert got.shape == (count, n, n)
+    assert cases.rel_l2(got, ref) < TOL
+    per = [cases.rel_l2(got[i], ref[i]) for i in (0, count // 2, count - 1)]
+    assert max(per) < 3 * TOL, per
+
+
 def _config2_layers(seed=0):
     rng = np.random.default_rng(seed)
     h = [0, 500, 1000, 2000, 4000, 8000, 12000, 16000, 20000]
