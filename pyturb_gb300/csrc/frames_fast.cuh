@@ -5,6 +5,10 @@
 // layers at once).
 #pragma once
 
+// Largest P * N (float2) of first basis rows the column kernels stage in
+// shared memory for the subharmonic epilogue.
+constexpr int kColBasisMax = 4096;
+
 template <int N>
 struct RegCfg {
   static constexpr int T = N / 8;
@@ -177,8 +181,11 @@ k_pair_cols_reg(const float2* __restrict__ tw, const float2* __restrict__ work, 
   __syncthreads();
   // per-column symmetric-basis constants: K (this thread's registers) and,
   // per level, (U_re, W_re, U_im, W_im) in a shared float4 table read once per
-  // output element (the FFT's own barriers order these writes before use)
+  // output element; the first basis row of each level is staged in shared
+  // memory too when it fits (kColBasisMax float2)
   float4* utab = (float4*)(mtab + 2 * 3 * P * C);
+  float2* sbasis = mtab + 8 * (P > 0 ? P : 1) * C;
+  const bool sb = st.sym && P * N <= kColBasisMax;
   float k0 = 0.f, k1 = 0.f;
   if (st.sym) {
     for (int p = 0; p < P; ++p) {
@@ -193,7 +200,11 @@ k_pair_cols_reg(const float2* __restrict__ tw, const float2* __restrict__ work, 
       const float2 m10 = mtab[(1 * 3 * P + 3 * p) * C + cc], m12 = mtab[(1 * 3 * P + 3 * p + 2) * C + cc];
       utab[i] = make_float4(m00.x + m02.x, m02.y - m00.y, m10.x + m12.x, m12.y - m10.y);
     }
+    if (sb)
+      for (int i = threadIdx.x; i < P * N; i += blockDim.x)
+        sbasis[i] = __ldg(st.basis + (size_t)(3 * (i / N)) * N + (i % N));
   }
+  __syncthreads();
   reg_fft<N>(x, j, stw, s);
   if (!ok) return;
   const size_t plane = (size_t)st.n_out * st.n_out;
@@ -212,7 +223,7 @@ k_pair_cols_reg(const float2* __restrict__ tw, const float2* __restrict__ work, 
       lre = k0;
       lim = k1;
       for (int p = 0; p < P; ++p) {
-        const float2 b = __ldg(st.basis + (size_t)(3 * p) * N + xr);
+        const float2 b = sb ? sbasis[p * N + xr] : __ldg(st.basis + (size_t)(3 * p) * N + xr);
         const float4 u = utab[p * C + c];
         lre = fmaf(b.x, u.x, fmaf(b.y, u.y, lre));
         lim = fmaf(b.x, u.z, fmaf(b.y, u.w, lim));

@@ -923,8 +923,10 @@ template <int N>
 static int pair_cols_reg_t(const pt_grid* g, const float2* work, int npair, int pair0,
                            const PairStore& st, cudaStream_t s) {
   using Cfg = RegCfg<N>;
-  const size_t smem =
-      (size_t)(N + Cfg::C * N + (2 * 3 + 2) * std::max(g->P, 1) * Cfg::C) * sizeof(float2);
+  const int P = g->P;
+  const size_t smem = (size_t)(N + Cfg::C * N + (2 * 3 + 2) * std::max(P, 1) * Cfg::C +
+                               (P * N <= kColBasisMax ? P * N : 0)) *
+                      sizeof(float2);
   if (int rc = set_smem(k_pair_cols_reg<N>, smem, "k_pair_cols_reg")) return rc;
   ProfScope ps("k_pair_cols", s);
   k_pair_cols_reg<N><<<dim3((N + Cfg::C - 1) / Cfg::C, npair), Cfg::THREADS, smem, s>>>(
