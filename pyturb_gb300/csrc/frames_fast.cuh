@@ -282,10 +282,18 @@ k_frame_rows_uniform_reg(const float2* __restrict__ tw, const float2* __restrict
   extern __shared__ float2 sm[];
   float2* stw = sm;
   float2* rows = sm + N;  // NV * fft_padded(N)
+  // exact Hermitian parts at (kx, N/2) of this anchor block's frames, read
+  // once here instead of by one thread inside the pair loop (which stalled
+  // every batch's barrier on a global load)
+  __shared__ float2 hcol[kAnchor];
   load_stage_tw<N>(stw, tw);
   const int kx = blockIdx.x;
   const int fbeg = blockIdx.y * kAnchor;
   const int nkx = (N - kx) & (N - 1);
+  const int nfr = min(kAnchor, F - fbeg);
+  // row N/2 is the Nyquist row: every element comes from hn, no recurrence
+  const bool nyq_row = kx == N / 2;
+  if (threadIdx.x < nfr) hcol[threadIdx.x] = hn[(size_t)(fbeg + threadIdx.x) * 2 * N + N + kx];
   // packed state: lanes (layer 2q, layer 2q+1). With one column per thread
   // -Ry is kept beside Ry so the complex step needs no separate negation
   // (two columns per thread would spill it).
@@ -326,14 +334,44 @@ k_frame_rows_uniform_reg(const float2* __restrict__ tw, const float2* __restrict
   // Hermitian symmetry H(-k) = conj H(k): this CTA synthesises row kx only and
   // also emits the mirrored row N - kx (columns reversed), so the recurrence
   // runs on half of the spectrum. Rows 0 and N/2 are their own mirrors.
-  const bool self = (kx == 0) || (kx == N / 2);
+  const bool self = (kx == 0) || nyq_row;
   constexpr int PB = NV / 2;  // frame pairs per transform batch (two rows each)
-  const int nfr = min(kAnchor, F - fbeg);
   const int npairs = (nfr + 1) / 2;
   const int v = threadIdx.x / T, j = threadIdx.x % T;
+  __syncthreads();  // hcol
   for (int pb = 0; pb < npairs; pb += PB) {
     const int np = min(PB, npairs - pb);
-    for (int p = 0; p < np; ++p) {
+    if (nyq_row) {
+      // loads of PH pairs in flight together, then their stores
+      constexpr int PH = E == 1 ? PB : 1;
+      for (int p0 = 0; p0 < np; p0 += PH) {
+        float2 hv[PH][2][E];
+#pragma unroll
+        for (int q = 0; q < PH; ++q) {
+          const int p = p0 + q;
+          const int fa = fbeg + 2 * (pb + p);
+#pragma unroll
+          for (int e = 0; e < E; ++e) {
+            const int ky = threadIdx.x + e * THREADS;
+            hv[q][0][e] = p < np ? hn[(size_t)fa * 2 * N + ky] : make_float2(0.f, 0.f);
+            hv[q][1][e] = p < np && fa + 1 < fbeg + nfr ? hn[(size_t)(fa + 1) * 2 * N + ky]
+                                                        : make_float2(0.f, 0.f);
+          }
+        }
+#pragma unroll
+        for (int q = 0; q < PH; ++q) {
+          const int p = p0 + q;
+          if (p >= np) break;
+#pragma unroll
+          for (int e = 0; e < E; ++e) {
+            const int ky = threadIdx.x + e * THREADS;
+            const RowLayout ra{rows + (2 * p) * fft_padded(N)};
+            ra[ky] = make_float2(hv[q][0][e].x - hv[q][1][e].y, hv[q][0][e].y + hv[q][1][e].x);
+          }
+        }
+      }
+    }
+    for (int p = 0; p < (nyq_row ? 0 : np); ++p) {
       const bool two = 2 * (pb + p) + 1 < nfr;
 #pragma unroll
       for (int e = 0; e < E; ++e) {
@@ -365,11 +403,9 @@ k_frame_rows_uniform_reg(const float2* __restrict__ tw, const float2* __restrict
           h[fr] = make_float2(a0 + a1, b0 + b1);
         }
         const int ky = threadIdx.x + e * THREADS;
-        if (kx == N / 2 || ky == N / 2) {
-          const int el = kx == N / 2 ? ky : N + kx;
-          const int fa = fbeg + 2 * (pb + p);
-          h[0] = hn[(size_t)fa * 2 * N + el];
-          h[1] = two ? hn[(size_t)(fa + 1) * 2 * N + el] : make_float2(0.f, 0.f);
+        if (ky == N / 2) {
+          h[0] = hcol[2 * (pb + p)];
+          h[1] = two ? hcol[2 * (pb + p) + 1] : make_float2(0.f, 0.f);
         }
         const RowLayout ra{rows + (2 * p) * fft_padded(N)};
         ra[ky] = make_float2(h[0].x - h[1].y, h[0].y + h[1].x);
