@@ -169,6 +169,26 @@ struct RegStages {
   }
 };
 
+// As RegStages, with the exchanges alternating between two scratch vectors a
+// and b: stage s scatters into one and gathers from it after one barrier; the
+// next stage scatters into the other, so every thread has passed this stage's
+// gather (the next barrier) before the vector is written again. One barrier
+// per exchange instead of two.
+template <int N, int S, int Ns, class Lay, class Sync>
+struct RegStages2 {
+  static __device__ __forceinline__ void run(float2 (&x)[8], int j, const float2* tw,
+                                             const Lay& a, const Lay& b, const Sync& sync) {
+    constexpr int R = Pow2Plan<N>::radix(S);
+    reg_stage<N, R, Ns, S>(x, j, tw);
+    if constexpr (S + 1 < Pow2Plan<N>::stages) {
+      reg_scatter<N, R, Ns>(x, j, a);
+      sync();
+      reg_gather8<N>(x, j, a);
+      RegStages2<N, S + 1, Ns * R, Lay, Sync>::run(x, j, tw, b, a, sync);
+    }
+  }
+};
+
 // Full transform of the thread's team. x in: element j + T i of the input;
 // x out: element j + T i of the output. `s` addresses this team's scratch
 // vector through its layout; tw is the shared per-stage twiddle table filled
@@ -179,6 +199,16 @@ template <int N, class Lay, class Sync = CtaSync>
 __device__ __forceinline__ void reg_fft(float2 (&x)[8], int j, const float2* tw, const Lay& s,
                                         const Sync& sync = Sync{}) {
   RegStages<N, 0, 1, Lay, Sync>::run(x, j, tw, s, sync);
+}
+
+// The same transform on two scratch vectors (first exchange in a). The caller
+// must synchronise the barrier's threads between its own last access of `a`
+// and this call; its last access of `b` only has to precede the call (the
+// first exchange's barrier orders it before b is written).
+template <int N, class Lay, class Sync = CtaSync>
+__device__ __forceinline__ void reg_fft_db(float2 (&x)[8], int j, const float2* tw, const Lay& a,
+                                           const Lay& b, const Sync& sync = Sync{}) {
+  RegStages2<N, 0, 1, Lay, Sync>::run(x, j, tw, a, b, sync);
 }
 
 }  // namespace pt

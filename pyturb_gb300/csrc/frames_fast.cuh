@@ -61,6 +61,7 @@ k_rows_reg(const float2* __restrict__ tw, const float2* __restrict__ in, int gen
   float2* stw = sm;
   const int v = threadIdx.x / T, j = threadIdx.x % T;
   const RowLayout s{sm + N + v * fft_padded(N)};
+  const RowLayout s2{sm + N + (NV + v) * fft_padded(N)};  // second exchange vector
   load_stage_tw<N>(stw, tw);
   const int kx = blockIdx.x * NV + v;
   const int img = blockIdx.y;
@@ -97,7 +98,7 @@ k_rows_reg(const float2* __restrict__ tw, const float2* __restrict__ in, int gen
     }
   }
   __syncthreads();  // twiddles loaded
-  reg_fft<N>(x, j, stw, s);
+  reg_fft_db<N>(x, j, stw, s, s2);
   if (ok) {
 #pragma unroll
     for (int i = 0; i < 8; ++i) work[((size_t)img * N + kx) * N + j + T * i] = x[i];
@@ -114,6 +115,7 @@ k_plain_cols_reg(const float2* __restrict__ tw, const float2* __restrict__ work,
   float2* stw = sm;
   const int c = threadIdx.x % C, j = threadIdx.x / C;
   const ColLayout<C> s{sm + N + c};
+  const ColLayout<C> s2{sm + N + N * C + c};  // second exchange buffer
   load_stage_tw<N>(stw, tw);
   const int y = blockIdx.x * C + c;
   const int img = blockIdx.y;
@@ -123,7 +125,7 @@ k_plain_cols_reg(const float2* __restrict__ tw, const float2* __restrict__ work,
   for (int i = 0; i < 8; ++i)
     x[i] = ok ? work[((size_t)img * N + j + T * i) * N + y] : make_float2(0.f, 0.f);
   __syncthreads();
-  reg_fft<N>(x, j, stw, s);
+  reg_fft_db<N>(x, j, stw, s, s2);
   if (ok) {
 #pragma unroll
     for (int i = 0; i < 8; ++i) out[((size_t)img * N + j + T * i) * N + y] = x[i];
@@ -143,10 +145,11 @@ k_pair_cols_reg(const float2* __restrict__ tw, const float2* __restrict__ work, 
   constexpr int T = RegCfg<N>::T, C = RegCfg<N>::C;
   extern __shared__ float2 sm[];
   float2* stw = sm;
-  float2* buf = sm + N;             // N * C, column-interleaved
-  float2* mtab = buf + N * C;       // (2, 3P, C) or (2, P, C) (U, W) + (2, C) (K, 0)
+  float2* buf = sm + N;             // 2 x N * C, column-interleaved exchange buffers
+  float2* mtab = buf + 2 * N * C;   // (2, 3P, C) or (2, P, C) (U, W) + (2, C) (K, 0)
   const int c = threadIdx.x % C, j = threadIdx.x / C;
   const ColLayout<C> s{buf + c};
+  const ColLayout<C> s2{buf + N * C + c};
   load_stage_tw<N>(stw, tw);
   const int y = blockIdx.x * C + c;
   const int pl = blockIdx.y;
@@ -205,7 +208,7 @@ k_pair_cols_reg(const float2* __restrict__ tw, const float2* __restrict__ work, 
         sbasis[i] = __ldg(st.basis + (size_t)(3 * (i / N)) * N + (i % N));
   }
   __syncthreads();
-  reg_fft<N>(x, j, stw, s);
+  reg_fft_db<N>(x, j, stw, s, s2);
   if (!ok) return;
   const size_t plane = (size_t)st.n_out * st.n_out;
   const int yo = y - st.crop;
@@ -281,7 +284,7 @@ k_frame_rows_uniform_reg(const float2* __restrict__ tw, const float2* __restrict
   constexpr int LP = (LM + 1) / 2;  // packed layer pairs
   extern __shared__ float2 sm[];
   float2* stw = sm;
-  float2* rows = sm + N;  // NV * fft_padded(N)
+  float2* rows = sm + N;  // NV * fft_padded(N), then NV exchange vectors
   // exact Hermitian parts at (kx, N/2) of this anchor block's frames, read
   // once here instead of by one thread inside the pair loop (which stalled
   // every batch's barrier on a global load)
@@ -421,11 +424,13 @@ k_frame_rows_uniform_reg(const float2* __restrict__ tw, const float2* __restrict
     const bool active = pv < np && (half == 0 || !self);
     float2 x[8];
     const RowLayout s{rows + v * fft_padded(N)};
-    // the team's own row from here on: team barriers, not CTA barriers
+    const RowLayout s2{rows + (NV + v) * fft_padded(N)};
+    // the team's own row from here on: team barriers, not CTA barriers. The
+    // first exchange goes to s2 (last read before this batch's first barrier),
+    // so the gather from s needs no barrier of its own.
     const TeamSync team{1 + v, T};
     if (active) reg_gather8<N>(x, j, s);
-    team();
-    reg_fft<N>(x, j, stw, s, team);
+    reg_fft_db<N>(x, j, stw, s2, s, team);
     if (active) {
       const int pair = fbeg / 2 + pb + pv;
       const int row = half ? nkx : kx;

@@ -802,7 +802,7 @@ static int uniform_reg_rows_t(const pt_grid* g, const float2* spectra, int L, in
   const int ns = g->ns;
   const dim3 pgrid(ns / 2 + 1, (nf + kAnchor - 1) / kAnchor);  // row pairs {kx, ns - kx}
   auto go = [&](auto kern, int threads, int nv) -> int {
-    const size_t smem = (size_t)(ns + nv * fft_padded(ns)) * sizeof(float2);
+    const size_t smem = (size_t)(ns + 2 * nv * fft_padded(ns)) * sizeof(float2);
     if (int rc = set_smem(kern, smem, "k_frame_rows_uniform_reg")) return rc;
     ProfScope ps("k_frame_rows_uniform", s);
     kern<<<pgrid, threads, smem, s>>>(g->tw, spectra, L, nf, ut, hn, img);
@@ -877,7 +877,7 @@ template <int N>
 static int rows_reg_t(const pt_grid* g, const float2* in, int gen, const GenRowArgs& ga, int nimg,
                       float2* work, cudaStream_t s) {
   using Cfg = RegCfg<N>;
-  const size_t smem = (size_t)(N + Cfg::NV * fft_padded(N)) * sizeof(float2);
+  const size_t smem = (size_t)(N + 2 * Cfg::NV * fft_padded(N)) * sizeof(float2);
   if (int rc = set_smem(k_rows_reg<N>, smem, "k_rows_reg")) return rc;
   ProfScope ps("k_rows", s);
   k_rows_reg<N><<<dim3((N + Cfg::NV - 1) / Cfg::NV, nimg), Cfg::THREADS, smem, s>>>(g->tw, in, gen,
@@ -900,7 +900,7 @@ template <int N>
 static int plain_cols_reg_t(const pt_grid* g, const float2* work, int nimg, float2* out,
                             cudaStream_t s) {
   using Cfg = RegCfg<N>;
-  const size_t smem = (size_t)(N + Cfg::C * N) * sizeof(float2);
+  const size_t smem = (size_t)(N + 2 * Cfg::C * N) * sizeof(float2);
   if (int rc = set_smem(k_plain_cols_reg<N>, smem, "k_plain_cols_reg")) return rc;
   ProfScope ps("k_plain_cols", s);
   k_plain_cols_reg<N><<<dim3((N + Cfg::C - 1) / Cfg::C, nimg), Cfg::THREADS, smem, s>>>(g->tw, work,
@@ -924,7 +924,7 @@ static int pair_cols_reg_t(const pt_grid* g, const float2* work, int npair, int 
                            const PairStore& st, cudaStream_t s) {
   using Cfg = RegCfg<N>;
   const int P = g->P;
-  const size_t smem = (size_t)(N + Cfg::C * N + (2 * 3 + 2) * std::max(P, 1) * Cfg::C +
+  const size_t smem = (size_t)(N + 2 * Cfg::C * N + (2 * 3 + 2) * std::max(P, 1) * Cfg::C +
                                (P * N <= kColBasisMax ? P * N : 0)) *
                       sizeof(float2);
   if (int rc = set_smem(k_pair_cols_reg<N>, smem, "k_pair_cols_reg")) return rc;
