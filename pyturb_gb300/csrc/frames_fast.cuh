@@ -210,48 +210,72 @@ k_pair_cols_reg(const float2* __restrict__ tw, const float2* __restrict__ work, 
   __syncthreads();
   reg_fft_db<N>(x, j, stw, s, s2);
   if (!ok) return;
-  const size_t plane = (size_t)st.n_out * st.n_out;
   const int yo = y - st.crop;
   if (yo < 0 || yo >= st.n_out) return;
-  const float mre = (P > 0 && do_re) ? st.mean[row_re] : 0.f;
-  const float mim = (P > 0 && do_im) ? st.mean[row_im] : 0.f;
-  const float sre = img_scale_of(st, img_re), sim = img_scale_of(st, img_im);
+  // the low-order screens of this column, level by level into the
+  // transform's registers (x[i].x: screen img_re, x[i].y: screen img_im)
+  if (st.sym) {
 #pragma unroll
-  for (int i = 0; i < 8; ++i) {
-    const int xr = j + T * i;
-    const int xo = xr - st.crop;
-    if (xo < 0 || xo >= st.n_out) continue;
-    float lre, lim;
-    if (st.sym) {
-      lre = k0;
-      lim = k1;
+    for (int i = 0; i < 8; ++i) {
+      x[i].x += k0;
+      x[i].y += k1;
+    }
+    if (sb) {
       for (int p = 0; p < P; ++p) {
-        const float2 b = sb ? sbasis[p * N + xr] : __ldg(st.basis + (size_t)(3 * p) * N + xr);
         const float4 u = utab[p * C + c];
-        lre = fmaf(b.x, u.x, fmaf(b.y, u.y, lre));
-        lim = fmaf(b.x, u.z, fmaf(b.y, u.w, lim));
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+          const float2 b = sbasis[p * N + j + T * i];
+          x[i].x = fmaf(b.x, u.x, fmaf(b.y, u.y, x[i].x));
+          x[i].y = fmaf(b.x, u.z, fmaf(b.y, u.w, x[i].y));
+        }
       }
     } else {
-      lre = -mre;
-      lim = -mim;
-      for (int pi = 0; pi < 3 * P; ++pi) {
-        const float2 b = st.basis[(size_t)pi * N + xr];
-        const float2 m0 = mtab[(0 * 3 * P + pi) * C + c];
-        const float2 m1 = mtab[(1 * 3 * P + pi) * C + c];
-        lre = fmaf(b.x, m0.x, fmaf(-b.y, m0.y, lre));
-        lim = fmaf(b.x, m1.x, fmaf(-b.y, m1.y, lim));
+      for (int p = 0; p < P; ++p) {
+        const float4 u = utab[p * C + c];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+          const float2 b = __ldg(st.basis + (size_t)(3 * p) * N + j + T * i);
+          x[i].x = fmaf(b.x, u.x, fmaf(b.y, u.y, x[i].x));
+          x[i].y = fmaf(b.x, u.z, fmaf(b.y, u.w, x[i].y));
+        }
       }
     }
-    const size_t o = (size_t)xo * st.n_out + yo;
-    if (do_re) {
-      const float val = sre * (x[i].x + lre);
-      float* dst = st.out + (size_t)img_re * plane + o;
-      *dst = st.accumulate ? *dst + val : val;
+  } else {
+    const float mre = (P > 0 && do_re) ? st.mean[row_re] : 0.f;
+    const float mim = (P > 0 && do_im) ? st.mean[row_im] : 0.f;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      x[i].x -= mre;
+      x[i].y -= mim;
     }
-    if (do_im) {
-      const float val = sim * (x[i].y + lim);
-      float* dst = st.out + (size_t)img_im * plane + o;
-      *dst = st.accumulate ? *dst + val : val;
+    for (int pi = 0; pi < 3 * P; ++pi) {
+      const float2 m0 = mtab[(0 * 3 * P + pi) * C + c];
+      const float2 m1 = mtab[(1 * 3 * P + pi) * C + c];
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        const float2 b = st.basis[(size_t)pi * N + j + T * i];
+        x[i].x = fmaf(b.x, m0.x, fmaf(-b.y, m0.y, x[i].x));
+        x[i].y = fmaf(b.x, m1.x, fmaf(-b.y, m1.y, x[i].y));
+      }
+    }
+  }
+  const size_t plane = (size_t)st.n_out * st.n_out;
+  const float sre = img_scale_of(st, img_re), sim = img_scale_of(st, img_im);
+  float* ore = st.out + (size_t)(do_re ? img_re : 0) * plane + yo;
+  float* oim = st.out + (size_t)(do_im ? img_im : 0) * plane + yo;
+  const bool full = st.crop == 0 && st.n_out == N;  // every row of the column is kept
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const int xo = j + T * i - st.crop;
+    if (!full && (xo < 0 || xo >= st.n_out)) continue;
+    const size_t o = (size_t)xo * st.n_out;
+    if (st.accumulate) {
+      if (do_re) ore[o] += sre * x[i].x;
+      if (do_im) oim[o] += sim * x[i].y;
+    } else {
+      if (do_re) ore[o] = sre * x[i].x;
+      if (do_im) oim[o] = sim * x[i].y;
     }
   }
 }
