@@ -97,14 +97,24 @@ __device__ __forceinline__ u32x4 philox4x32_10(u32x4 c, uint64_t key) {
 }
 
 // Two independent N(0,1) draws from two 32-bit uniforms (Box-Muller).
-// u1 is mapped to (0, 1] so the logarithm is finite.
+// u1 is mapped to (0, 1] so the logarithm is finite. The radius and angle use
+// the hardware approximations (log2, sqrt, sin/cos on [-pi, pi)): absolute
+// errors near 1e-6, far below the statistical scatter of the draws, at a
+// fraction of the instructions of the correctly rounded functions.
+__device__ __forceinline__ float sqrt_approx(float x) {
+  float r;
+  asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
 __device__ __forceinline__ float2 box_muller(uint32_t a, uint32_t b) {
-  float u1 = ((float)(a >> 8) + 1.0f) * (1.0f / 16777216.0f);
-  float u2 = (float)(b >> 8) * (1.0f / 16777216.0f);
-  float r = sqrtf(-2.0f * logf(u1));
+  const float u1 = ((float)(a >> 8) + 1.0f) * (1.0f / 16777216.0f);
+  const float u2 = (float)(b >> 8) * (1.0f / 16777216.0f) - 0.5f;  // [-0.5, 0.5)
+  // -2 ln u1 = -2 ln 2 log2 u1 >= 0
+  const float r = sqrt_approx(-1.3862943611198906f * __log2f(u1));
   float s, c;
-  sincospif(2.0f * u2, &s, &c);
-  return make_float2(r * c, r * s);
+  __sincosf(6.283185307179586f * u2, &s, &c);
+  // angle 2 pi u2 - pi: negate to keep the orientation of 2 pi (u2 + 0.5)
+  return make_float2(-r * c, -r * s);
 }
 
 // Noise domains keep the streams of different consumers disjoint.
