@@ -36,6 +36,10 @@ constexpr int kTM = 64;   // output rows per CTA
 constexpr int kTJ = 32;   // jobs (columns) per CTA
 constexpr int kTK = 32;   // K step
 constexpr int kMaxSplit = 16;
+// register-tiled extrusion GEMM: 128 rows x 16 TJ jobs per CTA, K steps of 16
+constexpr int kGBM = 128;
+constexpr int kGBK = 16;
+constexpr int kMaxSplitTiled = 32;
 
 struct GatherJob {
   int screen, head;
@@ -180,6 +184,92 @@ k_extrude_gemm(int W, int K, int J, int kslice, const float* __restrict__ M,
     }
 }
 
+// The same partial products for the extrusion shapes (W ~ 10^3 rows, tens to
+// hundreds of jobs, K = (m+1) W): 256 threads as 16 row lanes x 16 job lanes,
+// thread (tm, tj) accumulating rows {4 tm + u, 64 + 4 tm + u} (u < 4) x jobs
+// tj TJ + v (v < TJ) in registers: per K value two 128-bit shared loads of A
+// and TJ broadcast loads of X feed 8 TJ FMAs. Both operands are row-major with
+// an odd K (no 16-byte alignment), so each stage is read with coalesced
+// scalar loads into registers while the previous stage is multiplied, then
+// stored K-major into the other shared buffer.
+template <int TJ>
+__global__ void __launch_bounds__(256, 2)
+k_extrude_gemm_tiled(int W, int K, int J, int kslice, const float* __restrict__ M,
+                     const float* __restrict__ X, float* __restrict__ partial) {
+  constexpr int BJ = 16 * TJ;
+  constexpr int AP = kGBM + 4;  // padded K-major rows (16-byte aligned)
+  constexpr int XP = BJ + 4;
+  __shared__ __align__(16) float sA[2][kGBK][AP];
+  __shared__ __align__(16) float sX[2][kGBK][XP];
+  const int tid = threadIdx.x;
+  const int tm = tid & 15, tj = tid >> 4;
+  const int r0 = blockIdx.x * kGBM, j0 = blockIdx.y * BJ;
+  const int kb = blockIdx.z * kslice, ke = min(K, kb + kslice);
+  // staging map: K offset lk, rows / jobs lr + 16 i
+  const int lk = tid & 15, lr = tid >> 4;
+  float ra[8], rx[TJ];
+  auto load = [&](int k0) {
+    const int k = k0 + lk;
+    const bool kin = k < ke;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int r = r0 + lr + 16 * i;
+      ra[i] = (kin && r < W) ? __ldg(M + (size_t)r * K + k) : 0.f;
+    }
+#pragma unroll
+    for (int v = 0; v < TJ; ++v) {
+      const int j = j0 + lr + 16 * v;
+      rx[v] = (kin && j < J) ? __ldg(X + (size_t)j * K + k) : 0.f;
+    }
+  };
+  auto store = [&](int b) {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) sA[b][lk][lr + 16 * i] = ra[i];
+#pragma unroll
+    for (int v = 0; v < TJ; ++v) sX[b][lk][lr + 16 * v] = rx[v];
+  };
+  float acc[8][TJ];
+#pragma unroll
+  for (int u = 0; u < 8; ++u)
+#pragma unroll
+    for (int v = 0; v < TJ; ++v) acc[u][v] = 0.f;
+  load(kb);
+  store(0);
+  __syncthreads();
+  int b = 0;
+  for (int k0 = kb; k0 < ke; k0 += kGBK) {
+    const bool more = k0 + kGBK < ke;
+    if (more) load(k0 + kGBK);
+#pragma unroll
+    for (int kk = 0; kk < kGBK; ++kk) {
+      const float4 a0 = *(const float4*)&sA[b][kk][tm * 4];
+      const float4 a1 = *(const float4*)&sA[b][kk][64 + tm * 4];
+      const float a[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+      float x[TJ];
+#pragma unroll
+      for (int v = 0; v < TJ; ++v) x[v] = sX[b][kk][tj * TJ + v];
+#pragma unroll
+      for (int u = 0; u < 8; ++u)
+#pragma unroll
+        for (int v = 0; v < TJ; ++v) acc[u][v] = fmaf(a[u], x[v], acc[u][v]);
+    }
+    // the other buffer was last read before the previous barrier
+    if (more) store(b ^ 1);
+    __syncthreads();
+    b ^= 1;
+  }
+  float* pz = partial + (size_t)blockIdx.z * J * W;
+#pragma unroll
+  for (int u = 0; u < 8; ++u) {
+    const int r = r0 + (u < 4 ? 4 * tm + u : 64 + 4 * tm + (u - 4));
+#pragma unroll
+    for (int v = 0; v < TJ; ++v) {
+      const int j = j0 + tj * TJ + v;
+      if (r < W && j < J) pz[(size_t)j * W + r] = acc[u][v];
+    }
+  }
+}
+
 __global__ void k_extrude_reduce(int W, int J, int cap, int nsplit, const float* __restrict__ partial,
                                  const JobParams jobs, float* __restrict__ buf) {
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
@@ -311,6 +401,29 @@ int tc_prepare_launch(int W, int m, int G, const float* M, int terms, void* tile
 int tc_gemm_launch(int W, int m, int J, int terms, const uint8_t* At, const uint8_t* Bt,
                    float* partial, int* nz_out, cudaStream_t s);
 
+// Jobs per thread of the tiled GEMM and its split-K: about two CTAs per SM,
+// each slice at least 8 K steps long.
+static int tiled_tj(int J) { return J <= 32 ? 2 : (J <= 64 ? 4 : 9); }
+static int tiled_split(int W, int J, int K) {
+  const int bj = 16 * tiled_tj(J);
+  const int ctas = ((W + kGBM - 1) / kGBM) * ((J + bj - 1) / bj);
+  int s = std::max(1, std::min(kMaxSplitTiled, (2 * 152 + ctas - 1) / ctas));
+  return std::max(1, std::min(s, K / (8 * kGBK)));
+}
+static void launch_gemm_tiled(int W, int K, int J, const float* M, const float* X, float* partial,
+                              int* nz_out, cudaStream_t s) {
+  const int tj = tiled_tj(J), bj = 16 * tj;
+  const int nsplit = tiled_split(W, J, K);
+  const int kslice = ((K + nsplit - 1) / nsplit + kGBK - 1) / kGBK * kGBK;
+  const int nz = (K + kslice - 1) / kslice;
+  const dim3 grid((W + kGBM - 1) / kGBM, (J + bj - 1) / bj, nz);
+  ProfScope ps("k_extrude_gemm", s);
+  if (tj == 2) k_extrude_gemm_tiled<2><<<grid, 256, 0, s>>>(W, K, J, kslice, M, X, partial);
+  else if (tj == 4) k_extrude_gemm_tiled<4><<<grid, 256, 0, s>>>(W, K, J, kslice, M, X, partial);
+  else k_extrude_gemm_tiled<9><<<grid, 256, 0, s>>>(W, K, J, kslice, M, X, partial);
+  *nz_out = nz;
+}
+
 static int split_for(int W, int J, int K) {
   const int ctas = ((W + kTM - 1) / kTM) * ((J + kTJ - 1) / kTJ);
   int s = std::max(1, std::min(kMaxSplit, (2 * 152 + ctas - 1) / ctas));
@@ -327,7 +440,8 @@ extern "C" size_t pt_extrude_workspace_bytes(int W, int m, int max_jobs) {
   if (W < 1 || m < 1 || max_jobs < 1) return 0;
   const size_t K = (size_t)(m + 1) * W;
   const size_t J = (size_t)std::min(max_jobs, kJobsPerLaunch);
-  return al256(J * K * sizeof(float)) + al256((size_t)kMaxSplit * J * W * sizeof(float));
+  return al256(J * K * sizeof(float)) +
+         al256((size_t)std::max(kMaxSplit, kMaxSplitTiled) * J * W * sizeof(float));
 }
 
 // The operator of one form: FP32 [A | B] (SIMT GEMM) or its bf16 term tiles
@@ -401,13 +515,8 @@ static int extrude_jobs(const char* who, const ExtrudeForm& form, int W, int m, 
         if (form.terms == 0) {
           k_extrude_gather<<<dim3(std::min((K + 255) / 256, 64), J), 256, 0, s>>>(W, m, cap, buf, jp,
                                                                                 J, noise, X);
-          const int nsplit = split_for(W, J, K);
-          const int kslice = ((K + nsplit - 1) / nsplit + kTK - 1) / kTK * kTK;
-          nz = (K + kslice - 1) / kslice;
           const float* Mg = form.M + (size_t)kv.first * W * K;
-          ProfScope ps("k_extrude_gemm", s);
-          k_extrude_gemm<<<dim3((W + kTM - 1) / kTM, (J + kTJ - 1) / kTJ, nz), 256, 0, s>>>(
-              W, K, J, kslice, Mg, X, partial);
+          launch_gemm_tiled(W, K, J, Mg, X, partial, &nz, s);
         } else {
           const int NP = std::max(16, (J + 15) / 16 * 16);
           const int nkc = (K + tc::kTcKc - 1) / tc::kTcKc;
