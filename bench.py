@@ -208,6 +208,15 @@ def bench_extrude(torch, G, steps: int = 128):
     torch.cuda.synchronize()
     step_s = e0.elapsed_time(e1) / 1000.0 / steps
     flops = 2.0 * W * 3 * W * S
+    # per-kernel event timings of the same steps (a separate pass)
+    _lib.prof_report()
+    _lib.prof_enable(True)
+    ring.extrude(steps * ones)
+    torch.cuda.synchronize()
+    prof32 = _lib.prof_report()
+    _lib.prof_enable(False)
+    g32 = prof32.get("k_extrude_gemm", (1, float("nan")))
+    gemm32_s = g32[1] / g32[0] / 1e3
     # the split-bf16 tensor-core forms from the same state
     tc = {}
     for form in ("bf16x2", "bf16x3"):
@@ -253,9 +262,12 @@ def bench_extrude(torch, G, steps: int = 128):
     return {"workload": f"n=1024, 9 layers x {R} realisations ({S} screens), W={W}, "
                         f"stencil 2 rows, {steps} row steps timed; readout bilinear 9 layers",
             "row_steps_per_s": 1.0 / step_s, "gemm_tflops": flops / step_s / 1e12,
+            "gemm_us": gemm32_s * 1e6, "gemm_kernel_tflops": flops / gemm32_s / 1e12,
+            "gemm_kernel_frac_of_fp32_nominal": flops / gemm32_s / 80.5e12,
             "readout_frames_per_s": 1.0 / ro_s,
             "readout_gbs_out": n * n * 4 / ro_s / 1e9, "host_setup_s": setup_s,
-            "note": "split-K SIMT FP32 GEMM (plain form)", "tensor_core": tc}
+            "note": "register-tiled split-K SIMT FP32 GEMM (default form); FP32 nominal "
+                    "80.5 TFLOP/s = 152 SMs x 128 lanes x 2 x 2.07 GHz", "tensor_core": tc}
 
 
 def bench_diff(torch, G, iters: int = 3):

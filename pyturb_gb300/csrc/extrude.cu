@@ -193,7 +193,7 @@ k_extrude_gemm(int W, int K, int J, int kslice, const float* __restrict__ M,
 // scalar loads into registers while the previous stage is multiplied, then
 // stored K-major into the other shared buffer.
 template <int TJ>
-__global__ void __launch_bounds__(256, 2)
+__global__ void __launch_bounds__(256, TJ >= 9 ? 1 : 2)
 k_extrude_gemm_tiled(int W, int K, int J, int kslice, const float* __restrict__ M,
                      const float* __restrict__ X, float* __restrict__ partial) {
   constexpr int BJ = 16 * TJ;
@@ -401,13 +401,14 @@ int tc_prepare_launch(int W, int m, int G, const float* M, int terms, void* tile
 int tc_gemm_launch(int W, int m, int J, int terms, const uint8_t* At, const uint8_t* Bt,
                    float* partial, int* nz_out, cudaStream_t s);
 
-// Jobs per thread of the tiled GEMM and its split-K: about two CTAs per SM,
-// each slice at least 8 K steps long.
+// Jobs per thread of the tiled GEMM and its split-K: one wave of resident
+// CTAs, each slice at least 8 K steps long.
 static int tiled_tj(int J) { return J <= 32 ? 2 : (J <= 64 ? 4 : 9); }
 static int tiled_split(int W, int J, int K) {
   const int bj = 16 * tiled_tj(J);
   const int ctas = ((W + kGBM - 1) / kGBM) * ((J + bj - 1) / bj);
-  int s = std::max(1, std::min(kMaxSplitTiled, (2 * 152 + ctas - 1) / ctas));
+  const int per_sm = tiled_tj(J) >= 9 ? 1 : 2;  // resident CTAs (registers)
+  int s = std::max(1, std::min(kMaxSplitTiled, per_sm * 152 / ctas));
   return std::max(1, std::min(s, K / (8 * kGBK)));
 }
 static void launch_gemm_tiled(int W, int K, int J, const float* M, const float* X, float* partial,
