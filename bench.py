@@ -566,9 +566,11 @@ def main() -> None:
     ns, L = N_PIX, 9
     frames_per_launch = FRAMES_PER_STEP * args.steps / max(1, nlaunch)
     pairs = frames_per_launch / 2.0
-    blocks = np.ceil(frames_per_launch / 32.0)  # recurrence anchor blocks per launch
+    blocks = np.ceil(frames_per_launch / 64.0)  # recurrence anchor blocks (64 frames) per launch
     log2n = np.log2(ns)
-    # algorithmic bytes and FP32 flops per launch ("Roofline accounting")
+    # algorithmic bytes and FP32 flops per launch: the rows kernel reads every
+    # layer's spectrum once per anchor block and writes the packed intermediate;
+    # the column kernel reads it and writes two float32 frames per pair
     algo = {
         "k_frame_rows_uniform": (blocks * L * ns * ns * 8 + pairs * ns * ns * 8,
                                  frames_per_launch * (L * 8 * ns * ns)

@@ -469,9 +469,9 @@ k_frame_rows_uniform_reg(const float2* __restrict__ tw, const float2* __restrict
 // Everything the uniform frame kernels need besides the spectra, in one launch
 // (block ranges select the role):
 //   tables  — separable anchor/ratio phasors (as k_uniform_tables);
-//   nyquist — exact Hermitian parts on the Nyquist cross for the anchor block
-//             of 32 frames, by the same geometric recurrence (one thread per
-//             cross element and block, 32 frame accumulators in registers);
+//   nyquist — exact Hermitian parts on the Nyquist cross, by the same
+//             geometric recurrence from an exact anchor every kNyqGroup
+//             frames (one thread per cross element and frame group);
 //   coef    — per frame, shifted subharmonic coefficients summed over layers
 //             and their grid mean (as k_frame_coef), with the shifts
 //             s0 + f delta formed in FP64.

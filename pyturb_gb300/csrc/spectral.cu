@@ -244,7 +244,7 @@ k_frame_rows(FftDesc d, const float2* __restrict__ tw, FrameRowArgs a, float2* _
 // pairs are packed as Y = H_f0 + i H_f1 and kPairsPerFft rows are transformed
 // together.
 constexpr int kMaxUniformLayers = 16;
-constexpr int kAnchor = 32;
+constexpr int kAnchor = 64;
 constexpr int kPairsPerFft = 4;
 
 struct UniformParams {
