@@ -5,10 +5,6 @@
 // layers at once).
 #pragma once
 
-// Largest P * N (float2) of first basis rows the column kernels stage in
-// shared memory for the subharmonic epilogue.
-constexpr int kColBasisMax = 4096;
-
 template <int N>
 struct RegCfg {
   static constexpr int T = N / 8;

@@ -47,6 +47,9 @@ namespace pt {
 
 constexpr int kMaxLevels = 16;
 constexpr int kThreads = 256;
+// Largest P * ns (float2) of first basis rows the column kernels stage in
+// shared memory for the subharmonic epilogue.
+constexpr int kColBasisMax = 4096;
 
 static inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
@@ -64,7 +67,9 @@ static inline int gen_chunk(int ns) {
   size_t c = (size_t)(64u << 20) / per;
   return (int)std::max<size_t>(1, std::min<size_t>(256, c));
 }
-static inline int rows_per_cta(int ns) { return std::max(1, std::min(8, 1024 / ns)); }
+// Rows per CTA of the shared-memory row pass: about 2048 elements, so every
+// stage gives most of the 256 threads a butterfly.
+static inline int rows_per_cta(int ns) { return std::max(1, std::min(16, 2048 / ns)); }
 static inline int cols_per_cta(int ns) { return std::max(1, std::min(16, 4096 / ns)); }
 
 static inline void count_launch(int k = 1) {
@@ -399,7 +404,8 @@ k_pair_cols(FftDesc d, const float2* __restrict__ tw, const float2* __restrict__
   float2* bufA = sm;
   float2* bufB = sm + ns * C;
   float2* stw = bufB + ns * C;
-  float2* mtab = stw + ns;  // (2, 3P, C)
+  // column tables from an even float2 offset: utab below is read as float4
+  float2* mtab = stw + ((ns + 1) & ~1);  // (2, 3P, C)
   for (int i = threadIdx.x; i < ns; i += blockDim.x) stw[i] = tw[i];
   for (int i = threadIdx.x; i < ns * C; i += blockDim.x) {
     const int x = i / C, c = i % C;
@@ -429,9 +435,39 @@ k_pair_cols(FftDesc d, const float2* __restrict__ tw, const float2* __restrict__
     mtab[i] = m;
   }
   __syncthreads();
+  // symmetric bases (b1 = 1, b2 = conj b0): per column K = sum_p m[p][1].x
+  // minus the mean, per (level, column) (U_re, W_re, U_im, W_im), and the
+  // first basis row of each level staged when it fits, as in the register
+  // column pass; the transform's barriers order these writes before the reads
+  float4* utab = (float4*)(mtab + 2 * 3 * P * C);   // P * C
+  float2* ktab = mtab + 8 * (P > 0 ? P : 1) * C;     // C: (K_re, K_im)
+  float2* sbasis = ktab + C;                         // P * ns
+  const bool sb = st.sym && P * ns <= kColBasisMax;
+  if (st.sym) {
+    for (int i = threadIdx.x; i < P * C; i += blockDim.x) {
+      const int p = i / C, c = i % C;
+      const float2 m00 = mtab[(0 * 3 * P + 3 * p) * C + c], m02 = mtab[(0 * 3 * P + 3 * p + 2) * C + c];
+      const float2 m10 = mtab[(1 * 3 * P + 3 * p) * C + c], m12 = mtab[(1 * 3 * P + 3 * p + 2) * C + c];
+      utab[i] = make_float4(m00.x + m02.x, m02.y - m00.y, m10.x + m12.x, m12.y - m10.y);
+    }
+    for (int c = threadIdx.x; c < C; c += blockDim.x) {
+      float k0 = 0.f, k1 = 0.f;
+      for (int p = 0; p < P; ++p) {
+        k0 += mtab[(0 * 3 * P + 3 * p + 1) * C + c].x;
+        k1 += mtab[(1 * 3 * P + 3 * p + 1) * C + c].x;
+      }
+      if (P > 0 && do_re) k0 -= st.mean[row_re];
+      if (P > 0 && do_im) k1 -= st.mean[row_im];
+      ktab[c] = make_float2(k0, k1);
+    }
+    if (sb)
+      for (int i = threadIdx.x; i < P * ns; i += blockDim.x)
+        sbasis[i] = __ldg(st.basis + (size_t)(3 * (i / ns)) * ns + (i % ns));
+  }
   float2* res = fft_smem(bufA, bufB, d, stw, C, 1, C, true);
   const float mre = (P > 0 && do_re) ? st.mean[row_re] : 0.f;
   const float mim = (P > 0 && do_im) ? st.mean[row_im] : 0.f;
+  const float sre = img_scale_of(st, img_re), sim = img_scale_of(st, img_im);
   const size_t plane = (size_t)st.n_out * st.n_out;
   for (int i = threadIdx.x; i < ns * C; i += blockDim.x) {
     const int x = i / C, c = i % C;
@@ -440,24 +476,35 @@ k_pair_cols(FftDesc d, const float2* __restrict__ tw, const float2* __restrict__
     const int xo = x - st.crop, yo = y - st.crop;
     if (xo < 0 || yo < 0 || xo >= st.n_out || yo >= st.n_out) continue;
     const float2 v = res[i];
-    float lre = 0.f, lim = 0.f;
-    for (int pi = 0; pi < 3 * P; ++pi) {
-      const float2 b = st.basis[(size_t)pi * ns + x];
-      const float2 m0 = mtab[(0 * 3 * P + pi) * C + c];
-      const float2 m1 = mtab[(1 * 3 * P + pi) * C + c];
-      lre = fmaf(b.x, m0.x, fmaf(-b.y, m0.y, lre));
-      lim = fmaf(b.x, m1.x, fmaf(-b.y, m1.y, lim));
+    float lre, lim;
+    if (st.sym) {
+      const float2 k = ktab[c];
+      lre = k.x;
+      lim = k.y;
+      for (int p = 0; p < P; ++p) {
+        const float2 b = sb ? sbasis[p * ns + x] : __ldg(st.basis + (size_t)(3 * p) * ns + x);
+        const float4 u = utab[p * C + c];
+        lre = fmaf(b.x, u.x, fmaf(b.y, u.y, lre));
+        lim = fmaf(b.x, u.z, fmaf(b.y, u.w, lim));
+      }
+    } else {
+      lre = -mre;
+      lim = -mim;
+      for (int pi = 0; pi < 3 * P; ++pi) {
+        const float2 b = st.basis[(size_t)pi * ns + x];
+        const float2 m0 = mtab[(0 * 3 * P + pi) * C + c];
+        const float2 m1 = mtab[(1 * 3 * P + pi) * C + c];
+        lre = fmaf(b.x, m0.x, fmaf(-b.y, m0.y, lre));
+        lim = fmaf(b.x, m1.x, fmaf(-b.y, m1.y, lim));
+      }
     }
     const size_t o = (size_t)xo * st.n_out + yo;
-    if (do_re) {
-      const float val = img_scale_of(st, img_re) * (v.x + (lre - mre));
-      float* dst = st.out + (size_t)img_re * plane + o;
-      *dst = st.accumulate ? *dst + val : val;
-    }
-    if (do_im) {
-      const float val = img_scale_of(st, img_im) * (v.y + (lim - mim));
-      float* dst = st.out + (size_t)img_im * plane + o;
-      *dst = st.accumulate ? *dst + val : val;
+    if (st.accumulate) {
+      if (do_re) st.out[(size_t)img_re * plane + o] += sre * (v.x + lre);
+      if (do_im) st.out[(size_t)img_im * plane + o] += sim * (v.y + lim);
+    } else {
+      if (do_re) st.out[(size_t)img_re * plane + o] = sre * (v.x + lre);
+      if (do_im) st.out[(size_t)img_im * plane + o] = sim * (v.y + lim);
     }
   }
 }
@@ -693,7 +740,10 @@ static size_t rows_smem(int ns, int rpc) {
 }
 static size_t frame_rows_smem(int ns) { return (size_t)(8 * (ns + 1) + ns) * sizeof(float2); }
 static size_t cols_smem(int ns, int C, int P) {
-  return (size_t)(2 * ns * C + ns + 2 * 3 * std::max(P, 1) * C) * sizeof(float2);
+  // exchange buffers, twiddles, (m, U/W, K) column tables, staged basis rows
+  return (size_t)(2 * ns * C + ((ns + 1) & ~1) + 8 * std::max(P, 1) * C + C +
+                  (P * ns <= kColBasisMax ? P * ns : 0)) *
+         sizeof(float2);
 }
 
 template <class K>
