@@ -14,6 +14,15 @@ struct RegCfg {
   static constexpr int THREADS = NV * T;
 };
 
+// The paired column pass (generate / frames epilogue): 8 columns per CTA at
+// N = 1024 (1024 threads) so each warp's output stores cover whole 32-byte
+// sectors; RegCfg's columns otherwise.
+template <int N>
+struct PairColCfg {
+  static constexpr int C = N == 1024 ? 8 : RegCfg<N>::C;
+  static constexpr int THREADS = C * RegCfg<N>::T;
+};
+
 __device__ __forceinline__ void load_tw(float2* stw, const float2* tw, int n) {
   for (int i = threadIdx.x; i < n; i += blockDim.x) stw[i] = tw[i];
 }
@@ -135,10 +144,10 @@ k_plain_cols_reg(const float2* __restrict__ tw, const float2* __restrict__ work,
 //   K = sum_p Re m1_p - mean, U_p = Re(m0_p + m2_p), W_p = Im(m2_p - m0_p)
 // with m_pi(y) = sum_j coef_pij b_pj(y): 2P FMAs per element and output.
 template <int N>
-__global__ void __launch_bounds__(RegCfg<N>::THREADS)
+__global__ void __launch_bounds__(PairColCfg<N>::THREADS)
 k_pair_cols_reg(const float2* __restrict__ tw, const float2* __restrict__ work, int pair0,
                 PairStore st) {
-  constexpr int T = RegCfg<N>::T, C = RegCfg<N>::C;
+  constexpr int T = RegCfg<N>::T, C = PairColCfg<N>::C;
   extern __shared__ float2 sm[];
   float2* stw = sm;
   float2* buf = sm + N;             // 2 x N * C, column-interleaved exchange buffers

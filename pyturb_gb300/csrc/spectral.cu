@@ -972,7 +972,7 @@ static int plain_cols_reg(const pt_grid* g, const float2* work, int nimg, float2
 template <int N>
 static int pair_cols_reg_t(const pt_grid* g, const float2* work, int npair, int pair0,
                            const PairStore& st, cudaStream_t s) {
-  using Cfg = RegCfg<N>;
+  using Cfg = PairColCfg<N>;
   const int P = g->P;
   const size_t smem = (size_t)(N + 2 * Cfg::C * N + (2 * 3 + 2) * std::max(P, 1) * Cfg::C +
                                (P * N <= kColBasisMax ? P * N : 0)) *

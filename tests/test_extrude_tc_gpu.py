@@ -70,6 +70,35 @@ def test_one_step_at_benchmark_size_against_float64(form, tol):
     assert err < tol
 
 
+@pytest.mark.parametrize("S", [1, 20, 40, 65, 144])
+def test_fp32_one_step_job_counts(S):
+    """The FP32 form's register-tiled GEMM at every job-tile width (2, 4 or 9
+    jobs per thread) and a partial 128-row tile (W = 301), one step against
+    the float64 product."""
+    import torch
+
+    from pyturb_gb300.backend import NoiseStream
+    from pyturb_gb300.extrude import RingExtruder, build_extrusion
+
+    W, m, cap = 301, 2, 16
+    A, B = build_extrusion(W, m, 0.02, 20.0)
+    M = np.concatenate([A, B], axis=1)
+    rng = np.random.default_rng(S)
+    init = rng.standard_normal((S, m, W)).astype(np.float32)
+    streams = [NoiseStream(7 + s, np.random.default_rng) for s in range(S)]
+    ring = RingExtruder(W, m, cap, [(A, B)], [0] * S, [1.0] * S, streams, form="fp32")
+    for s in range(S):
+        ring.seed_rows(s, torch.tensor(init[s], device="cuda"))
+    ring.extrude(np.ones(S, dtype=np.int32))
+    torch.cuda.synchronize()
+    got = ring.buf[:, m].double().cpu().numpy()
+    again = [NoiseStream(7 + s, np.random.default_rng) for s in range(S)]
+    X = np.stack([np.concatenate([init[s].astype(np.float64).ravel(), again[s].draw((W,))])
+                  for s in range(S)])
+    err = rel_l2(got, X @ M.T)
+    assert err < 1e-6, err
+
+
 def test_tc_form_rejects_bad_terms():
     from pyturb_gb300.extrude import RingExtruder
 
