@@ -133,6 +133,22 @@ __device__ __forceinline__ void bfly_direct(float2* v, const float2* tw, int n) 
   for (int q = 0; q < R; ++q) v[q] = o[q];
 }
 
+// q = t / d, r = t mod d for 0 <= t < 2^22 and 1 <= d <= 2^14, through the
+// float reciprocal inv = 1/d: t * inv carries a relative error below 2^-23,
+// so the truncated quotient is off by at most one, and one step corrects it
+// (a runtime integer division costs several times the instructions).
+__device__ __forceinline__ void divmod_f(int t, int d, float inv, int& q, int& r) {
+  q = __float2int_rz(__int2float_rn(t) * inv);
+  r = t - q * d;
+  if (r < 0) {
+    --q;
+    r += d;
+  } else if (r >= d) {
+    ++q;
+    r -= d;
+  }
+}
+
 // One Stockham stage with a compile-time radix. Work items are (vector,
 // butterfly) pairs; `vfast` selects whether consecutive threads walk the
 // vector index (column tiles) or the butterfly index (rows).
@@ -143,18 +159,16 @@ __device__ __forceinline__ void stage_r(const float2* __restrict__ a, float2* __
   const int nb = n / R;
   const int total = nb * nvec;
   const int twstep = n / (Ns * R);
+  const float inv_split = 1.0f / (float)(vfast ? nvec : nb);
+  const float inv_ns = 1.0f / (float)Ns;
   for (int t = threadIdx.x; t < total; t += blockDim.x) {
     int v, j;
-    if (vfast) {
-      v = t % nvec;
-      j = t / nvec;
-    } else {
-      j = t % nb;
-      v = t / nb;
-    }
+    if (vfast) divmod_f(t, nvec, inv_split, j, v);
+    else divmod_f(t, nb, inv_split, v, j);
     const float2* src = a + v * vs;
     float2* dst = b + v * vs;
-    const int jm = j % Ns;
+    int jq, jm;
+    divmod_f(j, Ns, inv_ns, jq, jm);
     float2 x[R];
 #pragma unroll
     for (int r = 0; r < R; ++r) x[r] = src[(j + r * nb) * es];
@@ -168,7 +182,7 @@ __device__ __forceinline__ void stage_r(const float2* __restrict__ a, float2* __
     else if (R == 3) bfly3(x);
     else if (R == 5) bfly5(x);
     else bfly_direct<R>(x, tw, n);
-    const int idxD = (j / Ns) * Ns * R + jm;
+    const int idxD = jq * Ns * R + jm;
 #pragma unroll
     for (int q = 0; q < R; ++q) dst[(idxD + q * Ns) * es] = x[q];
   }
