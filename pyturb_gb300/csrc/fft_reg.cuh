@@ -76,9 +76,12 @@ __host__ __device__ constexpr int tw_offset(int s) {
   return off;
 }
 
-// Fill the per-stage tables from the N-entry table exp(+2 pi i k / N).
+// Fill the per-stage tables from the N-entry table exp(+2 pi i k / N), or
+// from a longer table exp(+2 pi i k / (stride N)) read at every stride-th
+// entry.
 template <int N>
-__device__ __forceinline__ void load_stage_tw(float2* stw, const float2* __restrict__ tw) {
+__device__ __forceinline__ void load_stage_tw(float2* stw, const float2* __restrict__ tw,
+                                              int stride = 1) {
   int ns = Pow2Plan<N>::radix(0);
   for (int s = 1; s < Pow2Plan<N>::stages; ++s) {
     const int r = Pow2Plan<N>::radix(s);
@@ -86,7 +89,7 @@ __device__ __forceinline__ void load_stage_tw(float2* stw, const float2* __restr
     const int off = tw_offset<N>(s);
     for (int i = threadIdx.x; i < ns * (r - 1); i += blockDim.x) {
       const int jm = i / (r - 1), q = i % (r - 1) + 1;
-      stw[off + i] = tw[(q * jm * twstep) & (N - 1)];
+      stw[off + i] = tw[((q * jm * twstep) & (N - 1)) * stride];
     }
     ns *= r;
   }
@@ -201,10 +204,40 @@ __device__ __forceinline__ void reg_fft(float2 (&x)[8], int j, const float2* tw,
   RegStages<N, 0, 1, Lay, Sync>::run(x, j, tw, s, sync);
 }
 
+// NV transforms of the same team in lockstep (one barrier per exchange for
+// all of them), each on its own pair of scratch vectors a[v], b[v] used
+// alternately as in RegStages2.
+template <int N, int S, int Ns, int NV, class Lay, class Sync>
+struct RegStagesMulti {
+  static __device__ __forceinline__ void run(float2 (&x)[NV][8], int j, const float2* tw,
+                                             const Lay* a, const Lay* b, const Sync& sync) {
+    constexpr int R = Pow2Plan<N>::radix(S);
+#pragma unroll
+    for (int v = 0; v < NV; ++v) reg_stage<N, R, Ns, S>(x[v], j, tw);
+    if constexpr (S + 1 < Pow2Plan<N>::stages) {
+#pragma unroll
+      for (int v = 0; v < NV; ++v) reg_scatter<N, R, Ns>(x[v], j, a[v]);
+      sync();
+#pragma unroll
+      for (int v = 0; v < NV; ++v) reg_gather8<N>(x[v], j, a[v]);
+      RegStagesMulti<N, S + 1, Ns * R, NV, Lay, Sync>::run(x, j, tw, b, a, sync);
+    }
+  }
+};
+
 // The same transform on two scratch vectors (first exchange in a). The caller
 // must synchronise the barrier's threads between its own last access of `a`
 // and this call; its last access of `b` only has to precede the call (the
 // first exchange's barrier orders it before b is written).
+// NV transforms in lockstep; the scratch vector arrays a and b hold NV
+// layouts each. Ordering contract as reg_fft_db, for every a[v] and b[v].
+template <int N, int NV, class Lay, class Sync = CtaSync>
+__device__ __forceinline__ void reg_fft_multi(float2 (&x)[NV][8], int j, const float2* tw,
+                                              const Lay* a, const Lay* b,
+                                              const Sync& sync = Sync{}) {
+  RegStagesMulti<N, 0, 1, NV, Lay, Sync>::run(x, j, tw, a, b, sync);
+}
+
 template <int N, class Lay, class Sync = CtaSync>
 __device__ __forceinline__ void reg_fft_db(float2 (&x)[8], int j, const float2* tw, const Lay& a,
                                            const Lay& b, const Sync& sync = Sync{}) {

@@ -733,6 +733,7 @@ __global__ void k_lgs_zoom(int L, int ns, int n, int T, const int32_t* __restric
 
 #include "frames_fast.cuh"  // power-of-two fast path kernels
 #include "cols_tma.cuh"     // TMA-fed column pass
+#include "gt_fast.cuh"       // register transforms of length 3 * 2^k (Good-Thomas)
 
 // ================================================================ host helpers
 static size_t rows_smem(int ns, int rpc) {
@@ -1044,6 +1045,62 @@ static int default_cols_variant() {
   return v;
 }
 
+// ---- Good-Thomas register path: ns = 3 M, M = 64 .. 512
+static int gt_m(int ns) {
+  if (ns % 3 != 0) return 0;
+  const int m = ns / 3;
+  return (m >= 64 && m <= 512 && (m & (m - 1)) == 0) ? m : 0;
+}
+
+template <int M>
+static int rows_gt_t(const pt_grid* g, const float2* in, int gen, const GenRowArgs& ga, int nimg,
+                     float2* work, cudaStream_t s) {
+  using G = GtCfg<3, M>;
+  const size_t smem = (size_t)(M + G::ROW_NV * 2 * 3 * G::PAD) * sizeof(float2);
+  if (int rc = set_smem(k_rows_gt<3, M>, smem, "k_rows_gt")) return rc;
+  ProfScope ps("k_rows", s);
+  k_rows_gt<3, M><<<dim3((G::N + G::ROW_NV - 1) / G::ROW_NV, nimg), G::ROW_THREADS, smem, s>>>(
+      g->tw, in, gen, ga, work);
+  return PT_OK;
+}
+
+template <int M>
+static int pair_cols_gt_t(const pt_grid* g, const float2* work, int npair, int pair0,
+                          const PairStore& st, cudaStream_t s) {
+  using G = GtCfg<3, M>;
+  const int P = g->P;
+  const size_t smem = (size_t)(M + 2 * 3 * M * G::C + 8 * std::max(P, 1) * G::C +
+                               (P * G::N <= kColBasisMax ? P * G::N : 0)) *
+                      sizeof(float2);
+  if (int rc = set_smem(k_pair_cols_gt<3, M>, smem, "k_pair_cols_gt")) return rc;
+  ProfScope ps("k_pair_cols", s);
+  k_pair_cols_gt<3, M><<<dim3((G::N + G::C - 1) / G::C, npair), G::COL_THREADS, smem, s>>>(
+      g->tw, work, pair0, st);
+  return PT_OK;
+}
+
+static int rows_gt(const pt_grid* g, const float2* in, int gen, const GenRowArgs& ga, int nimg,
+                   float2* work, cudaStream_t s) {
+  switch (gt_m(g->ns)) {
+    case 64: return rows_gt_t<64>(g, in, gen, ga, nimg, work, s);
+    case 128: return rows_gt_t<128>(g, in, gen, ga, nimg, work, s);
+    case 256: return rows_gt_t<256>(g, in, gen, ga, nimg, work, s);
+    case 512: return rows_gt_t<512>(g, in, gen, ga, nimg, work, s);
+  }
+  return fail(PT_ERR_UNSUPPORTED, "rows_gt: not 3 x 2^k");
+}
+
+static int pair_cols_gt(const pt_grid* g, const float2* work, int npair, int pair0,
+                        const PairStore& st, cudaStream_t s) {
+  switch (gt_m(g->ns)) {
+    case 64: return pair_cols_gt_t<64>(g, work, npair, pair0, st, s);
+    case 128: return pair_cols_gt_t<128>(g, work, npair, pair0, st, s);
+    case 256: return pair_cols_gt_t<256>(g, work, npair, pair0, st, s);
+    case 512: return pair_cols_gt_t<512>(g, work, npair, pair0, st, s);
+  }
+  return fail(PT_ERR_UNSUPPORTED, "pair_cols_gt: not 3 x 2^k");
+}
+
 static int pair_cols_reg(const pt_grid* g, const float2* work, int npair, int pair0,
                          const PairStore& st, cudaStream_t s) {
   if (g->cols_variant == 1) {
@@ -1271,6 +1328,8 @@ static int generate_impl(const pt_grid* g, int count, const float* amplitude,
     GenRowArgs ga{amplitude, noise, n_fft, b0, seed, call};
     if (pow2_fast(ns)) {
       if (int rc = rows_reg(g, nullptr, 1, ga, nb, w.img, s)) return rc;
+    } else if (gt_m(ns)) {
+      if (int rc = rows_gt(g, nullptr, 1, ga, nb, w.img, s)) return rc;
     } else {
       ProfScope ps("k_rows", s);
       k_rows<<<dim3((ns + rpc - 1) / rpc, nb), kThreads, rs, s>>>(g->desc, g->tw, rpc, nullptr, 1,
@@ -1307,6 +1366,8 @@ static int generate_impl(const pt_grid* g, int count, const float* amplitude,
     }
     if (pow2_fast(ns)) {
       if (int rc = pair_cols_reg(g, w.img, nb, b0, st, s)) return rc;
+    } else if (gt_m(ns)) {
+      if (int rc = pair_cols_gt(g, w.img, nb, b0, st, s)) return rc;
     } else {
       ProfScope ps("k_pair_cols", s);
       k_pair_cols<<<dim3((ns + C - 1) / C, nb), kThreads, cs, s>>>(g->desc, g->tw, w.img, C, b0, st);
