@@ -32,7 +32,7 @@ struct GtCfg {
   static_assert(U > 0 && V > 0 && (M & (M - 1)) == 0 && M >= 64, "R1, M coprime; M = 2^k >= 64");
   static constexpr int ROW_NV = 256 / T;        // rows (teams) per row-pass CTA
   static constexpr int ROW_THREADS = ROW_NV * T;
-  static constexpr int C = 8;                   // columns per column-pass CTA
+  static constexpr int C = M <= 128 ? 16 : 8;  // columns per column-pass CTA
   static constexpr int COL_THREADS = C * T;
   static constexpr int PAD = fft_padded(M);     // one padded row sub-vector
   // input position of (n1, n2) and output position of (k1, k2)
