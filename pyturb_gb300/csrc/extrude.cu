@@ -53,38 +53,35 @@ struct JobParams {
   GatherJob j[kJobsPerLaunch];
 };
 
-// X[j][k], k < mW: stencil rows; k >= mW: bscale * beta
-__device__ __forceinline__ float gather_value(int W, int m, int cap, const float* __restrict__ slab,
-                                              const GatherJob& jb, int k,
-                                              const float* __restrict__ noise) {
-  if (k < m * W) {
-    const int r = k / W, c = k % W;
-    int phys = jb.head - m + r;
-    if (phys < 0) phys += cap;
-    return slab[(size_t)phys * W + c];
-  }
-  const int c = k - m * W;
-  float z;
-  if (noise) {
-    z = noise[jb.noise_off + c];
-  } else {
-    // one Philox call yields a pair: even/odd columns share it
-    const float2 p = philox_cnormal(jb.key, (uint64_t)(c >> 1), jb.row, kDomainExtrude);
-    z = (c & 1) ? p.y : p.x;
-  }
-  return jb.bscale * z;
-}
-
+// X[j] for job j = blockIdx.z: block row blockIdx.y < m copies stencil row y
+// from the ring, row m holds bscale * beta; each thread makes two adjacent
+// columns (one Philox call for both noise values).
 __global__ void k_extrude_gather(int W, int m, int cap, const float* __restrict__ buf,
                                  const JobParams jobs, int J, const float* __restrict__ noise,
                                  float* __restrict__ X) {
-  const int j = blockIdx.y;
+  const int j = blockIdx.z;
   if (j >= J) return;
   const GatherJob& jb = jobs.j[j];
   const int K = (m + 1) * W;
-  const float* slab = buf + (size_t)jb.screen * cap * W;
-  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < K; k += gridDim.x * blockDim.x)
-    X[(size_t)j * K + k] = gather_value(W, m, cap, slab, jb, k, noise);
+  const int r = blockIdx.y;
+  const int c = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
+  if (c >= W) return;
+  float* dst = X + (size_t)j * K + (size_t)r * W + c;
+  const bool two = c + 1 < W;
+  if (r < m) {
+    int phys = jb.head - m + r;
+    if (phys < 0) phys += cap;
+    const float* src = buf + ((size_t)jb.screen * cap + phys) * W + c;
+    dst[0] = src[0];
+    if (two) dst[1] = src[1];
+  } else if (noise) {
+    dst[0] = jb.bscale * noise[jb.noise_off + c];
+    if (two) dst[1] = jb.bscale * noise[jb.noise_off + c + 1];
+  } else {
+    const float2 p = philox_cnormal(jb.key, (uint64_t)(c >> 1), jb.row, kDomainExtrude);
+    dst[0] = jb.bscale * p.x;
+    if (two) dst[1] = jb.bscale * p.y;
+  }
 }
 
 // The same operand for the tensor-core form: split into `terms` bf16 terms and
@@ -109,10 +106,41 @@ __global__ void k_tc_gather(int W, int m, int cap, const float* __restrict__ buf
     if (j < J) {
       const GatherJob& jb = jobs.j[j];
       const float* slab = buf + (size_t)jb.screen * cap * W;
+      // stencil row and column of k0 once; k0 is even, so noise pairs
+      // (c, c + 1) of one Philox call stay together unless a row ends
+      int r = k0 / W, c = k0 - r * W;
+      const float* src = nullptr;
+      auto row_src = [&](int rr) {
+        int phys = jb.head - m + rr;
+        if (phys < 0) phys += cap;
+        return slab + (size_t)phys * W;
+      };
+      if (r < m) src = row_src(r);
+      float2 pn = make_float2(0.f, 0.f);
+      int pc = -2;  // column pair whose normals are in pn
 #pragma unroll
       for (int q = 0; q < 8; ++q) {
-        const int k = k0 + q;
-        v[q] = k < K ? gather_value(W, m, cap, slab, jb, k, noise) : 0.f;
+        float val = 0.f;
+        if (k0 + q < K) {
+          if (r < m) {
+            val = src[c];
+          } else if (noise) {
+            val = jb.bscale * noise[jb.noise_off + c];
+          } else {
+            if ((c >> 1) != pc) {
+              pn = philox_cnormal(jb.key, (uint64_t)(c >> 1), jb.row, kDomainExtrude);
+              pc = c >> 1;
+            }
+            val = jb.bscale * ((c & 1) ? pn.y : pn.x);
+          }
+        }
+        v[q] = val;
+        if (++c == W) {
+          c = 0;
+          ++r;
+          if (r < m) src = row_src(r);
+          pc = -2;
+        }
       }
     } else {
 #pragma unroll
@@ -514,21 +542,30 @@ static int extrude_jobs(const char* who, const ExtrudeForm& form, int W, int m, 
         for (int q = 0; q < J; ++q) jp.j[q] = hj[b + q];
         int nz = 0;
         if (form.terms == 0) {
-          k_extrude_gather<<<dim3(std::min((K + 255) / 256, 64), J), 256, 0, s>>>(W, m, cap, buf, jp,
-                                                                                J, noise, X);
+          {
+            ProfScope ps("k_extrude_gather", s);
+            k_extrude_gather<<<dim3((W + 511) / 512, m + 1, J), 256, 0, s>>>(W, m, cap, buf, jp,
+                                                                               J, noise, X);
+          }
           const float* Mg = form.M + (size_t)kv.first * W * K;
           launch_gemm_tiled(W, K, J, Mg, X, partial, &nz, s);
         } else {
           const int NP = std::max(16, (J + 15) / 16 * 16);
           const int nkc = (K + tc::kTcKc - 1) / tc::kTcKc;
           const size_t items = (size_t)nkc * (tc::kTcKc / 8) * NP;
-          k_tc_gather<<<(unsigned)std::min<size_t>((items + 255) / 256, 152 * 8), 256, 0, s>>>(
-              W, m, cap, buf, jp, J, NP, nkc, form.terms, noise, Bt);
+          {
+            ProfScope ps("k_tc_gather", s);
+            k_tc_gather<<<(unsigned)std::min<size_t>((items + 255) / 256, 152 * 8), 256, 0, s>>>(
+                W, m, cap, buf, jp, J, NP, nkc, form.terms, noise, Bt);
+          }
           if (int rc = tc_gemm_launch(W, m, J, form.terms, form.tiles + (size_t)kv.first * op_group,
                                       Bt, partial, &nz, s))
             return rc;
         }
-        k_extrude_reduce<<<dim3((W + 255) / 256, J), 256, 0, s>>>(W, J, cap, nz, partial, jp, buf);
+        {
+          ProfScope ps("k_extrude_reduce", s);
+          k_extrude_reduce<<<dim3((W + 255) / 256, J), 256, 0, s>>>(W, J, cap, nz, partial, jp, buf);
+        }
         count_launch_e(form.terms ? 2 : 3);
         if (int rc = check_launch(who)) return rc;
       }
