@@ -52,6 +52,11 @@ constexpr int kJobsPerLaunch = 192;
 struct JobParams {
   GatherJob j[kJobsPerLaunch];
 };
+// Ring destination (screen, physical row) of each job's new row: what the
+// reduce needs, in a fifth of the launch parameters.
+struct RingDst {
+  int2 d[kJobsPerLaunch];
+};
 
 // X[j] for job j = blockIdx.z: block row blockIdx.y < m copies stencil row y
 // from the ring, row m holds bscale * beta; each thread makes two adjacent
@@ -299,14 +304,13 @@ k_extrude_gemm_tiled(int W, int K, int J, int kslice, const float* __restrict__ 
 }
 
 __global__ void k_extrude_reduce(int W, int J, int cap, int nsplit, const float* __restrict__ partial,
-                                 const JobParams jobs, float* __restrict__ buf) {
+                                 const RingDst dst, float* __restrict__ buf) {
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y;
   if (r >= W || j >= J) return;
   float s = 0.f;
   for (int z = 0; z < nsplit; ++z) s += __ldcs(partial + ((size_t)z * J + j) * W + r);
-  const GatherJob& jb = jobs.j[j];
-  buf[((size_t)jb.screen * cap + jb.head) * W + r] = s;
+  buf[((size_t)dst.d[j].x * cap + dst.d[j].y) * W + r] = s;
 }
 
 // ---------------------------------------------------------------- readout
@@ -563,8 +567,10 @@ static int extrude_jobs(const char* who, const ExtrudeForm& form, int W, int m, 
             return rc;
         }
         {
+          RingDst dst;
+          for (int q = 0; q < J; ++q) dst.d[q] = make_int2(jp.j[q].screen, jp.j[q].head);
           ProfScope ps("k_extrude_reduce", s);
-          k_extrude_reduce<<<dim3((W + 255) / 256, J), 256, 0, s>>>(W, J, cap, nz, partial, jp, buf);
+          k_extrude_reduce<<<dim3((W + 255) / 256, J), 256, 0, s>>>(W, J, cap, nz, partial, dst, buf);
         }
         count_launch_e(form.terms ? 2 : 3);
         if (int rc = check_launch(who)) return rc;
