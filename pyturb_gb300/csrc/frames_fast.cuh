@@ -185,7 +185,7 @@ k_pair_cols_reg(const float2* __restrict__ tw, const float2* __restrict__ work, 
   float2 x[8];
 #pragma unroll
   for (int i = 0; i < 8; ++i)
-    x[i] = ok ? work[((size_t)pl * N + j + T * i) * N + y] : make_float2(0.f, 0.f);
+    x[i] = ok ? __ldcs(work + ((size_t)pl * N + j + T * i) * N + y) : make_float2(0.f, 0.f);
   __syncthreads();
   // per-column symmetric-basis constants: K (this thread's registers) and,
   // per level, (U_re, W_re, U_im, W_im) in a shared float4 table read once per
@@ -279,8 +279,8 @@ k_pair_cols_reg(const float2* __restrict__ tw, const float2* __restrict__ work, 
       if (do_re) ore[o] += sre * x[i].x;
       if (do_im) oim[o] += sim * x[i].y;
     } else {
-      if (do_re) ore[o] = sre * x[i].x;
-      if (do_im) oim[o] = sim * x[i].y;
+      if (do_re) __stcs(ore + o, sre * x[i].x);
+      if (do_im) __stcs(oim + o, sim * x[i].y);
     }
   }
 }
