@@ -188,7 +188,7 @@ k_pair_cols_gt(const float2* __restrict__ tw, const float2* __restrict__ work, i
   for (int n1 = 0; n1 < R1; ++n1)
 #pragma unroll
     for (int i = 0; i < 8; ++i)
-      x[n1][i] = ok ? work[((size_t)pl * N + G::in_pos(n1, j + T * i)) * N + y]
+      x[n1][i] = ok ? __ldcs(work + ((size_t)pl * N + G::in_pos(n1, j + T * i)) * N + y)
                     : make_float2(0.f, 0.f);
   __syncthreads();
   float4* utab = (float4*)(mtab + 2 * 3 * P * C);  // even offset: M C and 6 P C are even
@@ -257,8 +257,8 @@ k_pair_cols_gt(const float2* __restrict__ tw, const float2* __restrict__ work, i
         if (do_re) ore[o] += sre * (x[k1i][i].x + lre);
         if (do_im) oim[o] += sim * (x[k1i][i].y + lim);
       } else {
-        if (do_re) ore[o] = sre * (x[k1i][i].x + lre);
-        if (do_im) oim[o] = sim * (x[k1i][i].y + lim);
+        if (do_re) __stcs(ore + o, sre * (x[k1i][i].x + lre));
+        if (do_im) __stcs(oim + o, sim * (x[k1i][i].y + lim));
       }
     }
 }

@@ -410,7 +410,7 @@ k_pair_cols(FftDesc d, const float2* __restrict__ tw, const float2* __restrict__
   for (int i = threadIdx.x; i < ns * C; i += blockDim.x) {
     const int x = i / C, c = i % C;
     const int y = y0 + c;
-    bufA[i] = y < ns ? work[((size_t)pl * ns + x) * ns + y] : make_float2(0.f, 0.f);
+    bufA[i] = y < ns ? __ldcs(work + ((size_t)pl * ns + x) * ns + y) : make_float2(0.f, 0.f);
   }
   const int img_re = pair * st.re_mul + st.re_add;
   const int img_im = pair * st.im_mul + st.im_add;
@@ -503,8 +503,8 @@ k_pair_cols(FftDesc d, const float2* __restrict__ tw, const float2* __restrict__
       if (do_re) st.out[(size_t)img_re * plane + o] += sre * (v.x + lre);
       if (do_im) st.out[(size_t)img_im * plane + o] += sim * (v.y + lim);
     } else {
-      if (do_re) st.out[(size_t)img_re * plane + o] = sre * (v.x + lre);
-      if (do_im) st.out[(size_t)img_im * plane + o] = sim * (v.y + lim);
+      if (do_re) __stcs(st.out + (size_t)img_re * plane + o, sre * (v.x + lre));
+      if (do_im) __stcs(st.out + (size_t)img_im * plane + o, sim * (v.y + lim));
     }
   }
 }
