@@ -27,6 +27,15 @@ __device__ __forceinline__ void load_tw(float2* stw, const float2* tw, int n) {
   for (int i = threadIdx.x; i < n; i += blockDim.x) stw[i] = tw[i];
 }
 
+// 64-bit read-only load with an L2 cache policy (createpolicy)
+__device__ __forceinline__ float2 ld_evict_last(const float2* p, uint64_t pol) {
+  float2 v;
+  asm("ld.global.nc.L2::cache_hint.v2.f32 {%0, %1}, [%2], %3;"
+               : "=f"(v.x), "=f"(v.y)
+               : "l"(p), "l"(pol));
+  return v;
+}
+
 // ------------------------------------------------------------------ packed f32x2
 typedef unsigned long long f2x;
 __device__ __forceinline__ f2x pk2(float lo, float hi) {
@@ -325,6 +334,9 @@ k_frame_rows_uniform_reg(const float2* __restrict__ tw, const float2* __restrict
   const int nfr = min(kAnchor, F - fbeg);
   // row N/2 is the Nyquist row: every element comes from hn, no recurrence
   const bool nyq_row = kx == N / 2;
+  // the layer spectra are re-read by every chunk: keep them in L2
+  uint64_t pol;
+  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
   if (threadIdx.x < nfr) hcol[threadIdx.x] = hn[(size_t)(fbeg + threadIdx.x) * 2 * N + N + kx];
   // packed state: lanes (layer 2q, layer 2q+1). With one column per thread
   // -Ry is kept beside Ry so the complex step needs no separate negation
@@ -344,8 +356,8 @@ k_frame_rows_uniform_reg(const float2* __restrict__ tw, const float2* __restrict
         ax[h] = ay[h] = ry[h] = 0.f;
         rx[h] = 1.f;
         if (l < LM && l < L) {
-          const float2 sa = spectra[((size_t)l * N + kx) * N + ky];
-          const float2 sb = spectra[((size_t)l * N + nkx) * N + nky];
+          const float2 sa = ld_evict_last(spectra + ((size_t)l * N + kx) * N + ky, pol);
+          const float2 sb = ld_evict_last(spectra + ((size_t)l * N + nkx) * N + nky, pol);
           const float2 sh = make_float2(0.5f * (sa.x + sb.x), 0.5f * (sa.y - sb.y));
           const size_t bl = (size_t)blockIdx.y * L + l;
           const float2 a = cmul(cmul(sh, ut.px0[bl * N + kx]), ut.py0[bl * N + ky]);
