@@ -165,6 +165,20 @@ __device__ __forceinline__ float2 screen_normal(uint64_t key, uint64_t row, int 
   return upper ? hi : lo;
 }
 
+// ---------------------------------------------------------------- L2 policy
+// An L2 evict-last policy (createpolicy) and read-only loads that carry it,
+// for tables every CTA re-reads (filters, operators).
+__device__ __forceinline__ uint64_t l2_evict_last() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ float ld_keep(const float* p, uint64_t pol) {
+  float v;
+  asm("ld.global.nc.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(v) : "l"(p), "l"(pol));
+  return v;
+}
+
 // ---------------------------------------------------------------- fixed point phase
 // Shift-theorem phases are formed as k * u (mod 1) with u = frac(s * df)
 // held as a 64-bit binary fraction, so the product wraps exactly and the

@@ -240,6 +240,7 @@ k_extrude_gemm_tiled(int W, int K, int J, int kslice, const float* __restrict__ 
   const int kb = blockIdx.z * kslice, ke = min(K, kb + kslice);
   // staging map: K offset lk, rows / jobs lr + 16 i
   const int lk = tid & 15, lr = tid >> 4;
+  const uint64_t pol = l2_evict_last();  // the operator is re-read every row step
   float ra[8], rx[TJ];
   auto load = [&](int k0) {
     const int k = k0 + lk;
@@ -247,7 +248,7 @@ k_extrude_gemm_tiled(int W, int K, int J, int kslice, const float* __restrict__ 
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
       const int r = r0 + lr + 16 * i;
-      ra[i] = (kin && r < W) ? __ldg(M + (size_t)r * K + k) : 0.f;
+      ra[i] = (kin && r < W) ? ld_keep(M + (size_t)r * K + k, pol) : 0.f;
     }
 #pragma unroll
     for (int v = 0; v < TJ; ++v) {

@@ -84,12 +84,13 @@ k_rows_reg(const float2* __restrict__ tw, const float2* __restrict__ in, int gen
   if (ok && gen && !ga.noise) {
     // one Philox call per element pair (ky, ky + N/2): elements i and i + 4
     const uint64_t row = (uint64_t)(ga.img0 + img) * N + kx;
+    const uint64_t pol = l2_evict_last();  // the filter is re-read by every image
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
       float2 lo, hi;
       philox_cnormal2(ga.seed, row * (N / 2) + j + T * i, ga.call, kDomainScreen, lo, hi);
-      const float a0 = ga.amplitude[(size_t)kx * N + j + T * i];
-      const float a1 = ga.amplitude[(size_t)kx * N + j + T * (i + 4)];
+      const float a0 = ld_keep(ga.amplitude + (size_t)kx * N + j + T * i, pol);
+      const float a1 = ld_keep(ga.amplitude + (size_t)kx * N + j + T * (i + 4), pol);
       x[i] = make_float2(lo.x * a0, lo.y * a0);
       x[i + 4] = make_float2(hi.x * a1, hi.y * a1);
     }

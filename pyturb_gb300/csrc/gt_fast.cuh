@@ -88,6 +88,7 @@ k_rows_gt(const float2* __restrict__ tw, const float2* __restrict__ in, int gen,
   for (int n1 = 0; n1 < R1; ++n1) {
     if (ok && gen && !ga.noise) {
       const uint64_t row = (uint64_t)(ga.img0 + img) * N + kx;
+      const uint64_t pol = l2_evict_last();  // the filter is re-read by every image
 #pragma unroll
       for (int i = 0; i < 4; ++i) {
         const int na = G::in_pos(n1, j + T * i);  // its partner is na + N/2 (mod N)
@@ -95,8 +96,8 @@ k_rows_gt(const float2* __restrict__ tw, const float2* __restrict__ in, int gen,
         float2 lo, hi;
         philox_cnormal2(ga.seed, row * H + (na < H ? na : nb), ga.call, kDomainScreen, lo, hi);
         const float2 za = na < H ? lo : hi, zb = na < H ? hi : lo;
-        const float a0 = ga.amplitude[(size_t)kx * N + na];
-        const float a1 = ga.amplitude[(size_t)kx * N + nb];
+        const float a0 = ld_keep(ga.amplitude + (size_t)kx * N + na, pol);
+        const float a1 = ld_keep(ga.amplitude + (size_t)kx * N + nb, pol);
         x[n1][i] = make_float2(za.x * a0, za.y * a0);
         x[n1][i + 4] = make_float2(zb.x * a1, zb.y * a1);
       }
