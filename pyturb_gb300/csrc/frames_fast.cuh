@@ -14,12 +14,13 @@ struct RegCfg {
   static constexpr int THREADS = NV * T;
 };
 
-// The paired column pass (generate / frames epilogue): 8 columns per CTA at
-// N = 1024 (1024 threads) so each warp's output stores cover whole 32-byte
-// sectors; RegCfg's columns otherwise.
+// The paired column pass (generate / frames epilogue): 16 columns per CTA at
+// N = 512 and 8 at N = 1024 (1024 threads: each CTA's twiddle and basis
+// staging serves more columns, and a warp's output stores cover whole
+// sectors); RegCfg's columns otherwise.
 template <int N>
 struct PairColCfg {
-  static constexpr int C = N == 1024 ? 8 : RegCfg<N>::C;
+  static constexpr int C = N == 1024 ? 8 : (N == 512 ? 16 : RegCfg<N>::C);
   static constexpr int THREADS = C * RegCfg<N>::T;
 };
 
