@@ -80,6 +80,7 @@ k_rows_reg(const float2* __restrict__ tw, const float2* __restrict__ in, int gen
   load_stage_tw<N>(stw, tw);
   const int kx = blockIdx.x * NV + v;
   const int img = blockIdx.y;
+  if (gen) gen_coef_pair(ga, img);
   const bool ok = kx < N;
   float2 x[8];
   if (ok && gen && !ga.noise) {

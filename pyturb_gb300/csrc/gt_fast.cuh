@@ -82,6 +82,7 @@ k_rows_gt(const float2* __restrict__ tw, const float2* __restrict__ in, int gen,
   load_stage_tw<M>(stw, tw, R1);  // exp(2 pi i k / M) = tw_N[R1 k]
   const int kx = blockIdx.x * NV + v;
   const int img = blockIdx.y;
+  if (gen) gen_coef_pair(ga, img);
   const bool ok = kx < N;
   float2 x[R1][8];
 #pragma unroll

@@ -120,7 +120,56 @@ struct GenRowArgs {
   int n_fft;
   int img0;            // first FFT index of this chunk
   uint64_t seed, call;
+  // subharmonic coefficients of the chunk's screens (P = 0: none), made by
+  // warps 0 and 1 of each pair's first row CTA
+  const float* sh_amp;    // (P, 9)
+  const float* sh_noise;  // (P, 2, count, 3, 3) or null
+  const double* beta;     // (P, 3, 2) grid means of the basis rows
+  float2* coef;           // (2 ch, P, 9)
+  float* mean;            // (2 ch)
+  int count, ch, P;
 };
+
+// coef[slot][p][ij] = (n0 + i n1) * sh_amp[p][ij] of screen gc and
+// mean[slot] = Re sum_p,ij coef beta_i beta_j: one warp, a lane per (level,
+// 3x3 cell), the mean reduced by shuffles.
+__device__ __forceinline__ void gen_coef_warp(const GenRowArgs& a, int gc, int slot, int lane) {
+  double mr = 0.0;
+  for (int q = lane; q < a.P * 9; q += 32) {
+    const int p = q / 9, ij = q - 9 * p;
+    float2 z;
+    if (a.sh_noise) {
+      // layout (P, 2, count, 3, 3)
+      const size_t base = (size_t)p * 2 * a.count * 9;
+      z = make_float2(a.sh_noise[base + (size_t)gc * 9 + ij],
+                      a.sh_noise[base + (size_t)a.count * 9 + (size_t)gc * 9 + ij]);
+    } else {
+      z = philox_cnormal(a.seed, ((uint64_t)gc * kMaxLevels + p) * 9 + ij, a.call, kDomainSub);
+    }
+    const float amp = a.sh_amp[q];
+    const float2 cf = make_float2(z.x * amp, z.y * amp);
+    a.coef[(size_t)slot * a.P * 9 + q] = cf;
+    const int i = ij / 3, j = ij % 3;
+    const double bir = a.beta[(p * 3 + i) * 2], bii = a.beta[(p * 3 + i) * 2 + 1];
+    const double bjr = a.beta[(p * 3 + j) * 2], bji = a.beta[(p * 3 + j) * 2 + 1];
+    const double br = bir * bjr - bii * bji, bi = bir * bji + bii * bjr;
+    mr += (double)cf.x * br - (double)cf.y * bi;
+  }
+  for (int o = 16; o > 0; o >>= 1) mr += __shfl_xor_sync(0xffffffffu, mr, o);
+  if (lane == 0) a.mean[slot] = (float)mr;
+}
+
+// In the first row CTA (blockIdx.x == 0) of transform pair `img` of the
+// chunk, warp 0 makes the coefficients of its real-part screen b0 + img
+// (slot img) and warp 1 those of its imaginary-part screen n_fft + b0 + img
+// (slot ch + img), when they exist. No barrier is involved.
+__device__ __forceinline__ void gen_coef_pair(const GenRowArgs& a, int img) {
+  if (a.P <= 0 || blockIdx.x != 0 || threadIdx.x >= 64) return;
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int gc = (w == 0 ? 0 : a.n_fft) + a.img0 + img;
+  if (gc >= a.count) return;  // warp-uniform
+  gen_coef_warp(a, gc, w == 0 ? img : a.ch + img, lane);
+}
 
 // Plain complex rows (pt_ifft2) and generate rows share this kernel: `gen`
 // selects the producer. rpc rows per CTA, one transform per row.
@@ -131,6 +180,7 @@ k_rows(FftDesc d, const float2* __restrict__ tw, int rpc, const float2* __restri
   const int ns = d.n;
   const int row0 = blockIdx.x * rpc;
   const int img = blockIdx.y;  // image within this chunk
+  if (gen) gen_coef_pair(ga, img);
   const int vs = ns + 1;
   float2* bufA = sm;
   float2* bufB = sm + rpc * vs;
@@ -533,45 +583,6 @@ k_plain_cols(FftDesc d, const float2* __restrict__ tw, const float2* __restrict_
     const int y = y0 + c;
     if (y < ns) out[((size_t)img * ns + x) * ns + y] = res[i];
   }
-}
-
-// ================================================================ coefficient prep
-// generate(): coef[slot][p][ij] = (n0 + i n1) * sh_amp[p][ij] and
-// mean[slot] = Re sum_p,ij coef beta_i beta_j for the chunk's screens.
-__global__ void __launch_bounds__(128)
-k_gen_coef(int count, int b0, int n_re, int n_im, int n_fft, int ch, int P,
-           const float* __restrict__ sh_amp, const float* __restrict__ sh_noise, uint64_t seed,
-           uint64_t call, const double* __restrict__ beta, float2* __restrict__ coef,
-           float* __restrict__ mean) {
-  // one warp per screen, a lane per (level, 3x3 cell): screens [0, n_re) are
-  // b0 + c (slots c), the rest n_fft + b0 + (c - n_re) (slots ch + c - n_re)
-  const int c = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
-  if (c >= n_re + n_im) return;
-  const int gc = c < n_re ? b0 + c : n_fft + b0 + (c - n_re);
-  const int slot = c < n_re ? c : ch + (c - n_re);
-  double mr = 0.0;
-  for (int q = lane; q < P * 9; q += 32) {
-    const int p = q / 9, ij = q - 9 * p;
-    float2 z;
-    if (sh_noise) {
-      // layout (P, 2, count, 3, 3)
-      const size_t base = (size_t)p * 2 * count * 9;
-      z = make_float2(sh_noise[base + (size_t)gc * 9 + ij],
-                      sh_noise[base + (size_t)count * 9 + (size_t)gc * 9 + ij]);
-    } else {
-      z = philox_cnormal(seed, ((uint64_t)gc * kMaxLevels + p) * 9 + ij, call, kDomainSub);
-    }
-    const float amp = sh_amp[q];
-    const float2 cf = make_float2(z.x * amp, z.y * amp);
-    coef[(size_t)slot * P * 9 + q] = cf;
-    const int i = ij / 3, j = ij % 3;
-    const double bir = beta[(p * 3 + i) * 2], bii = beta[(p * 3 + i) * 2 + 1];
-    const double bjr = beta[(p * 3 + j) * 2], bji = beta[(p * 3 + j) * 2 + 1];
-    const double br = bir * bjr - bii * bji, bi = bir * bji + bii * bjr;
-    mr += (double)cf.x * br - (double)cf.y * bi;
-  }
-  for (int o = 16; o > 0; o >>= 1) mr += __shfl_xor_sync(0xffffffffu, mr, o);
-  if (lane == 0) mean[slot] = (float)mr;
 }
 
 // frames: per frame f of a chunk, shifted-and-summed subharmonic
@@ -1325,7 +1336,8 @@ static int generate_impl(const pt_grid* g, int count, const float* amplitude,
   if (int rc = set_smem(k_pair_cols, cs, "k_pair_cols")) return rc;
   for (int b0 = 0; b0 < n_fft; b0 += ch) {
     const int nb = std::min(ch, n_fft - b0);
-    GenRowArgs ga{amplitude, noise, n_fft, b0, seed, call};
+    GenRowArgs ga{amplitude, noise, n_fft, b0, seed, call, sh_amp, sh_noise, g->beta,
+                  w.coef, w.mean, count, ch, P};
     if (pow2_fast(ns)) {
       if (int rc = rows_reg(g, nullptr, 1, ga, nb, w.img, s)) return rc;
     } else if (gt_m(ns)) {
@@ -1356,14 +1368,6 @@ static int generate_impl(const pt_grid* g, int count, const float* amplitude,
     st.P = P;
     st.sym = g->sym;
     st.img_scale = screen_scale;
-    if (P > 0) {
-      const int n_re = std::min(nb, count - b0);
-      const int n_im = std::max(0, std::min(nb, count - (n_fft + b0)));
-      const int nsc = n_re + n_im;
-      k_gen_coef<<<(nsc + 3) / 4, 128, 0, s>>>(count, b0, n_re, n_im, n_fft, ch, P, sh_amp,
-                                               sh_noise, seed, call, g->beta, w.coef, w.mean);
-      count_launch();
-    }
     if (pow2_fast(ns)) {
       if (int rc = pair_cols_reg(g, w.img, nb, b0, st, s)) return rc;
     } else if (gt_m(ns)) {
