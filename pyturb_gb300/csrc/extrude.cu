@@ -61,9 +61,15 @@ struct RingDst {
 // X[j] for job j = blockIdx.z: block row blockIdx.y < m copies stencil row y
 // from the ring, row m holds bscale * beta; each thread makes two adjacent
 // columns (one Philox call for both noise values).
-__global__ void k_extrude_gather(int W, int m, int cap, const float* __restrict__ buf,
+//
+// With `prev` set, the previous launch extruded the same screens one row
+// earlier and its split-K slices (prev_nz of them) are still unreduced: row
+// m - 1 here is that new row, summed in the order of k_extrude_reduce and
+// written both into the ring and into X (no thread reads that ring row).
+__global__ void k_extrude_gather(int W, int m, int cap, float* __restrict__ buf,
                                  const JobParams jobs, int J, const float* __restrict__ noise,
-                                 float* __restrict__ X) {
+                                 float* __restrict__ X, const float* __restrict__ prev,
+                                 int prev_nz) {
   const int j = blockIdx.z;
   if (j >= J) return;
   const GatherJob& jb = jobs.j[j];
@@ -76,9 +82,24 @@ __global__ void k_extrude_gather(int W, int m, int cap, const float* __restrict_
   if (r < m) {
     int phys = jb.head - m + r;
     if (phys < 0) phys += cap;
-    const float* src = buf + ((size_t)jb.screen * cap + phys) * W + c;
-    dst[0] = src[0];
-    if (two) dst[1] = src[1];
+    float* src = buf + ((size_t)jb.screen * cap + phys) * W + c;
+    if (prev && r == m - 1) {
+      float s0 = 0.f, s1 = 0.f;
+      for (int z = 0; z < prev_nz; ++z) {
+        const float* pz = prev + ((size_t)z * J + j) * W + c;
+        s0 += __ldcs(pz);
+        if (two) s1 += __ldcs(pz + 1);
+      }
+      src[0] = s0;
+      dst[0] = s0;
+      if (two) {
+        src[1] = s1;
+        dst[1] = s1;
+      }
+    } else {
+      dst[0] = src[0];
+      if (two) dst[1] = src[1];
+    }
   } else if (noise) {
     dst[0] = jb.bscale * noise[jb.noise_off + c];
     if (two) dst[1] = jb.bscale * noise[jb.noise_off + c + 1];
@@ -528,6 +549,26 @@ static int extrude_jobs(const char* who, const ExtrudeForm& form, int W, int m, 
   float* partial = (float*)((char*)work + first);
   const size_t op_group = form.terms ? tc_operator_bytes(W, m, 1, form.terms) : 0;
   std::vector<GatherJob> hj;
+  // The split-K reduce of a launch is deferred: when the next FP32 launch
+  // extrudes the same screens in the same order one row further, its gather
+  // makes the pending rows (they are its newest stencil rows); otherwise, and
+  // after the last launch, the reduce runs on its own.
+  struct Pending {
+    bool on = false;
+    int J = 0, nz = 0;
+    RingDst dst;
+  } pend;
+  auto flush = [&]() -> int {
+    if (!pend.on) return PT_OK;
+    {
+      ProfScope ps("k_extrude_reduce", s);
+      k_extrude_reduce<<<dim3((W + 255) / 256, pend.J), 256, 0, s>>>(W, pend.J, cap, pend.nz,
+                                                                    partial, pend.dst, buf);
+    }
+    count_launch_e(1);
+    pend.on = false;
+    return check_launch(who);
+  };
   int i = 0;
   while (i < n_jobs) {
     int e = i;
@@ -545,12 +586,24 @@ static int extrude_jobs(const char* who, const ExtrudeForm& form, int W, int m, 
         const int J = (int)std::min<size_t>(per_launch, hj.size() - b);
         JobParams jp;
         for (int q = 0; q < J; ++q) jp.j[q] = hj[b + q];
+        RingDst dst;
+        for (int q = 0; q < J; ++q) dst.d[q] = make_int2(jp.j[q].screen, jp.j[q].head);
+        // FP32 only: the tensor-core gather's threads each make 8 consecutive
+        // values, so summing the slices there costs more than the reduce
+        bool fuse = form.terms == 0 && pend.on && pend.J == J;
+        for (int q = 0; fuse && q < J; ++q)
+          fuse = pend.dst.d[q].x == dst.d[q].x && (pend.dst.d[q].y + 1) % cap == dst.d[q].y;
+        if (!fuse)
+          if (int rc = flush()) return rc;
+        const float* prev = fuse ? partial : nullptr;
+        const int prev_nz = fuse ? pend.nz : 0;
+        pend.on = false;
         int nz = 0;
         if (form.terms == 0) {
           {
             ProfScope ps("k_extrude_gather", s);
-            k_extrude_gather<<<dim3((W + 511) / 512, m + 1, J), 256, 0, s>>>(W, m, cap, buf, jp,
-                                                                               J, noise, X);
+            k_extrude_gather<<<dim3((W + 511) / 512, m + 1, J), 256, 0, s>>>(
+                W, m, cap, buf, jp, J, noise, X, prev, prev_nz);
           }
           const float* Mg = form.M + (size_t)kv.first * W * K;
           launch_gemm_tiled(W, K, J, Mg, X, partial, &nz, s);
@@ -567,19 +620,17 @@ static int extrude_jobs(const char* who, const ExtrudeForm& form, int W, int m, 
                                       Bt, partial, &nz, s))
             return rc;
         }
-        {
-          RingDst dst;
-          for (int q = 0; q < J; ++q) dst.d[q] = make_int2(jp.j[q].screen, jp.j[q].head);
-          ProfScope ps("k_extrude_reduce", s);
-          k_extrude_reduce<<<dim3((W + 255) / 256, J), 256, 0, s>>>(W, J, cap, nz, partial, dst, buf);
-        }
-        count_launch_e(form.terms ? 2 : 3);
+        pend.on = true;
+        pend.J = J;
+        pend.nz = nz;
+        pend.dst = dst;
+        count_launch_e(form.terms ? 1 : 2);
         if (int rc = check_launch(who)) return rc;
       }
     }
     i = e;
   }
-  return PT_OK;
+  return flush();
 }
 
 namespace pt {
