@@ -166,6 +166,11 @@ def tune_grid(grid, run: Callable[[], Any], batch: int, workload: str = "generat
     n = grid.ns
     out: Dict[str, Any] = {}
     pow2 = n >= 8 and (n & (n - 1)) == 0 and n <= 4096
+    # generate at n = 3 * 2^k (2^k in 64 .. 512) runs the Good-Thomas register
+    # transforms, which have no radix plan to choose
+    m3 = n // 3
+    if workload in ("generate", "ragged") and n % 3 == 0 and 64 <= m3 <= 512 and (m3 & (m3 - 1)) == 0:
+        return out
     if not pow2:
         default = grid_radices(grid)
         cands = radix_plans(n)

@@ -50,14 +50,16 @@ def test_autotune_is_cached_and_keeps_the_stream(tmp_path, monkeypatch):
     from pyturb_gb300 import PhaseScreen, tuning
 
     monkeypatch.setenv("PYTURB_GB300_TUNE_CACHE", str(tmp_path / "tune.json"))
-    ps = PhaseScreen(n=384, pixel_scale=0.02, r0=0.1, L0=20.0, subharmonics=2, seed=4)
+    ps = PhaseScreen(n=96, pixel_scale=0.02, r0=0.1, L0=20.0, subharmonics=2, seed=4)
     call = ps._rng.call
     choice = ps.autotune(4)
     assert ps._rng.call == call and "radices" in choice
     assert tuple(choice["radices"]) == tuning.grid_radices(ps._grid)
-    assert any("radices|n=384|batch=4" in k for k in tuning._load())
-    ps2 = PhaseScreen(n=384, pixel_scale=0.02, r0=0.1, L0=20.0, subharmonics=2, seed=4)
+    assert any("radices|n=96|batch=4" in k for k in tuning._load())
+    ps2 = PhaseScreen(n=96, pixel_scale=0.02, r0=0.1, L0=20.0, subharmonics=2, seed=4)
     assert ps2.autotune(4) == choice          # from the cache
+    # generate at 3 x 2^k (here 384) has no radix plan to tune
+    assert PhaseScreen(n=384, pixel_scale=0.02, r0=0.1, L0=20.0, seed=4).autotune(4) == {}
     with pytest.raises(ValueError):
         PhaseScreen(n=64, pixel_scale=0.02, r0=0.1, host_noise=np.random.default_rng).autotune(2)
 
