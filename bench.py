@@ -408,6 +408,44 @@ def run_reference(args, rank: int) -> None:
     print(json.dumps(line), flush=True)
 
 
+def run_case(args) -> None:
+    """One small, named workload for profiling a kernel family under ncu (no
+    JSON line): ``generate`` (``--n``, ``--count``, ``--calls``) or
+    ``extrude`` (``--width``, ``--screens``, ``--case-steps``, ``--form``)."""
+    import torch
+
+    import pyturb_gb300 as G
+    from pyturb_gb300.backend import NoiseStream, cuda_device
+    from pyturb_gb300.extrude import RingExtruder, build_extrusion
+
+    torch.cuda.set_device(0)
+    if args.case == "generate":
+        g = G.PhaseScreen(n=args.n, pixel_scale=8.0 / args.n, r0=0.15, L0=25.0,
+                          subharmonics=3, seed=1)
+        g.generate(args.count)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.calls):
+            g.generate(args.count)
+        torch.cuda.synchronize()
+        dt = (time.perf_counter() - t0) / max(1, args.calls)
+        print(f"generate n={args.n} count={args.count}: {dt * 1e6:.1f} us per call")
+        return
+    W, m, S = args.width, 2, args.screens
+    A, B = build_extrusion(W, m, 8.0 / 1024, 25.0)
+    ring = RingExtruder(W, m, args.case_steps + m + 8, [(A, B)], [0] * S, [1.0] * S,
+                        [NoiseStream(100 + s, None) for s in range(S)], form=args.form)
+    for s in range(S):
+        ring.seed_rows(s, torch.zeros((m, W), device=cuda_device()))
+    ring.extrude(np.ones(S, dtype=np.int32))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ring.extrude(np.full(S, args.case_steps - 1, dtype=np.int32))
+    torch.cuda.synchronize()
+    dt = (time.perf_counter() - t0) / max(1, args.case_steps - 1)
+    print(f"extrude form={args.form} W={W} screens={S}: {dt * 1e6:.1f} us per row step")
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -417,7 +455,19 @@ def main() -> None:
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extrude", action="store_true")
     ap.add_argument("--no-diff", action="store_true")
+    ap.add_argument("--case", choices=["generate", "extrude"], default=None,
+                    help="run one small named workload for profiling and exit")
+    ap.add_argument("--n", type=int, default=384)
+    ap.add_argument("--count", type=int, default=64)
+    ap.add_argument("--calls", type=int, default=4)
+    ap.add_argument("--width", type=int, default=1449)
+    ap.add_argument("--screens", type=int, default=144)
+    ap.add_argument("--case-steps", type=int, default=16)
+    ap.add_argument("--form", default="fp32", choices=["fp32", "bf16x2", "bf16x3"])
     args = ap.parse_args()
+    if args.case:
+        run_case(args)
+        return
     args.warmup = max(3, args.warmup)
 
     world = int(os.environ.get("WORLD_SIZE", "1"))

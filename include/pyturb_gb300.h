@@ -98,10 +98,13 @@ int pt_ifft2(const pt_grid* grid, const float* in, float* out, int batch, void* 
  * start-up): no grid plan and no workspace. Its scratch is a fixed 8 MiB
  * file-scope device array (plus a 1024-entry twiddle table) that every GPU
  * loading this library holds until exit. ns must be in [2, 1024]; larger
- * grids are rejected with PT_ERR_ARG. The first call on each device resolves
- * the arrays' addresses (cudaGetSymbolAddress) with that device current:
- * make it before any stream capture. All calls share the arrays, so calls
- * that overlap on the GPU race; nothing in them has to start at zero. */
+ * grids are rejected with PT_ERR_ARG. Every uncaptured call resolves the
+ * arrays' addresses (cudaGetSymbolAddress) on the current device; a call made
+ * while its stream is captured reuses the address of the last uncaptured call
+ * on that device, so make one call on each device before any stream capture.
+ * All calls share the arrays, so calls that overlap on the GPU (different
+ * streams or threads) race: serialise them, e.g. on one stream. Nothing in
+ * the arrays has to start at zero. */
 int pt_ifft2_noalloc(int ns, const float* in, float* out, int batch, void* stream);
 
 /* PhaseScreen.generate(count) (src/pyturb/fourier.py:233-282): coloured

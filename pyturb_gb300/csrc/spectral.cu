@@ -1579,9 +1579,12 @@ extern "C" int pt_boil_step(const pt_grid* g, int L, float* spectra, float* sh_c
 // not grow its footprint after start-up. Its scratch is not a caller
 // workspace but a file-scope device array of fixed size, which every GPU that
 // loads this library holds until the process exits. Host code cannot use the
-// array's name as a device address, so the first call on each device, with
-// that device current, resolves the addresses with cudaGetSymbolAddress and
-// caches them; make that first call before any stream capture. All calls
+// array's name as a device address, so every call resolves the addresses with
+// cudaGetSymbolAddress on the current device (a device reset or a rebuilt
+// primary context can move the arrays, so an address kept from an earlier
+// call could be stale). While the stream is being captured the address from
+// the last uncaptured call on that device is used instead; make one call on
+// each device before any stream capture. All calls
 // share the arrays and the last call's contents stay in them; the row pass
 // overwrites every scratch element it later reads and the twiddle table is
 // rewritten by each call, so nothing has to start at zero. Calls that
@@ -1605,13 +1608,16 @@ static std::mutex g_noalloc_mu;
 static NoAllocPtrs g_noalloc_ptrs[kNoAllocMaxDevices];
 static bool g_noalloc_ready[kNoAllocMaxDevices];
 
-static int noalloc_setup(NoAllocPtrs* out) {
+static int noalloc_setup(cudaStream_t s, NoAllocPtrs* out) {
   int dev = 0;
   if (int rc = check_cuda(cudaGetDevice(&dev), "pt_ifft2_noalloc: cudaGetDevice")) return rc;
   if (dev < 0 || dev >= kNoAllocMaxDevices)
     return fail(PT_ERR_UNSUPPORTED, "pt_ifft2_noalloc: device index beyond 63");
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (int rc = check_cuda(cudaStreamIsCapturing(s, &cap), "pt_ifft2_noalloc: cudaStreamIsCapturing"))
+    return rc;
   std::lock_guard<std::mutex> lk(g_noalloc_mu);
-  if (!g_noalloc_ready[dev]) {
+  if (cap == cudaStreamCaptureStatusNone || !g_noalloc_ready[dev]) {
     NoAllocPtrs p{};
     if (int rc = check_cuda(cudaGetSymbolAddress(&p.scratch, g_noalloc_scratch),
                             "pt_ifft2_noalloc: cudaGetSymbolAddress(scratch)"))
@@ -1643,8 +1649,8 @@ extern "C" int pt_ifft2_noalloc(int ns, const float* in, float* out, int batch, 
   if (!in || !out || batch < 0) return fail(PT_ERR_ARG, "pt_ifft2_noalloc: bad arguments");
   if (batch == 0) return PT_OK;
   NoAllocPtrs p{};
-  if (int rc = noalloc_setup(&p)) return rc;
   cudaStream_t s = (cudaStream_t)stream;
+  if (int rc = noalloc_setup(s, &p)) return rc;
   pt_grid g{};  // a stack view over the static arrays: nothing is allocated
   g.ns = ns;
   g.dx = 1.0;
@@ -1653,7 +1659,9 @@ extern "C" int pt_ifft2_noalloc(int ns, const float* in, float* out, int batch, 
   g.tw = (float2*)p.tw;
   float2* scratch = (float2*)p.scratch;
   const size_t per = (size_t)ns * ns;
-  const int chunk = (int)std::max<size_t>(1, kNoAllocScratchBytes / (per * sizeof(float2)));
+  // images per pass: what the scratch holds, and at most 65535 (grid y limit)
+  const int chunk = (int)std::min<size_t>(
+      65535, std::max<size_t>(1, kNoAllocScratchBytes / (per * sizeof(float2))));
   k_noalloc_twiddles<<<(ns + 127) / 128, 128, 0, s>>>(g.tw, ns);
   count_launch();
   const int rpc = rows_per_cta(ns), C = cols_per_cta(ns);

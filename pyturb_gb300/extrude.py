@@ -470,35 +470,3 @@ class ExtrudedAtmosphere:
                   stream_handle())
         return out
 
-
-def _main(argv=None) -> None:
-    """``python -m pyturb_gb300.extrude``: step ``--screens`` ring screens of
-    width ``--width`` for ``--steps`` row steps in one form and print the mean
-    step time (a compact driver for profiling the extrusion kernels)."""
-    import argparse
-    import time
-
-    ap = argparse.ArgumentParser(description=_main.__doc__)
-    ap.add_argument("--width", type=int, default=1449)
-    ap.add_argument("--screens", type=int, default=144)
-    ap.add_argument("--steps", type=int, default=16)
-    ap.add_argument("--form", default="bf16x2", choices=sorted(RingExtruder.FORMS))
-    a = ap.parse_args(argv)
-    torch = torch_module()
-    W, m, S = a.width, 2, a.screens
-    A, B = build_extrusion(W, m, 8.0 / 1024, 25.0)
-    ring = RingExtruder(W, m, a.steps + m + 8, [(A, B)], [0] * S, [1.0] * S,
-                        [NoiseStream(100 + s, None) for s in range(S)], form=a.form)
-    for s in range(S):
-        ring.seed_rows(s, torch.zeros((m, W), device=cuda_device()))
-    ring.extrude(np.ones(S, dtype=np.int32))
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    ring.extrude(np.full(S, a.steps - 1, dtype=np.int32))
-    torch.cuda.synchronize()
-    dt = (time.perf_counter() - t0) / max(1, a.steps - 1)
-    print(f"form={a.form} W={W} screens={S}: {dt * 1e6:.1f} us per row step")
-
-
-if __name__ == "__main__":
-    _main()

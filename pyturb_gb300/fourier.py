@@ -256,31 +256,3 @@ class PhaseScreen:
                 f"L0={self.L0}, subharmonics={self.subharmonics}{extra}, "
                 f"device={self.device!r}, dtype={self.dtype.name!r})")
 
-
-def _main(argv=None) -> None:
-    """``python -m pyturb_gb300.fourier``: ``--calls`` calls of
-    ``PhaseScreen.generate(--count)`` at ``--n``\\ ² (D = 8 m, r0 = 0.15 m,
-    L0 = 25 m, 3 subharmonic levels) and the mean time per call (a compact
-    driver for profiling the generate kernels)."""
-    import argparse
-    import time
-
-    ap = argparse.ArgumentParser(description=_main.__doc__)
-    ap.add_argument("--n", type=int, default=384)
-    ap.add_argument("--count", type=int, default=64)
-    ap.add_argument("--calls", type=int, default=4)
-    a = ap.parse_args(argv)
-    torch = torch_module()
-    g = PhaseScreen(n=a.n, pixel_scale=8.0 / a.n, r0=0.15, L0=25.0, subharmonics=3, seed=1)
-    g.generate(a.count)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(a.calls):
-        g.generate(a.count)
-    torch.cuda.synchronize()
-    dt = (time.perf_counter() - t0) / max(1, a.calls)
-    print(f"n={a.n} count={a.count}: {dt * 1e6:.1f} us per generate call")
-
-
-if __name__ == "__main__":
-    _main()

@@ -78,6 +78,18 @@ def test_no_alloc_ifft2_matches_planned_entry_point_on_two_calls():
         assert np.linalg.norm(got - exact) / np.linalg.norm(exact) < TOL
 
 
+def test_no_alloc_tiny_grids_with_more_images_than_one_launch():
+    """ns = 4 and ns = 3 (mixed-radix path) with 70000 images: the scratch
+    holds more than 65535 such images, so the call must split them into
+    launches that the grid limit allows."""
+    rng = np.random.default_rng(8)
+    for n in (4, 3):
+        x = _complex_input(rng, 70000, n)
+        got = _no_alloc(x)
+        exact = np.fft.ifft2(x) * (n * n)
+        assert np.linalg.norm(got - exact) / np.linalg.norm(exact) < TOL, n
+
+
 def test_no_alloc_rejects_grids_beyond_its_scratch():
     from pyturb_gb300 import _lib
 
