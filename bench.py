@@ -184,10 +184,12 @@ def bench_generate(torch, G):
     return reps * 64 / (e0.elapsed_time(e1) / 1000.0)
 
 
-def bench_extrude(torch, G, steps: int = 128):
-    """Assemat-Wilson extrusion at n = 1024, 9 layers x 16 realisations = 144 ring
-    screens (one [A | B] GEMM per row step, M = W, N = 144, K = 3W), and the fused
-    9-layer bilinear readout of one realisation at 1024^2."""
+def bench_extrude(torch, G, steps: int = 4096):
+    """Assemat-Wilson extrusion at n = 1024 with the configured stencil (2 full
+    rows + 2 sparse columns), 9 layers x 16 realisations = 144 ring screens,
+    4096 row steps (one [A | B] GEMM per row step: M = W, N = 144,
+    K = 3 W + 18), in each product form; the rows-only stencil beside it; and
+    the fused 9-layer bilinear readout of one realisation at 1024^2."""
     from pyturb_gb300 import _lib
     from pyturb_gb300.backend import NoiseStream, stream_handle
     from pyturb_gb300.extrude import RingExtruder
@@ -198,94 +200,88 @@ def bench_extrude(torch, G, steps: int = 128):
     frac = np.array(FRACTIONS) / np.sum(FRACTIONS)
     r0s = [R0 * cos_z ** 0.6 * f ** (-0.6) for f in frac]
     winds = [(v * np.cos(np.deg2rad(d)), v * np.sin(np.deg2rad(d))) for _, _, v, d in tab]
-    t0 = time.perf_counter()
-    ext = G.ExtrudedAtmosphere(n=n, pixel_scale=DIAM / n, layer_r0=r0s, layer_L0=[L0] * 9,
-                               layer_wind=winds, layer_altitude_los=[h / cos_z for h in HEIGHTS],
-                               interp="linear", seeds=list(range(9)))
-    setup_s = time.perf_counter() - t0
-    W, cap = ext.width, ext.capacity
     R = 16
     S = 9 * R
-    streams = [NoiseStream(100 + s, None) for s in range(S)]
-    ring = RingExtruder(W, 2, cap, [], [0] * S, [r ** (-5.0 / 6.0) for r in r0s] * R, streams,
-                        device_operator=ext._ring.M)
-    for s in range(S):  # every realisation starts from layer (s % 9)'s seeded rows
-        ring.buf[s].copy_(ext._ring.buf[s % 9])
-        ring.top[s] = ext._ring.top[s % 9]
-    ones = np.ones(S, dtype=np.int32)
-    for _ in range(3):
-        ring.extrude(ones)
-    torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record()
-    ring.extrude(steps * ones)
-    e1.record()
-    torch.cuda.synchronize()
-    step_s = e0.elapsed_time(e1) / 1000.0 / steps
-    flops = 2.0 * W * 3 * W * S
-    # per-kernel event timings of the same steps (a separate pass)
-    _lib.prof_report()
-    _lib.prof_enable(True)
-    ring.extrude(steps * ones)
-    torch.cuda.synchronize()
-    prof32 = _lib.prof_report()
-    _lib.prof_enable(False)
-    g32 = prof32.get("k_extrude_gemm", (1, float("nan")))
-    gemm32_s = g32[1] / g32[0] / 1e3
-    # the split-bf16 tensor-core forms from the same state
-    tc = {}
-    for form in ("bf16x2", "bf16x3"):
-        r2 = RingExtruder(W, 2, cap, [], [0] * S, [r ** (-5.0 / 6.0) for r in r0s] * R,
-                          [NoiseStream(100 + s, None) for s in range(S)],
-                          device_operator=ext._ring.M, form=form)
-        for s in range(S):
-            r2.buf[s].copy_(ext._ring.buf[s % 9])
-            r2.top[s] = ext._ring.top[s % 9]
-        for _ in range(3):
-            r2.extrude(ones)
+    ones = np.ones(S, dtype=np.int32)
+    out = {}
+    for columns in (2, 0):
         torch.cuda.synchronize()
-        e0.record()
-        r2.extrude(steps * ones)
-        e1.record()
+        t0 = time.perf_counter()
+        ext = G.ExtrudedAtmosphere(n=n, pixel_scale=DIAM / n, layer_r0=r0s, layer_L0=[L0] * 9,
+                                   layer_wind=winds,
+                                   layer_altitude_los=[h / cos_z for h in HEIGHTS],
+                                   interp="linear", seeds=list(range(9)),
+                                   stencil_columns=columns)
         torch.cuda.synchronize()
-        st = e0.elapsed_time(e1) / 1000.0 / steps
-        # per-kernel event timings in a separate pass (the events cost time)
-        _lib.prof_report()
-        _lib.prof_enable(True)
-        r2.extrude(steps * ones)
-        torch.cuda.synchronize()
-        prof = _lib.prof_report()
-        _lib.prof_enable(False)
-        g = prof.get("k_tc_gemm", (1, float("nan")))
-        tc[form] = {"row_steps_per_s": 1.0 / st, "effective_tflops": flops / st / 1e12,
-                    "gemm_us": g[1] / g[0] * 1e3,
-                    "gemm_tflops_issued": flops * (3 if form == "bf16x2" else 6)
-                    / (g[1] / g[0] / 1e3) / 1e12}
-        del r2
-    # readout: the 9 layers of one realisation, bilinear, at 1024^2
-    out = torch.empty((n, n), dtype=torch.float32, device="cuda")
-    ext.set_time(0.01)
-    params = ext.readout_params()
-    for _ in range(3):
-        ext.integrate(out=out)
-    torch.cuda.synchronize()
-    e0.record()
-    reps = 50
-    for _ in range(reps):
-        _lib.call("pt_readout", n, W, cap, 0, 9, params, ext._buf.data_ptr(), 1.0,
-                  out.data_ptr(), stream_handle())
-    e1.record()
-    torch.cuda.synchronize()
-    ro_s = e0.elapsed_time(e1) / 1000.0 / reps
-    return {"workload": f"n=1024, 9 layers x {R} realisations ({S} screens), W={W}, "
-                        f"stencil 2 rows, {steps} row steps timed; readout bilinear 9 layers",
-            "row_steps_per_s": 1.0 / step_s, "gemm_tflops": flops / step_s / 1e12,
-            "gemm_us": gemm32_s * 1e6, "gemm_kernel_tflops": flops / gemm32_s / 1e12,
-            "gemm_kernel_frac_of_fp32_nominal": flops / gemm32_s / 80.5e12,
-            "readout_frames_per_s": 1.0 / ro_s,
-            "readout_gbs_out": n * n * 4 / ro_s / 1e9, "host_setup_s": setup_s,
-            "note": "register-tiled split-K SIMT FP32 GEMM (default form); FP32 nominal "
-                    "80.5 TFLOP/s = 152 SMs x 128 lanes x 2 x 2.07 GHz", "tensor_core": tc}
+        setup_s = time.perf_counter() - t0
+        W, cap, sparse = ext.width, ext.capacity, ext.sparse
+        K = 3 * W + len(sparse)
+        flops = 2.0 * W * K * S
+        res = {"stencil": f"2 full rows + {columns} sparse columns ({len(sparse)} points)",
+               "W": W, "K": K, "host_setup_s": setup_s, "forms": {}}
+        for form in ("fp32", "bf16x2", "bf16x3"):
+            ring = RingExtruder(W, 2, cap, [], [0] * S, [r ** (-5.0 / 6.0) for r in r0s] * R,
+                                [NoiseStream(100 + s, None) for s in range(S)],
+                                device_operator=ext._ring.M, form=form, sparse=sparse)
+            for s in range(S):  # every realisation starts from layer (s % 9)'s seeded rows
+                ring.buf[s].copy_(ext._ring.buf[s % 9])
+                ring.top[s] = ext._ring.top[s % 9]
+            for _ in range(3):
+                ring.extrude(ones)
+            torch.cuda.synchronize()
+            e0.record()
+            ring.extrude(steps * ones)
+            e1.record()
+            torch.cuda.synchronize()
+            st = e0.elapsed_time(e1) / 1000.0 / steps
+            # per-kernel event timings in a separate pass (the events cost time)
+            _lib.prof_report()
+            _lib.prof_enable(True)
+            ring.extrude(256 * ones)
+            torch.cuda.synchronize()
+            prof = _lib.prof_report()
+            _lib.prof_enable(False)
+            g = prof.get("k_tc_gemm" if form != "fp32" else "k_extrude_gemm", (1, float("nan")))
+            gemm_s = g[1] / g[0] / 1e3
+            products = {"fp32": 1, "bf16x2": 3, "bf16x3": 6}[form]
+            res["forms"][form] = {
+                "row_steps_per_s": 1.0 / st, "effective_tflops": flops / st / 1e12,
+                "gemm_us": gemm_s * 1e6, "gemm_tflops_issued": products * flops / gemm_s / 1e12,
+                "kernel_share": {k: round(v[1] / max(1e-9, sum(x[1] for x in prof.values())), 4)
+                                 for k, v in prof.items()}}
+            del ring
+        f32 = res["forms"]["fp32"]
+        f32["gemm_kernel_frac_of_fp32_nominal"] = f32["gemm_tflops_issued"] / 80.5
+        if columns == 2:
+            # readout: the 9 layers of one realisation, bilinear, at 1024^2
+            o = torch.empty((n, n), dtype=torch.float32, device="cuda")
+            ext.set_time(0.01)
+            params = ext.readout_params()
+            for _ in range(3):
+                ext.integrate(out=o)
+            torch.cuda.synchronize()
+            e0.record()
+            reps = 50
+            for _ in range(reps):
+                _lib.call("pt_readout", n, W, cap, 0, 9, params, ext._buf.data_ptr(), 1.0,
+                          o.data_ptr(), stream_handle())
+            e1.record()
+            torch.cuda.synchronize()
+            ro_s = e0.elapsed_time(e1) / 1000.0 / reps
+            res["readout_frames_per_s"] = 1.0 / ro_s
+            res["readout_gbs_out"] = n * n * 4 / ro_s / 1e9
+        out["configured" if columns == 2 else "rows_only"] = res
+        del ext
+    cfg = out["configured"]
+    return {"workload": f"n=1024, 9 layers x {R} realisations ({S} screens), "
+                        f"W={cfg['W']}, stencil {cfg['stencil']}, {steps} row steps timed per "
+                        "form; readout bilinear 9 layers",
+            "row_steps_per_s": cfg["forms"]["fp32"]["row_steps_per_s"],
+            "note": "FP32 register-tiled split-K SIMT GEMM is the default form; FP32 nominal "
+                    "80.5 TFLOP/s = 152 SMs x 128 lanes x 2 x 2.07 GHz; operator built in FP64 "
+                    "on the GPU (host_setup_s includes seeding the 9 rings)",
+            **out}
 
 
 def bench_diff(torch, G, iters: int = 3):
@@ -461,7 +457,8 @@ def run_case(args) -> None:
 
     import pyturb_gb300 as G
     from pyturb_gb300.backend import NoiseStream, cuda_device
-    from pyturb_gb300.extrude import RingExtruder, build_extrusion
+    from pyturb_gb300.covariance import build_operator
+    from pyturb_gb300.extrude import RingExtruder
 
     torch.cuda.set_device(0)
     if args.case == "generate":
@@ -477,9 +474,10 @@ def run_case(args) -> None:
         print(f"generate n={args.n} count={args.count}: {dt * 1e6:.1f} us per call")
         return
     W, m, S = args.width, 2, args.screens
-    A, B = build_extrusion(W, m, 8.0 / 1024, 25.0)
-    ring = RingExtruder(W, m, args.case_steps + m + 8, [(A, B)], [0] * S, [1.0] * S,
-                        [NoiseStream(100 + s, None) for s in range(S)], form=args.form)
+    op = build_operator(W, m, 8.0 / 1024, 25.0)
+    ring = RingExtruder(W, m, args.case_steps + m + 8, [], [0] * S, [1.0] * S,
+                        [NoiseStream(100 + s, None) for s in range(S)], form=args.form,
+                        device_operator=op.M)
     for s in range(S):
         ring.seed_rows(s, torch.zeros((m, W), device=cuda_device()))
     ring.extrude(np.ones(S, dtype=np.int32))

@@ -27,7 +27,8 @@ enum {
   PT_OK = 0,
   PT_ERR_ARG = 1,         /* invalid argument (sizes, NULL pointers, workspace too small) */
   PT_ERR_CUDA = 2,        /* a CUDA runtime call or kernel launch failed */
-  PT_ERR_UNSUPPORTED = 3  /* valid request outside what this build implements */
+  PT_ERR_UNSUPPORTED = 3, /* valid request outside what this build implements */
+  PT_ERR_NUMERIC = 4      /* a factorisation met a non-positive pivot (see the message) */
 };
 
 /* Library version (major*10000 + minor*100 + patch). */
@@ -191,13 +192,47 @@ int pt_boil_step(const pt_grid* grid, int n_layers, float* spectra, float* sh_co
                  uint64_t seed, uint64_t call, void* stream);
 
 /* ------------------------------------------------------------------ extrusion
- * One Assemat-Wilson row step for a set of ring-buffer screens
+ * Sparse points appended to the m full stencil rows: point i is column
+ * column[i] of the row depth[i] rows behind the new row (m < depth < ring
+ * capacity). No reference counterpart: the reference stencil is
+ * `stencil_rows` full rows only (src/pyturb/extrude.py:272-275,
+ * src/pyturb/infinite.py:244-248). NULL (or count 0) = rows only. */
+#define PT_MAX_SPARSE 64
+typedef struct {
+  int32_t count;
+  int32_t depth[PT_MAX_SPARSE];
+  int32_t column[PT_MAX_SPARSE];
+} pt_sparse_stencil;
+
+/* The Assemat-Wilson operator in FP64 on the GPU, at unit r0: the joint
+ * von Karman covariance of the stencil (m rows of W pixels, then the sparse
+ * points) and the new row, one blocked Cholesky factorisation
+ * [[L, 0], [Y^T, Ls]] of it, and A = Y^T L^-1. Replaces phase_covariance,
+ * _spd_solve and build_extrusion (src/pyturb/infinite.py:54-117,
+ * src/pyturb/extrude.py:250-304) and the seed factor
+ * (src/pyturb/extrude.py:290-303). Outputs (device, each may be NULL but
+ * not both M and M64):
+ *   M (W, K) f32 and M64 (W, K) f64 = [A | Ls], K = (m+1) W + count
+ *     (Ls Ls^T is the conditional covariance the reference factors with
+ *     eigh; any factor gives the same statistics);
+ *   seed (Kz, Kz) f32 = L (L L^T = C_zz, Kz = m W + count), or NULL;
+ *   sigma (W, W) f64 = Ls Ls^T, or NULL.
+ * `jitter` adds jitter * C(0) to the stencil diagonal. A non-positive pivot
+ * of the stencil block returns PT_ERR_NUMERIC; pivots of the conditional
+ * block at or below 1e-13 C(0) zero their column. Synchronises `stream`. */
+size_t pt_aw_workspace_bytes(int W, int m, const pt_sparse_stencil* sparse);
+int pt_aw_build(int W, int m, const pt_sparse_stencil* sparse, double pixel_scale, double L0,
+                double jitter, float* M, double* M64, float* seed, double* sigma, void* work,
+                size_t work_bytes, void* stream);
+
+/* One Assemat-Wilson row step for a set of ring-buffer screens
  * (_ExtrudeLayer._extrude_one, src/pyturb/extrude.py:424-430;
  * InfinitePhaseScreen._extrude_one, src/pyturb/infinite.py:274-281):
- *   buf[s, head] = A_g . buf[s, head-m .. head-1] + B_g . (bscale * beta)
+ *   buf[s, head] = A_g . [buf[s, head-m .. head-1] ; sparse values]
+ *                  + B_g . (bscale * beta)
  * with ring rows taken modulo cap. M holds [A_g | B_unit_g] row-major,
- * shape (G, W, (m+1) W). Jobs are processed in `step` order; the jobs of
- * one step are independent (distinct screens). */
+ * shape (G, W, K), K = (m+1) W + sparse count. Jobs are processed in `step`
+ * order; the jobs of one step are independent (distinct screens). */
 typedef struct {
   int32_t screen;     /* slab of buf: (screen, cap, W) */
   int32_t group;      /* which [A | B] matrix */
@@ -210,7 +245,7 @@ typedef struct {
   int64_t noise_off;  /* element offset of this row's W normals in `noise` */
 } pt_extrude_job;
 
-size_t pt_extrude_workspace_bytes(int W, int m, int max_jobs_per_step);
+size_t pt_extrude_workspace_bytes(int W, int m, int n_sparse, int max_jobs_per_step);
 
 /* The same steps for S screens given as arrays (host): screen s extrudes
  * counts[s] rows, its k-th at virtual row top[s] + k (ring row modulo cap,
@@ -220,14 +255,15 @@ size_t pt_extrude_workspace_bytes(int W, int m, int max_jobs_per_step);
  * screen s+1, all step-k rows before step k+1). Replaces the per-row loop of
  * _ExtrudeLayer._ensure (src/pyturb/extrude.py:446-449) for all layers and
  * realisations at once. */
-int pt_extrude_batch(int W, int m, int cap, int n_groups, const float* M, float* buf, int S,
-                     const int32_t* group, const float* bscale, const uint64_t* key,
-                     int64_t* top, const int32_t* counts, const float* noise, void* work,
-                     size_t work_bytes, void* stream);
+int pt_extrude_batch(int W, int m, const pt_sparse_stencil* sparse, int cap, int n_groups,
+                     const float* M, float* buf, int S, const int32_t* group,
+                     const float* bscale, const uint64_t* key, int64_t* top,
+                     const int32_t* counts, const float* noise, void* work, size_t work_bytes,
+                     void* stream);
 
-int pt_extrude_rows(int W, int m, int cap, int n_groups, const float* M, float* buf,
-                    int n_jobs, const pt_extrude_job* jobs, const float* noise, void* work,
-                    size_t work_bytes, void* stream);
+int pt_extrude_rows(int W, int m, const pt_sparse_stencil* sparse, int cap, int n_groups,
+                    const float* M, float* buf, int n_jobs, const pt_extrude_job* jobs,
+                    const float* noise, void* work, size_t work_bytes, void* stream);
 
 /* Fused multi-layer rotated sub-pixel readout of the extrusion engine
  * (ExtrudedAtmosphere._integrate_fused_kernel / _integrate_looped,
@@ -275,19 +311,20 @@ int pt_ring_blend(int W, int cap, float* screen, int phys0, int h, float a, floa
  * the per-step operand [stencil ; bscale * beta] are split into `terms`
  * bf16 terms (x = x_hi + x_lo (+ x_mid); 2 terms: 3 products, 3 terms: 6)
  * and multiplied by tcgen05 MMAs into an fp32 accumulator in tensor memory.
- * pt_extrude_tc_prepare converts the FP32 (G, W, (m+1)W) operator M once
+ * pt_extrude_tc_prepare converts the FP32 (G, W, K) operator M once
  * into `tiles` (pt_extrude_tc_operator_bytes bytes, 256-byte aligned); the
  * workspace of pt_extrude_batch_tc is pt_extrude_tc_workspace_bytes (for the
  * largest number of screens stepped at once), 256-byte aligned. No reference
  * counterpart beyond the product it replaces. */
-size_t pt_extrude_tc_operator_bytes(int W, int m, int n_groups, int terms);
-int pt_extrude_tc_prepare(int W, int m, int n_groups, const float* M, int terms, void* tiles,
-                          size_t tiles_bytes, void* stream);
-size_t pt_extrude_tc_workspace_bytes(int W, int m, int max_jobs, int terms);
-int pt_extrude_batch_tc(int W, int m, int cap, int n_groups, const void* tiles, int terms,
-                        float* buf, int n_screens, const int32_t* group, const float* bscale,
-                        const uint64_t* key, int64_t* top, const int32_t* counts,
-                        const float* noise, void* work, size_t work_bytes, void* stream);
+size_t pt_extrude_tc_operator_bytes(int W, int m, int n_sparse, int n_groups, int terms);
+int pt_extrude_tc_prepare(int W, int m, int n_sparse, int n_groups, const float* M, int terms,
+                          void* tiles, size_t tiles_bytes, void* stream);
+size_t pt_extrude_tc_workspace_bytes(int W, int m, int n_sparse, int max_jobs, int terms);
+int pt_extrude_batch_tc(int W, int m, const pt_sparse_stencil* sparse, int cap, int n_groups,
+                        const void* tiles, int terms, float* buf, int n_screens,
+                        const int32_t* group, const float* bscale, const uint64_t* key,
+                        int64_t* top, const int32_t* counts, const float* noise, void* work,
+                        size_t work_bytes, void* stream);
 
 /* ---- differentiable multi-layer readout --------------------------------
  * out[b,t,d,i,j] = sum_l w[l] * bilerp(screens[b,l], u_r, u_c) with

@@ -28,10 +28,28 @@ def phase_covariance(r, r0, L0):
     return pref * core
 
 
-def build_extrusion(width, m, dx, L0, r0=1.0):
-    """``src/pyturb/extrude.py:250-304`` / ``src/pyturb/infinite.py:231-269``."""
+def sparse_points(width, m, columns, max_depth=None):
+    """Sparse stencil points ``(depth, column)`` beside the m full rows (no
+    reference counterpart; the package's rule restated): ``columns`` columns
+    at round((c + 1)(W - 1)/(columns + 1)), at every depth 2^j with
+    m < 2^j <= max_depth (default the largest power of two <= W)."""
+    if columns <= 0:
+        return []
+    dmax = max_depth if max_depth is not None else 1 << (int(width).bit_length() - 1)
+    depths = [1 << j for j in range(1, 31) if m < (1 << j) <= dmax]
+    cols = [int(round((c + 1) * (width - 1) / (columns + 1))) for c in range(columns)]
+    return [(d, c) for d in depths for c in cols]
+
+
+def build_extrusion(width, m, dx, L0, r0=1.0, sparse=()):
+    """``src/pyturb/extrude.py:250-304`` / ``src/pyturb/infinite.py:231-269``;
+    ``sparse`` appends points (column, m - depth) to the stencil (rows-only
+    when empty, as the reference)."""
     yz, xz = np.mgrid[0:m, 0:width]
     st = np.column_stack((xz.ravel(), yz.ravel())).astype(float)
+    if len(sparse):
+        extra = np.array([(c, m - d) for d, c in sparse], dtype=float)
+        st = np.concatenate([st, extra])
     nr = np.column_stack((np.arange(width, dtype=float), np.full(width, float(m))))
 
     def cov(a, b):
@@ -75,10 +93,18 @@ def compact_row_ring(buf, base, fill, m, first_readable_row):
     return base + keep_from, keep
 
 
-class _Layer:
-    """``src/pyturb/extrude.py:307-496`` (frozen flow)."""
+def _smooth_size(n):
+    """Smallest 2^a 3^b >= n."""
+    return min(v for v in (2 ** a * 3 ** b for a in range(40) for b in range(25)) if v >= n)
 
-    def __init__(self, n, W, dx, r0, L0, vx, vy, alt, m, rng, a, b_unit, cap, mag, fov):
+
+class _Layer:
+    """``src/pyturb/extrude.py:307-496`` (frozen flow). With sparse points the
+    buffer also keeps ``history`` older rows below the readable window and
+    the seed screen is ``seed_side`` square (cropped to W columns)."""
+
+    def __init__(self, n, W, dx, r0, L0, vx, vy, alt, m, rng, a, b_unit, cap, mag, fov,
+                 sparse=(), history=0, seed_side=None):
         self.n, self.W, self.dx, self.m, self.rng = n, W, dx, m, rng
         speed = float(np.hypot(vx, vy))
         self.speed = speed
@@ -97,17 +123,22 @@ class _Layer:
         self.cap = cap
         emin = self.amin - self.fov
         span = int(np.ceil(self.amax + self.fov)) - int(np.floor(emin)) + 3
-        self.base = int(np.floor(emin)) - 2
-        init = OraclePhaseScreen(W, dx, r0, L0, rng=rng).generate()
-        self.buf[:span] = init[:span]
-        self.fill = span
+        self.sparse = list(sparse)
+        self.depth = max([m] + [d for d, _ in self.sparse])
+        self.base = int(np.floor(emin)) - 2 - history
+        side = W if seed_side is None else seed_side
+        init = OraclePhaseScreen(side, dx, r0, L0, rng=rng).generate()
+        self.buf[:span + history] = init[:span + history, :W]
+        self.fill = span + history
         self.travel = 0.0
 
     def extrude_one(self):
         if self.fill == self.cap:
-            self.base, self.fill = compact_row_ring(self.buf, self.base, self.fill, self.m,
+            self.base, self.fill = compact_row_ring(self.buf, self.base, self.fill, self.depth,
                                                     self.amin - self.fov + self.travel)
         z = self.buf[self.fill - self.m:self.fill].ravel()
+        if self.sparse:
+            z = np.concatenate([z, [self.buf[self.fill - d, c] for d, c in self.sparse]])
         beta = self.rng.standard_normal(self.W)
         self.buf[self.fill] = self.a @ z + self.b @ beta
         self.fill += 1
@@ -129,7 +160,8 @@ class OracleExtruded:
 
     def __init__(self, n, pixel_scale, layer_r0, layer_L0, layer_wind, layer_altitude_los,
                  field_of_view_pix=0.0, stencil_rows=2, interp="cubic", lgs_altitude_los=None,
-                 seeds=None, rng_factory=np.random.default_rng, tau_boil=None, boil_seed=None):
+                 seeds=None, rng_factory=np.random.default_rng, tau_boil=None, boil_seed=None,
+                 stencil_columns=0, sparse_depth=None):
         self.n, self.dx, self.interp, self.m = int(n), float(pixel_scale), interp, stencil_rows
         L = len(layer_r0)
         fov = ([float(field_of_view_pix)] * L if np.ndim(field_of_view_pix) == 0
@@ -145,7 +177,10 @@ class OracleExtruded:
             exts.append(e)
             spans.append(int(np.ceil(e + fv)) - int(np.floor(-e - fv)) + 3)
         self.W = int(np.ceil(2.0 * max(exts) + 2.0 * max(fov))) + 4
-        self.cap = max(spans) + self.n + self.m + 32
+        self.sparse = sparse_points(self.W, self.m, stencil_columns, sparse_depth)
+        history = max([0] + [d for d, _ in self.sparse])
+        self.cap = max(spans) + self.n + self.m + 32 + history
+        side = self.W if not self.sparse else _smooth_size(max(self.W, max(spans) + history))
         cache = {}
         seeds = seeds if seeds is not None else [None] * L
         self.layers = []
@@ -153,10 +188,11 @@ class OracleExtruded:
                                                       layer_altitude_los, seeds, mags, fov):
             key = round(float(L0), 9)
             if key not in cache:
-                cache[key] = build_extrusion(self.W, self.m, self.dx, L0)
+                cache[key] = build_extrusion(self.W, self.m, self.dx, L0, sparse=self.sparse)
             a, b = cache[key]
             self.layers.append(_Layer(self.n, self.W, self.dx, r0, L0, vx, vy, alt, self.m,
-                                      rng_factory(sd), a, b, self.cap, mag, fv))
+                                      rng_factory(sd), a, b, self.cap, mag, fv, self.sparse,
+                                      history, side))
         # boiling (src/pyturb/extrude.py:472-496, 643-650, 695-753, the NumPy path)
         self.tau = [float("inf")] * L if tau_boil is None else [
             float("inf") if t is None else float(t) for t in tau_boil]

@@ -15,7 +15,8 @@ from typing import Any
 
 from . import _build
 
-PT_OK, PT_ERR_ARG, PT_ERR_CUDA, PT_ERR_UNSUPPORTED = 0, 1, 2, 3
+PT_OK, PT_ERR_ARG, PT_ERR_CUDA, PT_ERR_UNSUPPORTED, PT_ERR_NUMERIC = 0, 1, 2, 3, 4
+PT_MAX_SPARSE = 64
 
 _lock = threading.Lock()
 _lib = None
@@ -43,6 +44,31 @@ class ExtrudeJob(C.Structure):
         ("row", C.c_uint64),
         ("noise_off", C.c_int64),
     ]
+
+
+class SparseStencil(C.Structure):
+    """``pt_sparse_stencil``: sparse points (rows back, column) after the full rows."""
+
+    _fields_ = [
+        ("count", C.c_int32),
+        ("depth", C.c_int32 * PT_MAX_SPARSE),
+        ("column", C.c_int32 * PT_MAX_SPARSE),
+    ]
+
+
+def sparse_stencil(points):
+    """A ``SparseStencil`` for ``points`` = [(depth, column), ...], or None if empty."""
+    points = list(points)
+    if not points:
+        return None
+    if len(points) > PT_MAX_SPARSE:
+        raise ValueError(f"at most {PT_MAX_SPARSE} sparse stencil points")
+    st = SparseStencil()
+    st.count = len(points)
+    for i, (d, c) in enumerate(points):
+        st.depth[i] = int(d)
+        st.column[i] = int(c)
+    return st
 
 
 class ReadoutLayer(C.Structure):
@@ -85,11 +111,14 @@ SIGNATURES = {
     "pt_layers_translate": (i32, [vp, i32, vp, vp, dptr, dptr, vp, vp, vp]),
     "pt_lgs_zoom": (i32, [i32, i32, i32, i32, vp, vp, vp, f32, vp, vp]),
     "pt_boil_step": (i32, [vp, i32, vp, vp, vp, vp, vp, vp, f64, vp, vp, u64, u64, vp]),
-    "pt_extrude_workspace_bytes": (sz, [i32, i32, i32]),
-    "pt_extrude_rows": (i32, [i32, i32, i32, i32, vp, vp, i32, C.POINTER(ExtrudeJob), vp, vp,
-                              sz, vp]),
-    "pt_extrude_batch": (i32, [i32, i32, i32, i32, vp, vp, i32, vp, vp, vp, vp, vp, vp, vp, sz,
-                               vp]),
+    "pt_aw_workspace_bytes": (sz, [i32, i32, C.POINTER(SparseStencil)]),
+    "pt_aw_build": (i32, [i32, i32, C.POINTER(SparseStencil), f64, f64, f64, vp, vp, vp, vp, vp,
+                          sz, vp]),
+    "pt_extrude_workspace_bytes": (sz, [i32, i32, i32, i32]),
+    "pt_extrude_rows": (i32, [i32, i32, C.POINTER(SparseStencil), i32, i32, vp, vp, i32,
+                              C.POINTER(ExtrudeJob), vp, vp, sz, vp]),
+    "pt_extrude_batch": (i32, [i32, i32, C.POINTER(SparseStencil), i32, i32, vp, vp, i32, vp,
+                               vp, vp, vp, vp, vp, vp, sz, vp]),
     "pt_readout": (i32, [i32, i32, i32, i32, i32, C.POINTER(ReadoutLayer), vp, f32, vp, vp]),
     "pt_rows_sample": (i32, [i32, i32, i32, i32, i32, f64, vp, vp, vp]),
     "pt_lr_fix": (i32, [i32, i32, i32, i32, i32, vp, dptr, vp, vp]),
@@ -106,11 +135,11 @@ SIGNATURES = {
     "pt_tc_probe": (i32, [i32, i32, vp, vp, vp, vp]),
     "pt_fill_normals": (i32, [u64, u64, i32, i32, C.POINTER(f32), vp, vp]),
     "pt_ring_blend": (i32, [i32, i32, vp, i32, i32, f32, f32, vp, vp]),
-    "pt_extrude_tc_operator_bytes": (sz, [i32, i32, i32, i32]),
-    "pt_extrude_tc_prepare": (i32, [i32, i32, i32, vp, i32, vp, sz, vp]),
-    "pt_extrude_tc_workspace_bytes": (sz, [i32, i32, i32, i32]),
-    "pt_extrude_batch_tc": (i32, [i32, i32, i32, i32, vp, i32, vp, i32, vp, vp, vp, vp, vp, vp,
-                                  vp, sz, vp]),
+    "pt_extrude_tc_operator_bytes": (sz, [i32, i32, i32, i32, i32]),
+    "pt_extrude_tc_prepare": (i32, [i32, i32, i32, i32, vp, i32, vp, sz, vp]),
+    "pt_extrude_tc_workspace_bytes": (sz, [i32, i32, i32, i32, i32]),
+    "pt_extrude_batch_tc": (i32, [i32, i32, C.POINTER(SparseStencil), i32, i32, vp, i32, vp, i32,
+                                  vp, vp, vp, vp, vp, vp, vp, sz, vp]),
     "pt_synth_adj_pack": (i32, [i32, i32, i32, i32, f32, vp, vp, vp]),
     "pt_synth_adj_phasors": (i32, [i32, f64, i32, i32, vp, vp, vp, vp]),
     "pt_synth_adj_spectra": (i32, [i32, i32, i32, vp, vp, vp, vp, vp]),

@@ -57,29 +57,49 @@ struct JobParams {
 struct RingDst {
   int2 d[kJobsPerLaunch];
 };
+// Sparse stencil points (column, rows back from the new row), appended to the
+// m full rows in the operand: X = [m rows ; sparse values ; bscale * beta].
+struct SparseDev {
+  int n;
+  int depth[PT_MAX_SPARSE];
+  int col[PT_MAX_SPARSE];
+};
+__device__ __forceinline__ int ring_back(int head, int d, int cap) {
+  int p = head - d;
+  return p < 0 ? p + cap : p;
+}
 
 // X[j] for job j = blockIdx.z: block row blockIdx.y < m copies stencil row y
-// from the ring, row m holds bscale * beta; each thread makes two adjacent
-// columns (one Philox call for both noise values).
+// from the ring, row m holds bscale * beta, row m + 1 (only with sparse
+// points) the sparse values; each thread makes two adjacent columns (one
+// Philox call for both noise values).
 //
 // With `prev` set, the previous launch extruded the same screens one row
 // earlier and its split-K slices (prev_nz of them) are still unreduced: row
 // m - 1 here is that new row, summed in the order of k_extrude_reduce and
-// written both into the ring and into X (no thread reads that ring row).
+// written both into the ring and into X (no thread reads that ring row; the
+// sparse points lie deeper than m rows).
 __global__ void k_extrude_gather(int W, int m, int cap, float* __restrict__ buf,
-                                 const JobParams jobs, int J, const float* __restrict__ noise,
-                                 float* __restrict__ X, const float* __restrict__ prev,
-                                 int prev_nz) {
+                                 const JobParams jobs, int J, const SparseDev sp,
+                                 const float* __restrict__ noise, float* __restrict__ X,
+                                 const float* __restrict__ prev, int prev_nz) {
   const int j = blockIdx.z;
   if (j >= J) return;
   const GatherJob& jb = jobs.j[j];
-  const int K = (m + 1) * W;
+  const int K = (m + 1) * W + sp.n;
   const int r = blockIdx.y;
   const int c = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
+  if (r == m + 1) {  // sparse points
+    const float* slab = buf + (size_t)jb.screen * cap * W;
+    float* dst = X + (size_t)j * K + (size_t)m * W;
+    for (int e = c; e < c + 2 && e < sp.n; ++e)
+      dst[e] = slab[(size_t)ring_back(jb.head, sp.depth[e], cap) * W + sp.col[e]];
+    return;
+  }
   if (c >= W) return;
-  float* dst = X + (size_t)j * K + (size_t)r * W + c;
   const bool two = c + 1 < W;
   if (r < m) {
+    float* dst = X + (size_t)j * K + (size_t)r * W + c;
     int phys = jb.head - m + r;
     if (phys < 0) phys += cap;
     float* src = buf + ((size_t)jb.screen * cap + phys) * W + c;
@@ -100,7 +120,10 @@ __global__ void k_extrude_gather(int W, int m, int cap, float* __restrict__ buf,
       dst[0] = src[0];
       if (two) dst[1] = src[1];
     }
-  } else if (noise) {
+    return;
+  }
+  float* dst = X + (size_t)j * K + (size_t)m * W + sp.n + c;
+  if (noise) {
     dst[0] = jb.bscale * noise[jb.noise_off + c];
     if (two) dst[1] = jb.bscale * noise[jb.noise_off + c + 1];
   } else {
@@ -117,10 +140,12 @@ __global__ void k_extrude_gather(int W, int m, int cap, float* __restrict__ buf,
 // of a core matrix; consecutive threads take consecutive K groups of the same
 // job, so a warp reads one contiguous stretch of that job's ring rows.
 __global__ void k_tc_gather(int W, int m, int cap, const float* __restrict__ buf,
-                            const JobParams jobs, int J, int NP, int nkc, int terms,
-                            const float* __restrict__ noise, uint8_t* __restrict__ tiles) {
+                            const JobParams jobs, int J, const SparseDev sp, int NP, int nkc,
+                            int terms, const float* __restrict__ noise,
+                            uint8_t* __restrict__ tiles) {
   constexpr int Kc = tc::kTcKc;
-  const int K = (m + 1) * W;
+  const int mW = m * W, Kn = mW + sp.n;  // the noise section starts at Kn
+  const int K = Kn + W;
   const size_t tile = (size_t)NP * Kc * 2;
   const int groups = nkc * (Kc / 8);
   const size_t total = (size_t)groups * NP;
@@ -132,8 +157,7 @@ __global__ void k_tc_gather(int W, int m, int cap, const float* __restrict__ buf
     if (j < J) {
       const GatherJob& jb = jobs.j[j];
       const float* slab = buf + (size_t)jb.screen * cap * W;
-      // stencil row and column of k0 once; k0 is even, so noise pairs
-      // (c, c + 1) of one Philox call stay together unless a row ends
+      // stencil row and column of k0 once (valid while k < mW), advanced per value
       int r = k0 / W, c = k0 - r * W;
       const float* src = nullptr;
       auto row_src = [&](int rr) {
@@ -143,30 +167,34 @@ __global__ void k_tc_gather(int W, int m, int cap, const float* __restrict__ buf
       };
       if (r < m) src = row_src(r);
       float2 pn = make_float2(0.f, 0.f);
-      int pc = -2;  // column pair whose normals are in pn
+      int pc = -2;  // noise column pair whose normals are in pn
 #pragma unroll
       for (int q = 0; q < 8; ++q) {
+        const int k = k0 + q;
         float val = 0.f;
-        if (k0 + q < K) {
-          if (r < m) {
-            val = src[c];
-          } else if (noise) {
-            val = jb.bscale * noise[jb.noise_off + c];
+        if (k < mW) {
+          val = src[c];
+          if (++c == W) {
+            c = 0;
+            ++r;
+            if (r < m) src = row_src(r);
+          }
+        } else if (k < Kn) {
+          const int e = k - mW;
+          val = slab[(size_t)ring_back(jb.head, sp.depth[e], cap) * W + sp.col[e]];
+        } else if (k < K) {
+          const int cn = k - Kn;
+          if (noise) {
+            val = jb.bscale * noise[jb.noise_off + cn];
           } else {
-            if ((c >> 1) != pc) {
-              pn = philox_cnormal(jb.key, (uint64_t)(c >> 1), jb.row, kDomainExtrude);
-              pc = c >> 1;
+            if ((cn >> 1) != pc) {
+              pn = philox_cnormal(jb.key, (uint64_t)(cn >> 1), jb.row, kDomainExtrude);
+              pc = cn >> 1;
             }
-            val = jb.bscale * ((c & 1) ? pn.y : pn.x);
+            val = jb.bscale * ((cn & 1) ? pn.y : pn.x);
           }
         }
         v[q] = val;
-        if (++c == W) {
-          c = 0;
-          ++r;
-          if (r < m) src = row_src(r);
-          pc = -2;
-        }
       }
     } else {
 #pragma unroll
@@ -448,12 +476,31 @@ static inline size_t al256(size_t x) { return (x + 255) & ~size_t(255); }
 
 // tensor-core launchers (extrude_tc.cu)
 int tc_max_jobs(int terms);
-size_t tc_operator_bytes(int W, int m, int G, int terms);
-size_t tc_btile_bytes(int W, int m, int J, int terms);
-size_t tc_partial_floats(int W, int m, int J, int terms);
-int tc_prepare_launch(int W, int m, int G, const float* M, int terms, void* tiles, cudaStream_t s);
-int tc_gemm_launch(int W, int m, int J, int terms, const uint8_t* At, const uint8_t* Bt,
+size_t tc_operator_bytes(int W, int K, int G, int terms);
+size_t tc_btile_bytes(int W, int K, int J, int terms);
+size_t tc_partial_floats(int W, int K, int J, int terms);
+int tc_prepare_launch(int W, int K, int G, const float* M, int terms, void* tiles, cudaStream_t s);
+int tc_gemm_launch(int W, int K, int J, int terms, const uint8_t* At, const uint8_t* Bt,
                    float* partial, int* nz_out, cudaStream_t s);
+
+// The sparse points of a stencil, checked against the ring and the width.
+static int sparse_dev(const char* who, const pt_sparse_stencil* sp, int W, int m, int cap,
+                      SparseDev& out) {
+  out = SparseDev{};
+  if (!sp) return PT_OK;
+  if (sp->count < 0 || sp->count > PT_MAX_SPARSE)
+    return fail(PT_ERR_ARG, std::string(who) + ": sparse count must be in [0, 64]");
+  out.n = sp->count;
+  for (int i = 0; i < sp->count; ++i) {
+    if (sp->depth[i] <= m || (cap > 0 && sp->depth[i] >= cap) || sp->column[i] < 0 ||
+        sp->column[i] >= W)
+      return fail(PT_ERR_ARG, std::string(who) +
+                                  ": sparse points need m < depth < cap and 0 <= column < W");
+    out.depth[i] = sp->depth[i];
+    out.col[i] = sp->column[i];
+  }
+  return PT_OK;
+}
 
 // Jobs per thread of the tiled GEMM and its split-K: one wave of resident
 // CTAs, each slice at least 8 K steps long.
@@ -491,9 +538,9 @@ static int split_for(int W, int J, int K) {
 
 using namespace pt;
 
-extern "C" size_t pt_extrude_workspace_bytes(int W, int m, int max_jobs) {
-  if (W < 1 || m < 1 || max_jobs < 1) return 0;
-  const size_t K = (size_t)(m + 1) * W;
+extern "C" size_t pt_extrude_workspace_bytes(int W, int m, int n_sparse, int max_jobs) {
+  if (W < 1 || m < 1 || max_jobs < 1 || n_sparse < 0 || n_sparse > PT_MAX_SPARSE) return 0;
+  const size_t K = (size_t)(m + 1) * W + n_sparse;
   const size_t J = (size_t)std::min(max_jobs, kJobsPerLaunch);
   return al256(J * K * sizeof(float)) +
          al256((size_t)std::max(kMaxSplit, kMaxSplitTiled) * J * W * sizeof(float));
@@ -507,10 +554,13 @@ struct ExtrudeForm {
   const uint8_t* tiles;    // tensor-core operator tiles
 };
 
-static int extrude_jobs(const char* who, const ExtrudeForm& form, int W, int m, int cap, int G,
-                        float* buf, int n_jobs, const pt_extrude_job* jobs, const float* noise,
-                        void* work, size_t work_bytes, cudaStream_t s) {
+static int extrude_jobs(const char* who, const ExtrudeForm& form, int W, int m,
+                        const pt_sparse_stencil* sparse, int cap, int G, float* buf, int n_jobs,
+                        const pt_extrude_job* jobs, const float* noise, void* work,
+                        size_t work_bytes, cudaStream_t s) {
   if (W < 1 || m < 1 || cap < m + 1 || G < 1) return fail(PT_ERR_ARG, std::string(who) + ": bad sizes");
+  SparseDev sp;
+  if (int rc = sparse_dev(who, sparse, W, m, cap, sp)) return rc;
   if ((form.terms == 0 && !form.M) || (form.terms != 0 && !form.tiles) || !buf ||
       (n_jobs > 0 && !jobs))
     return fail(PT_ERR_ARG, std::string(who) + ": NULL pointer");
@@ -535,19 +585,19 @@ static int extrude_jobs(const char* who, const ExtrudeForm& form, int W, int m, 
       max_j = std::max(max_j, cur);
     }
   }
-  const size_t need = form.terms ? pt_extrude_tc_workspace_bytes(W, m, max_j, form.terms)
-                                 : pt_extrude_workspace_bytes(W, m, max_j);
+  const size_t need = form.terms ? pt_extrude_tc_workspace_bytes(W, m, sp.n, max_j, form.terms)
+                                 : pt_extrude_workspace_bytes(W, m, sp.n, max_j);
   if (!work || work_bytes < need) return fail(PT_ERR_ARG, std::string(who) + ": workspace too small");
-  const int K = (m + 1) * W;
+  const int K = (m + 1) * W + sp.n;
   const int per_launch = form.terms ? tc_max_jobs(form.terms) : kJobsPerLaunch;
   const int jcap = std::min(max_j, per_launch);
   // FP32: X (jcap, K) then partials; tensor cores: B tiles then partials
-  const size_t first = form.terms ? al256(tc_btile_bytes(W, m, jcap, form.terms))
+  const size_t first = form.terms ? al256(tc_btile_bytes(W, K, jcap, form.terms))
                                   : al256((size_t)jcap * K * sizeof(float));
   float* X = (float*)work;
   uint8_t* Bt = (uint8_t*)work;
   float* partial = (float*)((char*)work + first);
-  const size_t op_group = form.terms ? tc_operator_bytes(W, m, 1, form.terms) : 0;
+  const size_t op_group = form.terms ? tc_operator_bytes(W, K, 1, form.terms) : 0;
   std::vector<GatherJob> hj;
   // The split-K reduce of a launch is deferred: when the next FP32 launch
   // extrudes the same screens in the same order one row further, its gather
@@ -602,8 +652,8 @@ static int extrude_jobs(const char* who, const ExtrudeForm& form, int W, int m, 
         if (form.terms == 0) {
           {
             ProfScope ps("k_extrude_gather", s);
-            k_extrude_gather<<<dim3((W + 511) / 512, m + 1, J), 256, 0, s>>>(
-                W, m, cap, buf, jp, J, noise, X, prev, prev_nz);
+            k_extrude_gather<<<dim3((W + 511) / 512, m + 1 + (sp.n > 0), J), 256, 0, s>>>(
+                W, m, cap, buf, jp, J, sp, noise, X, prev, prev_nz);
           }
           const float* Mg = form.M + (size_t)kv.first * W * K;
           launch_gemm_tiled(W, K, J, Mg, X, partial, &nz, s);
@@ -614,9 +664,9 @@ static int extrude_jobs(const char* who, const ExtrudeForm& form, int W, int m, 
           {
             ProfScope ps("k_tc_gather", s);
             k_tc_gather<<<(unsigned)std::min<size_t>((items + 255) / 256, 152 * 8), 256, 0, s>>>(
-                W, m, cap, buf, jp, J, NP, nkc, form.terms, noise, Bt);
+                W, m, cap, buf, jp, J, sp, NP, nkc, form.terms, noise, Bt);
           }
-          if (int rc = tc_gemm_launch(W, m, J, form.terms, form.tiles + (size_t)kv.first * op_group,
+          if (int rc = tc_gemm_launch(W, K, J, form.terms, form.tiles + (size_t)kv.first * op_group,
                                       Bt, partial, &nz, s))
             return rc;
         }
@@ -734,11 +784,11 @@ extern "C" int pt_matmul_nt(int R, int K, int J, const float* M, const float* X,
   return check_launch("pt_matmul_nt");
 }
 
-extern "C" int pt_extrude_rows(int W, int m, int cap, int G, const float* M, float* buf,
-                               int n_jobs, const pt_extrude_job* jobs, const float* noise,
-                               void* work, size_t work_bytes, void* stream) {
-  return extrude_jobs("pt_extrude_rows", ExtrudeForm{0, M, nullptr}, W, m, cap, G, buf, n_jobs,
-                      jobs, noise, work, work_bytes, (cudaStream_t)stream);
+extern "C" int pt_extrude_rows(int W, int m, const pt_sparse_stencil* sparse, int cap, int G,
+                               const float* M, float* buf, int n_jobs, const pt_extrude_job* jobs,
+                               const float* noise, void* work, size_t work_bytes, void* stream) {
+  return extrude_jobs("pt_extrude_rows", ExtrudeForm{0, M, nullptr}, W, m, sparse, cap, G, buf,
+                      n_jobs, jobs, noise, work, work_bytes, (cudaStream_t)stream);
 }
 
 // Jobs of `counts[s]` row steps on every screen s, step-major (the order of
@@ -775,46 +825,58 @@ static int batch_jobs(const char* who, int W, int cap, int S, const int32_t* gro
   return PT_OK;
 }
 
-extern "C" int pt_extrude_batch(int W, int m, int cap, int n_groups, const float* M, float* buf,
-                                int S, const int32_t* group, const float* bscale,
-                                const uint64_t* key, int64_t* top, const int32_t* counts,
-                                const float* noise, void* work, size_t work_bytes,
-                                void* stream) {
+extern "C" int pt_extrude_batch(int W, int m, const pt_sparse_stencil* sparse, int cap,
+                                int n_groups, const float* M, float* buf, int S,
+                                const int32_t* group, const float* bscale, const uint64_t* key,
+                                int64_t* top, const int32_t* counts, const float* noise,
+                                void* work, size_t work_bytes, void* stream) {
   std::vector<pt_extrude_job> jobs;
   if (int rc = batch_jobs("pt_extrude_batch", W, cap, S, group, bscale, key, top, counts, jobs))
     return rc;
-  return extrude_jobs("pt_extrude_batch", ExtrudeForm{0, M, nullptr}, W, m, cap, n_groups, buf,
-                      (int)jobs.size(), jobs.data(), noise, work, work_bytes, (cudaStream_t)stream);
+  return extrude_jobs("pt_extrude_batch", ExtrudeForm{0, M, nullptr}, W, m, sparse, cap, n_groups,
+                      buf, (int)jobs.size(), jobs.data(), noise, work, work_bytes,
+                      (cudaStream_t)stream);
 }
 
-extern "C" size_t pt_extrude_tc_operator_bytes(int W, int m, int n_groups, int terms) {
-  if (W < 1 || m < 1 || n_groups < 1 || (terms != 2 && terms != 3)) return 0;
-  return tc_operator_bytes(W, m, n_groups, terms);
+static bool tc_sizes_ok(int W, int m, int n_sparse, int n, int terms) {
+  return W >= 1 && m >= 1 && n >= 1 && n_sparse >= 0 && n_sparse <= PT_MAX_SPARSE &&
+         (terms == 2 || terms == 3);
 }
 
-extern "C" int pt_extrude_tc_prepare(int W, int m, int n_groups, const float* M, int terms,
-                                     void* tiles, size_t tiles_bytes, void* stream) {
-  if (W < 1 || m < 1 || n_groups < 1) return fail(PT_ERR_ARG, "pt_extrude_tc_prepare: bad sizes");
+extern "C" size_t pt_extrude_tc_operator_bytes(int W, int m, int n_sparse, int n_groups,
+                                               int terms) {
+  if (!tc_sizes_ok(W, m, n_sparse, n_groups, terms)) return 0;
+  return tc_operator_bytes(W, (m + 1) * W + n_sparse, n_groups, terms);
+}
+
+extern "C" int pt_extrude_tc_prepare(int W, int m, int n_sparse, int n_groups, const float* M,
+                                     int terms, void* tiles, size_t tiles_bytes, void* stream) {
+  if (W < 1 || m < 1 || n_groups < 1 || n_sparse < 0 || n_sparse > PT_MAX_SPARSE)
+    return fail(PT_ERR_ARG, "pt_extrude_tc_prepare: bad sizes");
   if (terms != 2 && terms != 3) return fail(PT_ERR_ARG, "pt_extrude_tc_prepare: terms must be 2 or 3");
   if (!M || !tiles) return fail(PT_ERR_ARG, "pt_extrude_tc_prepare: NULL pointer");
-  if (tiles_bytes < tc_operator_bytes(W, m, n_groups, terms))
+  const int K = (m + 1) * W + n_sparse;
+  if (tiles_bytes < tc_operator_bytes(W, K, n_groups, terms))
     return fail(PT_ERR_ARG, "pt_extrude_tc_prepare: tile buffer too small");
   if (((uintptr_t)tiles & 255) != 0)
     return fail(PT_ERR_ARG, "pt_extrude_tc_prepare: tiles must be 256-byte aligned");
-  return tc_prepare_launch(W, m, n_groups, M, terms, tiles, (cudaStream_t)stream);
+  return tc_prepare_launch(W, K, n_groups, M, terms, tiles, (cudaStream_t)stream);
 }
 
-extern "C" size_t pt_extrude_tc_workspace_bytes(int W, int m, int max_jobs, int terms) {
-  if (W < 1 || m < 1 || max_jobs < 1 || (terms != 2 && terms != 3)) return 0;
+extern "C" size_t pt_extrude_tc_workspace_bytes(int W, int m, int n_sparse, int max_jobs,
+                                                int terms) {
+  if (!tc_sizes_ok(W, m, n_sparse, max_jobs, terms)) return 0;
   const int J = std::min(max_jobs, tc_max_jobs(terms));
-  return al256(tc_btile_bytes(W, m, J, terms)) + al256(tc_partial_floats(W, m, J, terms) * sizeof(float));
+  const int K = (m + 1) * W + n_sparse;
+  return al256(tc_btile_bytes(W, K, J, terms)) + al256(tc_partial_floats(W, K, J, terms) * sizeof(float));
 }
 
-extern "C" int pt_extrude_batch_tc(int W, int m, int cap, int n_groups, const void* tiles,
-                                   int terms, float* buf, int S, const int32_t* group,
-                                   const float* bscale, const uint64_t* key, int64_t* top,
-                                   const int32_t* counts, const float* noise, void* work,
-                                   size_t work_bytes, void* stream) {
+extern "C" int pt_extrude_batch_tc(int W, int m, const pt_sparse_stencil* sparse, int cap,
+                                   int n_groups, const void* tiles, int terms, float* buf, int S,
+                                   const int32_t* group, const float* bscale,
+                                   const uint64_t* key, int64_t* top, const int32_t* counts,
+                                   const float* noise, void* work, size_t work_bytes,
+                                   void* stream) {
   if (terms != 2 && terms != 3) return fail(PT_ERR_ARG, "pt_extrude_batch_tc: terms must be 2 or 3");
   if (work && ((uintptr_t)work & 255) != 0)
     return fail(PT_ERR_ARG, "pt_extrude_batch_tc: workspace must be 256-byte aligned");
@@ -824,7 +886,7 @@ extern "C" int pt_extrude_batch_tc(int W, int m, int cap, int n_groups, const vo
   if (int rc = batch_jobs("pt_extrude_batch_tc", W, cap, S, group, bscale, key, top, counts, jobs))
     return rc;
   return extrude_jobs("pt_extrude_batch_tc", ExtrudeForm{terms, nullptr, (const uint8_t*)tiles}, W,
-                      m, cap, n_groups, buf, (int)jobs.size(), jobs.data(), noise, work,
+                      m, sparse, cap, n_groups, buf, (int)jobs.size(), jobs.data(), noise, work,
                       work_bytes, (cudaStream_t)stream);
 }
 

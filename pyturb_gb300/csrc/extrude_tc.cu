@@ -4,8 +4,9 @@
 // The extrusion step is new_row = [A | B_unit] [stencil ; bscale * beta] for
 // every screen that needs a row (_ExtrudeLayer._extrude_one,
 // src/pyturb/extrude.py:424-430): a GEMM with M = W output pixels, N = screens
-// and K = (m + 1) W. Here both operands are split into bf16 terms, x = x_hi +
-// x_lo (+ x_mid), and the products accumulate in fp32 in tensor memory.
+// and K = (m + 1) W plus any sparse stencil points. Here both operands are
+// split into bf16 terms, x = x_hi + x_lo (+ x_mid), and the products
+// accumulate in fp32 in tensor memory.
 
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -225,9 +226,9 @@ struct TcShape {
   int K, MT, nkc, NP, cps, nz, stages;
   size_t stage_bytes;
 };
-TcShape tc_shape(int W, int m, int J, int terms) {
+TcShape tc_shape(int W, int K, int J, int terms) {
   TcShape t{};
-  t.K = (m + 1) * W;
+  t.K = K;
   t.MT = (W + kTcM - 1) / kTcM;
   t.nkc = (t.K + kTcKc - 1) / kTcKc;
   t.NP = std::max(16, (J + 15) / 16 * 16);
@@ -241,23 +242,23 @@ TcShape tc_shape(int W, int m, int J, int terms) {
   return t;
 }
 int tc_max_jobs(int terms) { return terms == 2 ? 192 : 160; }
-size_t tc_operator_bytes(int W, int m, int G, int terms) {
-  const TcShape t = tc_shape(W, m, 1, terms);
+size_t tc_operator_bytes(int W, int K, int G, int terms) {
+  const TcShape t = tc_shape(W, K, 1, terms);
   return (size_t)G * t.MT * t.nkc * terms * kTcTileA;
 }
-size_t tc_btile_bytes(int W, int m, int J, int terms) {
-  const TcShape t = tc_shape(W, m, J, terms);
+size_t tc_btile_bytes(int W, int K, int J, int terms) {
+  const TcShape t = tc_shape(W, K, J, terms);
   return (size_t)t.nkc * terms * t.NP * kTcKc * 2;
 }
 
-size_t tc_partial_floats(int W, int m, int J, int terms) {
-  const TcShape t = tc_shape(W, m, J, terms);
+size_t tc_partial_floats(int W, int K, int J, int terms) {
+  const TcShape t = tc_shape(W, K, J, terms);
   return (size_t)t.nz * J * W;
 }
 
-int tc_prepare_launch(int W, int m, int G, const float* M, int terms, void* tiles,
+int tc_prepare_launch(int W, int K, int G, const float* M, int terms, void* tiles,
                       cudaStream_t s) {
-  const TcShape t = tc_shape(W, m, 1, terms);
+  const TcShape t = tc_shape(W, K, 1, terms);
   const size_t total = (size_t)G * t.MT * kTcM * t.nkc * kTcKc;
   const int blocks = (int)std::min<size_t>((total + 255) / 256, 152 * 16);
   k_tc_prepare<<<blocks, 256, 0, s>>>(W, t.K, G, t.MT, t.nkc, terms, M, (uint8_t*)tiles);
@@ -265,9 +266,9 @@ int tc_prepare_launch(int W, int m, int G, const float* M, int terms, void* tile
   return check_launch("pt_extrude_tc_prepare");
 }
 
-int tc_gemm_launch(int W, int m, int J, int terms, const uint8_t* At, const uint8_t* Bt,
+int tc_gemm_launch(int W, int K, int J, int terms, const uint8_t* At, const uint8_t* Bt,
                    float* partial, int* nz_out, cudaStream_t s) {
-  const TcShape t = tc_shape(W, m, J, terms);
+  const TcShape t = tc_shape(W, K, J, terms);
   if (t.stages < 2) return fail(PT_ERR_UNSUPPORTED, "extrusion tensor-core form: too many jobs");
   const size_t smem = (size_t)t.stages * t.stage_bytes + 1024;
   dim3 grid(t.MT, t.nz);

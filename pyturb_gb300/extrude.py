@@ -1,11 +1,10 @@
 """Non-periodic frozen flow by Assemat-Wilson row extrusion on the GB300
 (drop-in for ``pyturb.extrude.ExtrudedAtmosphere``).
 
-Setup (host, FP64, once per outer scale — as in the reference): the von
-Karman covariances of the stencil rows and the new row, ``A = C_xz C_zz^-1``
-by Cholesky and ``B`` from the eigen-decomposition of the conditional
-covariance (``src/pyturb/extrude.py:250-304``), uploaded once as the float32
-operator ``M = [A | B_unit]`` (W x (m+1) W).
+Setup (device, FP64, once per outer scale): the operator ``M = [A | B_unit]``
+(W x K float32, K = (m+1) W plus any sparse stencil points) from one
+factorisation of the joint stencil/new-row covariance (``covariance.py``;
+the reference builds it on the host, ``src/pyturb/extrude.py:250-304``).
 
 Device state: one ``(L, cap, W)`` float32 slab of ring buffers. Virtual row v
 of a layer sits in physical row ``(v - v0) mod cap``, so the wind advances an
@@ -31,6 +30,7 @@ import numpy as np
 from . import _lib
 from .backend import NoiseStream, cuda_device, dptr, stream_handle, torch_module, upload
 from .config import ExtrusionConfig
+from .covariance import build_extrusion, build_operator, phase_covariance, sparse_points
 from .fourier import PhaseScreen
 
 __all__ = ["ExtrudedAtmosphere", "build_extrusion", "phase_covariance", "RingExtruder"]
@@ -38,77 +38,17 @@ __all__ = ["ExtrudedAtmosphere", "build_extrusion", "phase_covariance", "RingExt
 _INTERP = {"linear": 0, "cubic": 1, "lanczos": 2}
 
 
-def phase_covariance(r, r0: float, L0: float) -> np.ndarray:
-    """Von Karman phase covariance [rad^2] (``src/pyturb/infinite.py:88-117``):
-    ``C(r) = (L0/r0)^{5/3} 2^{-5/6} Gamma(11/6) / pi^{8/3} ((24/5) Gamma(6/5))^{5/6}
-    x^{5/6} K_{5/6}(x)``, ``x = 2 pi r / L0``, with the ``x -> 0`` limit
-    ``2^{-1/6} Gamma(5/6)``."""
-    from scipy.special import gamma, kv
-
-    if not np.isfinite(L0):
-        raise ValueError("phase_covariance requires a finite outer scale L0")
-    r = np.asarray(r, dtype=np.float64)
-    pref = ((L0 / r0) ** (5.0 / 3.0)
-            * (2.0 ** (-5.0 / 6.0) * gamma(11.0 / 6.0) / np.pi ** (8.0 / 3.0))
-            * ((24.0 / 5.0) * gamma(6.0 / 5.0)) ** (5.0 / 6.0))
-    x = 2.0 * np.pi * r / L0
-    core = np.full_like(x, 2.0 ** (-1.0 / 6.0) * gamma(5.0 / 6.0))
-    nz = x > 0
-    core[nz] = x[nz] ** (5.0 / 6.0) * kv(5.0 / 6.0, x[nz])
-    return pref * core
-
-
-def _spd_solve(spd: np.ndarray, rhs: np.ndarray) -> np.ndarray:
-    """Cholesky solve with a least-squares fallback (``src/pyturb/infinite.py:54-64``)."""
-    from scipy import linalg
-
-    try:
-        return linalg.cho_solve(linalg.cho_factor(spd), rhs)
-    except np.linalg.LinAlgError:
-        return np.linalg.lstsq(spd, rhs, rcond=None)[0]
-
-
-def build_extrusion(width: int, stencil_rows: int, pixel_scale: float, L0: float,
-                    r0: float = 1.0) -> Tuple[np.ndarray, np.ndarray]:
-    """FP64 ``(A (W, mW), B (W, W))`` for extruding one W-pixel row from the m
-    rows below it (``src/pyturb/extrude.py:250-304``, ``src/pyturb/infinite.py:231-269``).
-    Stencil rows sit at y = 0..m-1, the new row at y = m; the stencil is
-    flattened row-major, matching ``buf[fill-m:fill].ravel()``."""
-    m, n = int(stencil_rows), int(width)
-    yz, xz = np.mgrid[0:m, 0:n]
-    stencil = np.column_stack((xz.ravel(), yz.ravel())).astype(np.float64)
-    new_row = np.column_stack((np.arange(n, dtype=np.float64), np.full(n, float(m))))
-
-    def cov(a, b):
-        sep = np.hypot(a[:, None, 0] - b[None, :, 0], a[:, None, 1] - b[None, :, 1])
-        return phase_covariance(sep * pixel_scale, r0, L0)
-
-    c_zz = cov(stencil, stencil)
-    c_xz = cov(new_row, stencil)
-    c_xx = cov(new_row, new_row)
-    a = _spd_solve(c_zz, c_xz.T).T
-    res = c_xx - a @ c_xz.T
-    res = (res + res.T) / 2.0
-    w, v = np.linalg.eigh(res)
-    b = v * np.sqrt(np.clip(w, 0.0, None))
-    return a, b
-
-
-def seed_factor(width: int, stencil_rows: int, pixel_scale: float, L0: float) -> np.ndarray:
-    """FP64 ``S`` with ``S S^T = C_zz`` (unit r0) for the m stencil rows: the
-    seed of boiling's fresh windows (``src/pyturb/extrude.py:290-303``),
-    Cholesky of the symmetrised covariance or an eigen square root."""
-    m, n = int(stencil_rows), int(width)
-    yz, xz = np.mgrid[0:m, 0:n]
-    st = np.column_stack((xz.ravel(), yz.ravel())).astype(np.float64)
-    sep = np.hypot(st[:, None, 0] - st[None, :, 0], st[:, None, 1] - st[None, :, 1])
-    c_zz = phase_covariance(sep * pixel_scale, 1.0, L0)
-    c_zz = (c_zz + c_zz.T) / 2.0
-    try:
-        return np.linalg.cholesky(c_zz)
-    except np.linalg.LinAlgError:
-        w, v = np.linalg.eigh(c_zz)
-        return v * np.sqrt(np.clip(w, 0.0, None))
+def _smooth_size(n: int) -> int:
+    """Smallest 2^a 3^b >= n (a fast transform size for the seed screen)."""
+    best = 1 << max(0, int(n - 1).bit_length())
+    p3 = 1
+    while p3 < 2 * n:
+        v = p3
+        while v < n:
+            v *= 2
+        best = min(best, v)
+        p3 *= 3
+    return best
 
 
 class _RowQueue:
@@ -137,12 +77,14 @@ def along_extent_and_span(n: int, vx: float, vy: float, mag: float,
     return ext, span
 
 
-def compact_bounds(base: int, fill: int, m: int, first_readable_row: float) -> Tuple[int, int]:
+def compact_bounds(base: int, fill: int, depth: int,
+                   first_readable_row: float) -> Tuple[int, int]:
     """New ``(base, fill)`` after the reference's ring compaction
     (``src/pyturb/ring.py:9-28``): rows below the readable window and the
-    stencil are dropped, at least one."""
+    stencil (the last ``depth`` rows: the m full rows, or as deep as the
+    sparse points reach) are dropped, at least one."""
     target = int(floor(first_readable_row)) - 1
-    stencil = base + fill - m
+    stencil = base + fill - depth
     keep_from = max(1, min(target, stencil) - base)
     return base + keep_from, fill - keep_from
 
@@ -151,28 +93,43 @@ class RingExtruder:
     """The device ring slabs plus the per-screen host bookkeeping.
 
     ``screens`` independent ring buffers of ``cap`` rows x ``W`` columns; screen
-    s uses operator group ``groups[s]`` scaled by ``bscale[s]``."""
+    s uses operator group ``groups[s]`` scaled by ``bscale[s]``. ``sparse``
+    lists the stencil's sparse points ``(depth, column)`` after its ``m`` full
+    rows (none: the reference's rows-only stencil). ``operators`` holds host
+    ``(A, B)`` pairs, or ``device_operator`` an existing ``(G, W, K)``
+    float32 CUDA tensor, K = (m + 1) W + len(sparse)."""
 
     FORMS = {"fp32": 0, "bf16x2": 2, "bf16x3": 3}
 
     def __init__(self, W: int, m: int, cap: int, operators: List[Tuple[np.ndarray, np.ndarray]],
                  groups: Sequence[int], bscale: Sequence[float], streams: Sequence[NoiseStream],
-                 device_operator=None, form: str = "fp32"):
+                 device_operator=None, form: str = "fp32",
+                 sparse: Sequence[Tuple[int, int]] = ()):
         torch = torch_module()
         if form not in self.FORMS:
             raise ValueError(f"form must be one of {sorted(self.FORMS)}, got {form!r}")
         self.form = form
         self.terms = self.FORMS[form]
         self.W, self.m, self.cap = int(W), int(m), int(cap)
+        self.sparse = [(int(d), int(c)) for d, c in sparse]
+        self.ns = len(self.sparse)
+        self._stencil = _lib.sparse_stencil(self.sparse)
+        self._sp = C.byref(self._stencil) if self._stencil is not None else None
+        self.depth = max([self.m] + [d for d, _ in self.sparse])
+        if self.depth >= self.cap:
+            raise ValueError("the ring must hold more rows than the stencil reaches back")
         self.S = len(groups)
         self.groups = [int(g) for g in groups]
         self.bscale = [float(b) for b in bscale]
         self.streams = list(streams)
-        if device_operator is not None:  # an existing (G, W, (m+1)W) float32 CUDA tensor
-            self.M = device_operator
+        if device_operator is not None:
+            self.M = device_operator if device_operator.dim() == 3 else device_operator[None]
         else:
             M = np.stack([np.concatenate([a, b], axis=1) for a, b in operators])
             self.M = upload(M)
+        if self.M.shape[1:] != (self.W, (self.m + 1) * self.W + self.ns):
+            raise ValueError(f"operator shape {tuple(self.M.shape)} does not match W={self.W}, "
+                             f"m={self.m} and {self.ns} sparse points")
         self.G = int(self.M.shape[0])
         self.buf = torch.empty((self.S, self.cap, self.W), dtype=torch.float32,
                                device=cuda_device())
@@ -186,19 +143,20 @@ class RingExtruder:
         self.tiles = None
         if self.terms:
             # the operator split into bf16 terms, tiled for the tensor cores (once)
-            nbytes = int(_lib.load().pt_extrude_tc_operator_bytes(self.W, self.m, self.G,
-                                                                  self.terms))
+            nbytes = int(_lib.load().pt_extrude_tc_operator_bytes(self.W, self.m, self.ns,
+                                                                  self.G, self.terms))
             self.tiles = torch.empty(nbytes, dtype=torch.uint8, device=cuda_device())
-            _lib.call("pt_extrude_tc_prepare", self.W, self.m, self.G, dptr(self.M), self.terms,
-                      dptr(self.tiles), nbytes, stream_handle())
+            _lib.call("pt_extrude_tc_prepare", self.W, self.m, self.ns, self.G, dptr(self.M),
+                      self.terms, dptr(self.tiles), nbytes, stream_handle())
 
     def _ensure_work(self, jobs_per_step: int) -> None:
         lib = _lib.load()
         if self.terms:
-            need = int(lib.pt_extrude_tc_workspace_bytes(self.W, self.m, max(1, jobs_per_step),
-                                                         self.terms))
+            need = int(lib.pt_extrude_tc_workspace_bytes(self.W, self.m, self.ns,
+                                                         max(1, jobs_per_step), self.terms))
         else:
-            need = int(lib.pt_extrude_workspace_bytes(self.W, self.m, max(1, jobs_per_step)))
+            need = int(lib.pt_extrude_workspace_bytes(self.W, self.m, self.ns,
+                                                      max(1, jobs_per_step)))
         if need > self.work_bytes:
             torch = torch_module()
             self.work = torch.empty(need, dtype=torch.uint8, device=cuda_device())
@@ -225,13 +183,13 @@ class RingExtruder:
         self._ensure_work(int((counts > 0).sum()))
         ptr = lambda a: a.ctypes.data  # noqa: E731
         if self.terms:
-            _lib.call("pt_extrude_batch_tc", self.W, self.m, self.cap, self.G, dptr(self.tiles),
-                      self.terms, dptr(self.buf), self.S, ptr(self._group), ptr(self._bscale),
-                      ptr(self._key), ptr(self.top), ptr(counts), dptr(noise), dptr(self.work),
-                      self.work_bytes, stream_handle())
+            _lib.call("pt_extrude_batch_tc", self.W, self.m, self._sp, self.cap, self.G,
+                      dptr(self.tiles), self.terms, dptr(self.buf), self.S, ptr(self._group),
+                      ptr(self._bscale), ptr(self._key), ptr(self.top), ptr(counts), dptr(noise),
+                      dptr(self.work), self.work_bytes, stream_handle())
         else:
-            _lib.call("pt_extrude_batch", self.W, self.m, self.cap, self.G, dptr(self.M),
-                      dptr(self.buf), self.S, ptr(self._group), ptr(self._bscale),
+            _lib.call("pt_extrude_batch", self.W, self.m, self._sp, self.cap, self.G,
+                      dptr(self.M), dptr(self.buf), self.S, ptr(self._group), ptr(self._bscale),
                       ptr(self._key), ptr(self.top), ptr(counts), dptr(noise), dptr(self.work),
                       self.work_bytes, stream_handle())
 
@@ -239,7 +197,7 @@ class RingExtruder:
 class _LayerGeom:
     """Per-layer geometry and reference bookkeeping (``src/pyturb/extrude.py:307-496``)."""
 
-    def __init__(self, n, W, dx, vx, vy, altitude_los, m, mag, fov_margin_pix):
+    def __init__(self, n, W, dx, vx, vy, altitude_los, m, mag, fov_margin_pix, history=0):
         speed = float(np.hypot(vx, vy))
         self.speed = speed
         self.cos = vx / speed if speed > 0 else 1.0
@@ -253,9 +211,12 @@ class _LayerGeom:
         self.fov = float(fov_margin_pix)
         extent_min = self.along_min - self.fov
         self.span = int(np.ceil(self.along_max + self.fov)) - int(np.floor(extent_min)) + 3
-        self.base = int(np.floor(extent_min)) - 2  # virtual row of buffer row 0
+        # `history` older rows sit below the readable window for a sparse
+        # stencil's deepest points (none for the rows-only stencil)
+        self.history = int(history)
+        self.base = int(np.floor(extent_min)) - 2 - self.history  # virtual row of buffer row 0
         self.v0 = self.base                         # virtual row of ring row 0
-        self.fill = self.span
+        self.fill = self.span + self.history
         self.travel = 0.0
         self.m = m
 
@@ -268,10 +229,17 @@ class _LayerGeom:
 class ExtrudedAtmosphere:
     """Multi-layer extrusion engine (``src/pyturb/extrude.py:499-915``).
 
-    Constructor as the reference's plus ``host_noise`` (parity mode) and
-    ``extrude_form``: ``"fp32"`` (FP32 SIMT products, the default),
-    ``"bf16x2"`` or ``"bf16x3"`` (operands split into 2 or 3 bf16 terms and
-    multiplied on the tensor cores with an fp32 accumulator).
+    Constructor as the reference's plus
+    - ``host_noise`` (parity mode: the reference's draw order, and the
+      reference's eigen-square-root ``B``);
+    - ``extrude_form``: ``"fp32"`` (FP32 SIMT products, the default),
+      ``"bf16x2"`` or ``"bf16x3"`` (operands split into 2 or 3 bf16 terms and
+      multiplied on the tensor cores with an fp32 accumulator);
+    - ``stencil_columns`` (default 0): sparse stencil columns beside the
+      ``stencil_rows`` full rows, each sampled at depths 4, 8, 16, ... up to
+      ``sparse_depth`` rows back (default: the largest power of two not above
+      the buffer width). ``stencil_rows=2, stencil_columns=2`` is the
+      "2 full rows + 2 sparse columns" stencil. The reference has rows only.
     :meth:`integrate` returns a float32 CUDA tensor ``(n, n)``.
     """
 
@@ -283,7 +251,8 @@ class ExtrudedAtmosphere:
                  lgs_altitude_los: Optional[float] = None, device: str = "gpu",
                  dtype: Any = "float32", seeds: Optional[Sequence[Any]] = None,
                  tau_boil: Optional[Sequence[float]] = None, boil_seed: Optional[Any] = None,
-                 host_noise=None, extrude_form: str = "fp32") -> None:
+                 host_noise=None, extrude_form: str = "fp32", stencil_columns: int = 0,
+                 sparse_depth: Optional[int] = None) -> None:
         config = ExtrusionConfig.create(
             n, pixel_scale, layer_r0, layer_L0, layer_wind, layer_altitude_los,
             field_of_view_pix, stencil_rows, interp, lgs_altitude_los, device, dtype, seeds,
@@ -306,44 +275,61 @@ class ExtrudedAtmosphere:
             extents.append(e)
             spans.append(s)
         self.width = int(np.ceil(2.0 * max(extents) + 2.0 * max(config.field_of_view_pix))) + 4
-        self.capacity = max(spans) + self.n + self.m + 32
         W = self.width
+        if (not isinstance(stencil_columns, (int, np.integer)) or isinstance(stencil_columns, bool)
+                or stencil_columns < 0):
+            raise ValueError("stencil_columns must be a non-negative integer")
+        self.sparse = sparse_points(W, self.m, int(stencil_columns), sparse_depth)
+        history = max([0] + [d for d, _ in self.sparse])
+        self.capacity = max(spans) + self.n + self.m + 32 + history
+        self._tau = [float(t) for t in config.tau_boil]
+        self.boiling = any(np.isfinite(t) for t in self._tau)
+        if self.boiling and self.sparse:
+            raise ValueError("boiling supports the rows-only stencil (stencil_columns=0)")
 
+        # one FP64 device build per distinct outer scale; the reference's
+        # eigen-square-root B in the parity mode, the build's Cholesky factor
+        # otherwise (the same conditional covariance)
         op_index: dict = {}
-        operators = []
+        ops = []
         groups = []
         for L0 in config.layer_L0:
             key = round(float(L0), 9)
             if key not in op_index:
-                op_index[key] = len(operators)
-                operators.append(build_extrusion(W, self.m, self.dx, float(L0)))
+                op_index[key] = len(ops)
+                ops.append(build_operator(W, self.m, self.dx, float(L0), self.sparse,
+                                          b_factor="eigh" if host_noise is not None
+                                          else "cholesky", want_seed=self.boiling))
             groups.append(op_index[key])
         streams = [NoiseStream(s, host_noise) for s in config.seeds]
         self._streams = streams
         self.layers: List[_LayerGeom] = []
         for (vx, vy), alt, mag, fov in zip(config.layer_wind, config.layer_altitude_los, mags,
                                            config.field_of_view_pix):
-            self.layers.append(_LayerGeom(self.n, W, self.dx, vx, vy, alt, self.m, mag, fov))
+            self.layers.append(_LayerGeom(self.n, W, self.dx, vx, vy, alt, self.m, mag, fov,
+                                          history))
         bscale = [float(r0) ** (-5.0 / 6.0) for r0 in config.layer_r0]
-        self._ring = RingExtruder(W, self.m, self.capacity, operators, groups, bscale, streams,
-                                  form=extrude_form)
-        # seed each ring with a von Karman screen from the layer's own stream
+        torch = torch_module()
+        self._ring = RingExtruder(W, self.m, self.capacity, [], groups, bscale, streams,
+                                  device_operator=torch.stack([op.M for op in ops]),
+                                  form=extrude_form, sparse=self.sparse)
+        # seed each ring with a von Karman screen from the layer's own stream:
+        # a W x W screen for the rows-only stencil (as the reference), a taller
+        # one cropped to W columns when sparse points need older rows
+        side = W if not self.sparse else _smooth_size(max(W, max(spans) + history))
         for i, (r0, L0) in enumerate(zip(config.layer_r0, config.layer_L0)):
-            gen = PhaseScreen(n=W, pixel_scale=self.dx, r0=float(r0), L0=float(L0),
+            gen = PhaseScreen(n=side, pixel_scale=self.dx, r0=float(r0), L0=float(L0),
                               _stream=streams[i], host_noise=host_noise)
             init = gen.generate()
-            self._ring.seed_rows(i, init[: self.layers[i].span])
+            ly = self.layers[i]
+            self._ring.seed_rows(i, init[: ly.span + ly.history, :W])
             del gen
         # boiling (src/pyturb/extrude.py:472-496, 586-650, 695-753)
-        self._tau = [float(t) for t in config.tau_boil]
-        self.boiling = any(np.isfinite(t) for t in self._tau)
         if self.boiling:
             self._boil_layers = [i for i, t in enumerate(self._tau) if np.isfinite(t)]
             self._host_boil = host_noise is not None
             self._boil = NoiseStream(config.boil_seed, host_noise)
-            seeds = [seed_factor(W, self.m, self.dx, a_L0) for a_L0 in
-                     sorted(op_index, key=op_index.get)]
-            self._S = upload(np.stack(seeds))                     # (G, mW, mW)
+            self._S = torch.stack([op.S for op in ops])          # (G, mW, mW)
             self._groups = groups
             self._bscale = bscale
             self._queues = [_RowQueue(self._host_boil) for _ in self._boil_layers]
@@ -363,7 +349,7 @@ class ExtrudedAtmosphere:
         count = 0
         while ly.base + ly.fill - 1 < top:
             if ly.fill == self.capacity:
-                ly.base, ly.fill = compact_bounds(ly.base, ly.fill, ly.m,
+                ly.base, ly.fill = compact_bounds(ly.base, ly.fill, self._ring.depth,
                                                   ly.along_min - ly.fov + ly.travel)
             ly.fill += 1
             count += 1

@@ -44,6 +44,7 @@ def test_library_is_built_for_sm_103a_only():
 def test_struct_layouts_match_header():
     assert C.sizeof(_lib.ExtrudeJob) == 48
     assert C.sizeof(_lib.ReadoutLayer) == 56
+    assert C.sizeof(_lib.SparseStencil) == 4 + 2 * 4 * _lib.PT_MAX_SPARSE
 
 
 def _status(name, *args):
@@ -62,13 +63,35 @@ def test_argument_errors_before_device_work():
     assert _status("pt_readout", 0, 8, 8, 1, 1, None, None, 1.0, None, None) == _lib.PT_ERR_ARG
     assert _status("pt_lgs_zoom", 1, 8, 8, 7, None, None, None, 1.0, None, None) == _lib.PT_ERR_ARG
     assert _status("pt_rows_sample", 8, 8, 3, 0, 4, 0.0, None, None, None) == _lib.PT_ERR_ARG
-    assert _status("pt_extrude_rows", 0, 2, 8, 1, None, None, 0, None, None, None, 0,
+    assert _status("pt_extrude_rows", 0, 2, None, 8, 1, None, None, 0, None, None, None, 0,
                    None) == _lib.PT_ERR_ARG
+    # sparse points must lie deeper than the full rows and inside the width
+    bad = _lib.sparse_stencil([(2, 5)])
+    assert _status("pt_extrude_batch", 64, 2, C.byref(bad), 128, 1, C.c_void_p(256),
+                   C.c_void_p(256), 1, None, None, None, None, None, None, None, 0,
+                   None) == _lib.PT_ERR_ARG
+    assert _status("pt_aw_build", 0, 2, None, 0.1, 25.0, 0.0, None, None, None, None, None, 0,
+                   None) == _lib.PT_ERR_ARG
+    assert _status("pt_aw_build", 16, 2, None, 0.1, float("inf"), 0.0, C.c_void_p(256), None,
+                   None, None, C.c_void_p(256), 1 << 20, None) == _lib.PT_ERR_ARG
+    assert "finite L0" in _lib.last_error()
+    assert _status("pt_aw_build", 16, 2, C.byref(bad), 0.1, 25.0, 0.0, C.c_void_p(256), None,
+                   None, None, C.c_void_p(256), 1 << 20, None) == _lib.PT_ERR_ARG
     assert lib.pt_version() >= 100
     with pytest.raises(ValueError, match="pt_grid_create"):
         _lib.call("pt_grid_create", C.byref(h), 1, 0.1, 0, None)
 
 
 def test_workspace_queries_are_pure():
-    assert _lib.load().pt_extrude_workspace_bytes(100, 2, 9) > 100 * 3 * 9 * 4
-    assert _lib.load().pt_extrude_workspace_bytes(0, 2, 9) == 0
+    lib = _lib.load()
+    assert lib.pt_extrude_workspace_bytes(100, 2, 0, 9) > 100 * 3 * 9 * 4
+    assert lib.pt_extrude_workspace_bytes(100, 2, 18, 9) > lib.pt_extrude_workspace_bytes(100, 2,
+                                                                                          0, 9)
+    assert lib.pt_extrude_workspace_bytes(0, 2, 0, 9) == 0
+    assert lib.pt_extrude_workspace_bytes(100, 2, 65, 9) == 0
+    # the FP64 operator build: the joint (Kz + W)^2 matrix dominates
+    st = _lib.sparse_stencil([(4, 10), (8, 90)])
+    nbytes = lib.pt_aw_workspace_bytes(100, 2, C.byref(st))
+    assert nbytes >= (3 * 100 + 2) ** 2 * 8
+    assert lib.pt_aw_workspace_bytes(100, 2, None) >= (3 * 100) ** 2 * 8
+    assert lib.pt_aw_workspace_bytes(100, 2, C.byref(_lib.sparse_stencil([(1, 10)]))) == 0

@@ -1,0 +1,143 @@
+"""The extrusion engine at its benchmark size (n = 1024, W = 1449) against the
+float64 oracle on injected noise, for the reference's rows-only stencil and
+for 2 full rows + 2 sparse columns, over more than 500 row steps:
+
+- the batched ring extrusion of 9 layers x 16 realisations (144 screens, one
+  GEMM per row step) checked on a subset of the screens (they are
+  independent) against a float64 recursion with the oracle's A and B;
+- the 9-layer atmosphere with the fused bilinear readout against the oracle
+  atmosphere, frame by frame.
+
+Tolerance: relative L2 1e-5 for the float32 form against float64."""
+
+import numpy as np
+import pytest
+
+from cases import rel_l2
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-5
+N, DX, L0 = 1024, 8.0 / 1024, 25.0
+
+
+def _layers():
+    import bench
+
+    cos_z = np.cos(np.deg2rad(bench.ZENITH))
+    frac = np.array(bench.FRACTIONS) / np.sum(bench.FRACTIONS)
+    r0s = [bench.R0 * cos_z ** 0.6 * f ** (-0.6) for f in frac]
+    tab = bench.layer_table()
+    winds = [(v * np.cos(np.deg2rad(d)), v * np.sin(np.deg2rad(d))) for _, _, v, d in tab]
+    alts = [h / cos_z for h in bench.HEIGHTS]
+    return r0s, winds, alts
+
+
+@pytest.mark.parametrize("columns", [0, 2])
+def test_batched_ring_extrusion_512_steps_vs_float64(columns):
+    import torch
+
+    import pyturb_gb300 as G
+    from oracle.extrusion import build_extrusion
+    from pyturb_gb300.backend import NoiseStream
+    from pyturb_gb300.covariance import build_operator, sparse_points
+    from pyturb_gb300.extrude import RingExtruder
+
+    r0s, winds, alts = _layers()
+    ext = G.ExtrudedAtmosphere(n=N, pixel_scale=DX, layer_r0=r0s, layer_L0=[L0] * 9,
+                               layer_wind=winds, layer_altitude_los=alts, interp="linear",
+                               seeds=list(range(9)))
+    W, m = ext.width, 2
+    assert W == 1449
+    sparse = sparse_points(W, m, columns)
+    depth = max([m] + [d for d, _ in sparse])
+    S, chunk, chunks = 144, 128, 4
+    cap = depth + chunk + 64
+    bscale = [r ** (-5.0 / 6.0) for r in r0s] * 16
+    op = build_operator(W, m, DX, L0, sparse, b_factor="eigh")
+    ring = RingExtruder(W, m, cap, [], [0] * S, bscale,
+                        [NoiseStream(500 + s, np.random.default_rng) for s in range(S)],
+                        device_operator=op.M, sparse=sparse)
+    # von Karman seed rows (device Philox), `depth` rows of history per screen
+    seed_rows = []
+    for s in range(S):
+        gen = G.PhaseScreen(n=1458, pixel_scale=DX, r0=r0s[s % 9], L0=L0, subharmonics=0,
+                            seed=900 + s)
+        rows = gen.generate()[:depth, :W].contiguous()
+        ring.seed_rows(s, rows)
+        seed_rows.append(rows)
+    # float64 recursion for a subset of the screens, one per layer plus extras
+    subset = [0, 10, 20, 30, 40, 50, 60, 70, 80, 100, 143]
+    a, b = build_extrusion(W, m, DX, L0, sparse=sparse)
+    hist = {s: [seed_rows[s].double().cpu().numpy()] for s in subset}
+    streams = {s: NoiseStream(500 + s, np.random.default_rng) for s in subset}
+    R = {s: np.concatenate([hist[s][0], np.empty((chunk * chunks, W))]) for s in subset}
+    t = depth
+    errs = []
+    for c in range(chunks):
+        ring.extrude(np.full(S, chunk, dtype=np.int32))
+        for _ in range(chunk):
+            Z = np.stack([np.concatenate([R[s][t - m:t].ravel(),
+                                          [R[s][t - d, col] for d, col in sparse]])
+                          for s in subset], axis=1)
+            beta = np.stack([streams[s].draw((W,)) * bscale[s] for s in subset], axis=1)
+            new = a @ Z + b @ beta
+            for q, s in enumerate(subset):
+                R[s][t] = new[:, q]
+            t += 1
+        torch.cuda.synchronize()
+        top = int(ring.top[0])
+        phys = [(top - k - 1) % cap for k in range(chunk)][::-1]
+        got = ring.buf[subset][:, phys].double().cpu().numpy()
+        want = np.stack([R[s][t - chunk:t] for s in subset])
+        errs.append(rel_l2(got, want))
+    print(f"sparse points {len(sparse)}: relative L2 per 128-step chunk " +
+          ", ".join(f"{e:.2e}" for e in errs))
+    assert t - depth == 512
+    assert max(errs) < TOL
+
+
+@pytest.mark.parametrize("columns", [0, 2])
+def test_nine_layer_atmosphere_bilinear_readout_vs_oracle(columns):
+    import pyturb_gb300 as G
+    from oracle.extrusion import OracleExtruded
+    from pyturb_gb300.backend import to_numpy
+
+    r0s, winds, alts = _layers()
+    kw = dict(n=N, pixel_scale=DX, layer_r0=r0s, layer_L0=[L0] * 9, layer_wind=winds,
+              layer_altitude_los=alts, interp="linear", seeds=[11 + i for i in range(9)],
+              stencil_columns=columns)
+    e = G.ExtrudedAtmosphere(host_noise=np.random.default_rng, **kw)
+    o = OracleExtruded(rng_factory=np.random.default_rng, **kw)
+    assert e.width == o.W and e.capacity == o.cap and e.sparse == o.sparse
+    speeds = [np.hypot(*w) for w in winds]
+    t_end = 520 * DX / max(speeds)  # the fastest layer extrudes > 500 rows
+    top0 = e._ring.top.copy()
+    errs = []
+    for t in np.linspace(0.0, t_end, 5):
+        e.set_time(float(t))
+        o.set_time(float(t))
+        errs.append(rel_l2(to_numpy(e.integrate()), o.integrate()))
+    rows = e._ring.top - top0
+    print(f"stencil columns {columns}: frame errors " + ", ".join(f"{x:.2e}" for x in errs)
+          + f"; rows extruded per layer {rows.tolist()}")
+    assert rows.max() > 500
+    assert max(errs) < TOL
+
+
+def test_sparse_stencil_small_atmosphere_all_interpolators():
+    """2 rows + 2 sparse columns at 32^2 (ring compaction reached) for each
+    interpolator, against the oracle."""
+    import pyturb_gb300 as G
+    from oracle.extrusion import OracleExtruded
+    from pyturb_gb300.backend import to_numpy
+
+    kw = dict(n=32, pixel_scale=1.0 / 32, layer_r0=[0.15, 0.2, 0.3], layer_L0=[25.0, 25.0, 10.0],
+              layer_wind=[(8.0, 3.0), (-5.0, 6.0), (0.0, -12.0)],
+              layer_altitude_los=[0.0, 5000.0, 12000.0], seeds=[1, 2, 3], stencil_columns=2)
+    for interp in ("linear", "cubic", "lanczos"):
+        e = G.ExtrudedAtmosphere(interp=interp, host_noise=np.random.default_rng, **kw)
+        o = OracleExtruded(interp=interp, rng_factory=np.random.default_rng, **kw)
+        for t in (0.0, 0.2, 0.6, 1.2):
+            e.set_time(t)
+            o.set_time(t)
+            assert rel_l2(to_numpy(e.integrate()), o.integrate()) < TOL, (interp, t)
