@@ -223,7 +223,8 @@ def bench_extrude(torch, G, steps: int = 4096):
         for form in ("fp32", "bf16x2", "bf16x3"):
             ring = RingExtruder(W, 2, cap, [], [0] * S, [r ** (-5.0 / 6.0) for r in r0s] * R,
                                 [NoiseStream(100 + s, None) for s in range(S)],
-                                device_operator=ext._ring.M, form=form, sparse=sparse)
+                                device_operator=ext._ring.M, form=form, sparse=sparse,
+                                operator_lo=ext._ring.M_lo)
             for s in range(S):  # every realisation starts from layer (s % 9)'s seeded rows
                 ring.buf[s].copy_(ext._ring.buf[s % 9])
                 ring.top[s] = ext._ring.top[s % 9]
@@ -474,10 +475,10 @@ def run_case(args) -> None:
         print(f"generate n={args.n} count={args.count}: {dt * 1e6:.1f} us per call")
         return
     W, m, S = args.width, 2, args.screens
-    op = build_operator(W, m, 8.0 / 1024, 25.0)
+    op = build_operator(W, m, 8.0 / 1024, 25.0, want_lo=True)
     ring = RingExtruder(W, m, args.case_steps + m + 8, [], [0] * S, [1.0] * S,
                         [NoiseStream(100 + s, None) for s in range(S)], form=args.form,
-                        device_operator=op.M)
+                        device_operator=op.M, operator_lo=op.Mlo)
     for s in range(S):
         ring.seed_rows(s, torch.zeros((m, W), device=cuda_device()))
     ring.extrude(np.ones(S, dtype=np.int32))

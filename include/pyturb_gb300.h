@@ -215,6 +215,8 @@ typedef struct {
  *   M (W, K) f32 and M64 (W, K) f64 = [A | Ls], K = (m+1) W + count
  *     (Ls Ls^T is the conditional covariance the reference factors with
  *     eigh; any factor gives the same statistics);
+ *   Mlo (W, Kz) f32 = A - (float)A, the correction that keeps a float32
+ *     recursion on the float64 operator (pt_extrude_lo_prepare), or NULL;
  *   seed (Kz, Kz) f32 = L (L L^T = C_zz, Kz = m W + count), or NULL;
  *   sigma (W, W) f64 = Ls Ls^T, or NULL.
  * `jitter` adds jitter * C(0) to the stencil diagonal. A non-positive pivot
@@ -222,8 +224,8 @@ typedef struct {
  * block at or below 1e-13 C(0) zero their column. Synchronises `stream`. */
 size_t pt_aw_workspace_bytes(int W, int m, const pt_sparse_stencil* sparse);
 int pt_aw_build(int W, int m, const pt_sparse_stencil* sparse, double pixel_scale, double L0,
-                double jitter, float* M, double* M64, float* seed, double* sigma, void* work,
-                size_t work_bytes, void* stream);
+                double jitter, float* M, double* M64, float* Mlo, float* seed, double* sigma,
+                void* work, size_t work_bytes, void* stream);
 
 /* One Assemat-Wilson row step for a set of ring-buffer screens
  * (_ExtrudeLayer._extrude_one, src/pyturb/extrude.py:424-430;
@@ -256,14 +258,27 @@ size_t pt_extrude_workspace_bytes(int W, int m, int n_sparse, int max_jobs_per_s
  * _ExtrudeLayer._ensure (src/pyturb/extrude.py:446-449) for all layers and
  * realisations at once. */
 int pt_extrude_batch(int W, int m, const pt_sparse_stencil* sparse, int cap, int n_groups,
-                     const float* M, float* buf, int S, const int32_t* group,
-                     const float* bscale, const uint64_t* key, int64_t* top,
-                     const int32_t* counts, const float* noise, void* work, size_t work_bytes,
-                     void* stream);
+                     const float* M, const void* lo_tiles, float* buf, int S,
+                     const int32_t* group, const float* bscale, const uint64_t* key,
+                     int64_t* top, const int32_t* counts, const float* noise, void* work,
+                     size_t work_bytes, void* stream);
 
 int pt_extrude_rows(int W, int m, const pt_sparse_stencil* sparse, int cap, int n_groups,
-                    const float* M, float* buf, int n_jobs, const pt_extrude_job* jobs,
-                    const float* noise, void* work, size_t work_bytes, void* stream);
+                    const float* M, const void* lo_tiles, float* buf, int n_jobs,
+                    const pt_extrude_job* jobs, const float* noise, void* work,
+                    size_t work_bytes, void* stream);
+
+/* Operator correction of the float32 form (no reference counterpart): the
+ * reference's float32 path multiplies by float32(A), whose rounding is a
+ * fixed bias that the row recursion accumulates (relative error ~1e-4 after
+ * 500 rows at W = 1449). Passing `lo_tiles` to pt_extrude_batch /
+ * pt_extrude_rows adds (A - (float)A) . stencil each step as one bf16
+ * tensor-core product, which keeps the recursion on the float64 operator.
+ * pt_extrude_lo_prepare converts the (G, W, Kz) Mlo of pt_aw_build into
+ * those tiles (pt_extrude_lo_bytes bytes, 256-byte aligned). */
+size_t pt_extrude_lo_bytes(int W, int m, int n_sparse, int n_groups);
+int pt_extrude_lo_prepare(int W, int m, int n_sparse, int n_groups, const float* Mlo,
+                          void* tiles, size_t tiles_bytes, void* stream);
 
 /* Fused multi-layer rotated sub-pixel readout of the extrusion engine
  * (ExtrudedAtmosphere._integrate_fused_kernel / _integrate_looped,

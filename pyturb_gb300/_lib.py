@@ -113,12 +113,14 @@ SIGNATURES = {
     "pt_boil_step": (i32, [vp, i32, vp, vp, vp, vp, vp, vp, f64, vp, vp, u64, u64, vp]),
     "pt_aw_workspace_bytes": (sz, [i32, i32, C.POINTER(SparseStencil)]),
     "pt_aw_build": (i32, [i32, i32, C.POINTER(SparseStencil), f64, f64, f64, vp, vp, vp, vp, vp,
-                          sz, vp]),
+                          vp, sz, vp]),
     "pt_extrude_workspace_bytes": (sz, [i32, i32, i32, i32]),
-    "pt_extrude_rows": (i32, [i32, i32, C.POINTER(SparseStencil), i32, i32, vp, vp, i32,
+    "pt_extrude_rows": (i32, [i32, i32, C.POINTER(SparseStencil), i32, i32, vp, vp, vp, i32,
                               C.POINTER(ExtrudeJob), vp, vp, sz, vp]),
-    "pt_extrude_batch": (i32, [i32, i32, C.POINTER(SparseStencil), i32, i32, vp, vp, i32, vp,
-                               vp, vp, vp, vp, vp, vp, sz, vp]),
+    "pt_extrude_batch": (i32, [i32, i32, C.POINTER(SparseStencil), i32, i32, vp, vp, vp, i32,
+                               vp, vp, vp, vp, vp, vp, vp, sz, vp]),
+    "pt_extrude_lo_bytes": (sz, [i32, i32, i32, i32]),
+    "pt_extrude_lo_prepare": (i32, [i32, i32, i32, i32, vp, vp, sz, vp]),
     "pt_readout": (i32, [i32, i32, i32, i32, i32, C.POINTER(ReadoutLayer), vp, f32, vp, vp]),
     "pt_rows_sample": (i32, [i32, i32, i32, i32, i32, f64, vp, vp, vp]),
     "pt_lr_fix": (i32, [i32, i32, i32, i32, i32, vp, dptr, vp, vp]),

@@ -106,15 +106,16 @@ def sparse_points(width: int, stencil_rows: int, columns: int,
 
 class ExtrusionOperator:
     """Device operator of one outer scale: ``M = [A | B]`` float32 ``(W, K)``
-    (``K = (m + 1) W + len(sparse)``), optionally its float64 twin ``M64``
-    and the stencil factor ``S`` (float32 ``(Kz, Kz)``, ``S S^T = C_zz``),
-    all at unit r0."""
+    (``K = (m + 1) W + len(sparse)``), optionally its float64 twin ``M64``,
+    the float32 rounding of the stencil part ``Mlo = A - float32(A)``
+    (``(W, Kz)``, ``Kz = m W + len(sparse)``) and the stencil factor ``S``
+    (float32 ``(Kz, Kz)``, ``S S^T = C_zz``), all at unit r0."""
 
-    def __init__(self, W: int, m: int, sparse, M, M64=None, S=None):
+    def __init__(self, W: int, m: int, sparse, M, M64=None, S=None, Mlo=None):
         self.W, self.m = int(W), int(m)
         self.sparse = list(sparse)
         self.Kz = self.m * self.W + len(self.sparse)
-        self.M, self.M64, self.S = M, M64, S
+        self.M, self.M64, self.S, self.Mlo = M, M64, S, Mlo
 
     def host(self, r0: float = 1.0) -> Tuple[np.ndarray, np.ndarray]:
         """``(A, B)`` as float64 host arrays, ``B`` scaled by r0^(-5/6)."""
@@ -125,7 +126,8 @@ class ExtrusionOperator:
 
 def build_operator(width: int, stencil_rows: int, pixel_scale: float, L0: float,
                    sparse: Sequence[Tuple[int, int]] = (), b_factor: str = "cholesky",
-                   want_seed: bool = False, want_float64: bool = False) -> ExtrusionOperator:
+                   want_seed: bool = False, want_float64: bool = False,
+                   want_lo: bool = False) -> ExtrusionOperator:
     """Build ``[A | B]`` for extruding one ``width``-pixel row from the stencil
     (``stencil_rows`` full rows below it, then the ``sparse`` points) at unit
     r0, in FP64 on the GPU. ``b_factor``: ``"cholesky"`` (the build's own
@@ -152,10 +154,11 @@ def build_operator(width: int, stencil_rows: int, pixel_scale: float, L0: float,
     M = torch.empty((W, K), dtype=torch.float32, device=dev)
     M64 = torch.empty((W, K), dtype=torch.float64, device=dev) if want_float64 else None
     S = torch.empty((Kz, Kz), dtype=torch.float32, device=dev) if want_seed else None
+    Mlo = torch.empty((W, Kz), dtype=torch.float32, device=dev) if want_lo else None
     sigma = torch.empty((W, W), dtype=torch.float64, device=dev) if b_factor == "eigh" else None
     for jitter in (0.0, 1e-12, 1e-10, 1e-8):
         rc = lib.pt_aw_build(W, m, sp, float(pixel_scale), float(L0), jitter, dptr(M), dptr(M64),
-                             dptr(S), dptr(sigma), dptr(work), nbytes, stream_handle())
+                             dptr(Mlo), dptr(S), dptr(sigma), dptr(work), nbytes, stream_handle())
         if rc == _lib.PT_OK:
             break
         if rc != _lib.PT_ERR_NUMERIC or jitter == 1e-8:
@@ -171,7 +174,7 @@ def build_operator(width: int, stencil_rows: int, pixel_scale: float, L0: float,
         M[:, Kz:] = torch.from_numpy(root).to(device=dev, dtype=torch.float32)
         if M64 is not None:
             M64[:, Kz:] = torch.from_numpy(root).to(device=dev)
-    return ExtrusionOperator(W, m, sparse, M, M64, S)
+    return ExtrusionOperator(W, m, sparse, M, M64, S, Mlo)
 
 
 def build_extrusion(width: int, stencil_rows: int, pixel_scale: float, L0: float,

@@ -216,6 +216,33 @@ __global__ void k_tc_gather(int W, int m, int cap, const float* __restrict__ buf
   }
 }
 
+// The stencil part of the FP32 form's operand, X[j][0, Kz), as one bf16
+// term in the tensor-core B-tile layout (zero beyond Kz and J): the operand
+// of the operator correction (A - (float)A) X, whose bf16 rounding is far
+// below float32 resolution (the correction itself is ~2^-24 of the product).
+__global__ void k_lo_operand(const float* __restrict__ X, int J, int K, int Kz, int NP, int nkc,
+                             uint8_t* __restrict__ tiles) {
+  constexpr int Kc = tc::kTcKc;
+  const int groups = nkc * (Kc / 8);
+  const size_t total = (size_t)groups * NP;
+  for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+       t += (size_t)gridDim.x * blockDim.x) {
+    const int j = (int)(t / groups);
+    const int k0 = (int)(t % groups) * 8;
+    uint32_t w4[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int ka = k0 + 2 * q, kb = ka + 1;
+      const float a = (j < J && ka < Kz) ? X[(size_t)j * K + ka] : 0.f;
+      const float b = (j < J && kb < Kz) ? X[(size_t)j * K + kb] : 0.f;
+      w4[q] = (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(a)) |
+              ((uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(b)) << 16);
+    }
+    uint8_t* blk = tiles + (size_t)(k0 / Kc) * NP * Kc * 2 + tc::core_offset(j, k0 % Kc, Kc);
+    *(uint4*)blk = make_uint4(w4[0], w4[1], w4[2], w4[3]);
+  }
+}
+
 // partial[z][j][r] = sum_{k in slice z} M[r][k] X[j][k]
 __global__ void __launch_bounds__(256)
 k_extrude_gemm(int W, int K, int J, int kslice, const float* __restrict__ M,
@@ -538,12 +565,27 @@ static int split_for(int W, int J, int K) {
 
 using namespace pt;
 
+// FP32-form workspace: X (J, K) | correction B tiles | partials of the FP32
+// GEMM (up to kMaxSplitTiled slices) followed by those of the correction.
+struct Fp32Work {
+  size_t x, lo_tiles, partial, total;
+  int lo_nz;
+};
+static Fp32Work fp32_work(int W, int m, int n_sparse, int J) {
+  Fp32Work w{};
+  const int K = (m + 1) * W + n_sparse, Kz = m * W + n_sparse;
+  w.x = al256((size_t)J * K * sizeof(float));
+  w.lo_tiles = al256(tc_btile_bytes(W, Kz, J, 1));
+  w.lo_nz = (int)(tc_partial_floats(W, Kz, J, 1) / ((size_t)J * W));
+  w.partial = al256((size_t)(std::max(kMaxSplit, kMaxSplitTiled) + w.lo_nz) * J * W *
+                    sizeof(float));
+  w.total = w.x + w.lo_tiles + w.partial;
+  return w;
+}
+
 extern "C" size_t pt_extrude_workspace_bytes(int W, int m, int n_sparse, int max_jobs) {
   if (W < 1 || m < 1 || max_jobs < 1 || n_sparse < 0 || n_sparse > PT_MAX_SPARSE) return 0;
-  const size_t K = (size_t)(m + 1) * W + n_sparse;
-  const size_t J = (size_t)std::min(max_jobs, kJobsPerLaunch);
-  return al256(J * K * sizeof(float)) +
-         al256((size_t)std::max(kMaxSplit, kMaxSplitTiled) * J * W * sizeof(float));
+  return fp32_work(W, m, n_sparse, std::min(max_jobs, kJobsPerLaunch)).total;
 }
 
 // The operator of one form: FP32 [A | B] (SIMT GEMM) or its bf16 term tiles
@@ -552,6 +594,7 @@ struct ExtrudeForm {
   int terms;               // 0: FP32
   const float* M;          // (G, W, K) FP32
   const uint8_t* tiles;    // tensor-core operator tiles
+  const uint8_t* lo;       // FP32 form: 1-term tiles of A - (float)A, or NULL
 };
 
 static int extrude_jobs(const char* who, const ExtrudeForm& form, int W, int m,
@@ -588,16 +631,19 @@ static int extrude_jobs(const char* who, const ExtrudeForm& form, int W, int m,
   const size_t need = form.terms ? pt_extrude_tc_workspace_bytes(W, m, sp.n, max_j, form.terms)
                                  : pt_extrude_workspace_bytes(W, m, sp.n, max_j);
   if (!work || work_bytes < need) return fail(PT_ERR_ARG, std::string(who) + ": workspace too small");
-  const int K = (m + 1) * W + sp.n;
+  const int K = (m + 1) * W + sp.n, Kz = m * W + sp.n;
   const int per_launch = form.terms ? tc_max_jobs(form.terms) : kJobsPerLaunch;
   const int jcap = std::min(max_j, per_launch);
-  // FP32: X (jcap, K) then partials; tensor cores: B tiles then partials
+  // FP32: X (jcap, K), correction B tiles, partials; tensor cores: B tiles then partials
+  const Fp32Work fw = fp32_work(W, m, sp.n, jcap);
   const size_t first = form.terms ? al256(tc_btile_bytes(W, K, jcap, form.terms))
-                                  : al256((size_t)jcap * K * sizeof(float));
+                                  : fw.x + fw.lo_tiles;
   float* X = (float*)work;
   uint8_t* Bt = (uint8_t*)work;
+  uint8_t* Blo = (uint8_t*)work + fw.x;
   float* partial = (float*)((char*)work + first);
   const size_t op_group = form.terms ? tc_operator_bytes(W, K, 1, form.terms) : 0;
+  const size_t lo_group = tc_operator_bytes(W, Kz, 1, 1);
   std::vector<GatherJob> hj;
   // The split-K reduce of a launch is deferred: when the next FP32 launch
   // extrudes the same screens in the same order one row further, its gather
@@ -657,6 +703,25 @@ static int extrude_jobs(const char* who, const ExtrudeForm& form, int W, int m,
           }
           const float* Mg = form.M + (size_t)kv.first * W * K;
           launch_gemm_tiled(W, K, J, Mg, X, partial, &nz, s);
+          if (form.lo) {
+            // + (A - (float)A) X on the tensor cores, into the slices after the
+            // FP32 GEMM's: without it the float32 rounding of A is a bias that
+            // the recursion accumulates row after row
+            const int NP = std::max(16, (J + 15) / 16 * 16);
+            const int nkc = (Kz + tc::kTcKc - 1) / tc::kTcKc;
+            const size_t items = (size_t)nkc * (tc::kTcKc / 8) * NP;
+            {
+              ProfScope ps("k_lo_operand", s);
+              k_lo_operand<<<(unsigned)std::min<size_t>((items + 255) / 256, 152 * 4), 256, 0,
+                             s>>>(X, J, K, Kz, NP, nkc, Blo);
+            }
+            count_launch_e();
+            int nz_lo = 0;
+            if (int rc = tc_gemm_launch(W, Kz, J, 1, form.lo + (size_t)kv.first * lo_group, Blo,
+                                        partial + (size_t)nz * J * W, &nz_lo, s))
+              return rc;
+            nz += nz_lo;
+          }
         } else {
           const int NP = std::max(16, (J + 15) / 16 * 16);
           const int nkc = (K + tc::kTcKc - 1) / tc::kTcKc;
@@ -785,10 +850,14 @@ extern "C" int pt_matmul_nt(int R, int K, int J, const float* M, const float* X,
 }
 
 extern "C" int pt_extrude_rows(int W, int m, const pt_sparse_stencil* sparse, int cap, int G,
-                               const float* M, float* buf, int n_jobs, const pt_extrude_job* jobs,
-                               const float* noise, void* work, size_t work_bytes, void* stream) {
-  return extrude_jobs("pt_extrude_rows", ExtrudeForm{0, M, nullptr}, W, m, sparse, cap, G, buf,
-                      n_jobs, jobs, noise, work, work_bytes, (cudaStream_t)stream);
+                               const float* M, const void* lo_tiles, float* buf, int n_jobs,
+                               const pt_extrude_job* jobs, const float* noise, void* work,
+                               size_t work_bytes, void* stream) {
+  if (lo_tiles && ((uintptr_t)lo_tiles & 255) != 0)
+    return fail(PT_ERR_ARG, "pt_extrude_rows: correction tiles must be 256-byte aligned");
+  return extrude_jobs("pt_extrude_rows", ExtrudeForm{0, M, nullptr, (const uint8_t*)lo_tiles}, W,
+                      m, sparse, cap, G, buf, n_jobs, jobs, noise, work, work_bytes,
+                      (cudaStream_t)stream);
 }
 
 // Jobs of `counts[s]` row steps on every screen s, step-major (the order of
@@ -826,16 +895,37 @@ static int batch_jobs(const char* who, int W, int cap, int S, const int32_t* gro
 }
 
 extern "C" int pt_extrude_batch(int W, int m, const pt_sparse_stencil* sparse, int cap,
-                                int n_groups, const float* M, float* buf, int S,
-                                const int32_t* group, const float* bscale, const uint64_t* key,
-                                int64_t* top, const int32_t* counts, const float* noise,
-                                void* work, size_t work_bytes, void* stream) {
+                                int n_groups, const float* M, const void* lo_tiles, float* buf,
+                                int S, const int32_t* group, const float* bscale,
+                                const uint64_t* key, int64_t* top, const int32_t* counts,
+                                const float* noise, void* work, size_t work_bytes,
+                                void* stream) {
+  if (lo_tiles && ((uintptr_t)lo_tiles & 255) != 0)
+    return fail(PT_ERR_ARG, "pt_extrude_batch: correction tiles must be 256-byte aligned");
   std::vector<pt_extrude_job> jobs;
   if (int rc = batch_jobs("pt_extrude_batch", W, cap, S, group, bscale, key, top, counts, jobs))
     return rc;
-  return extrude_jobs("pt_extrude_batch", ExtrudeForm{0, M, nullptr}, W, m, sparse, cap, n_groups,
-                      buf, (int)jobs.size(), jobs.data(), noise, work, work_bytes,
-                      (cudaStream_t)stream);
+  return extrude_jobs("pt_extrude_batch", ExtrudeForm{0, M, nullptr, (const uint8_t*)lo_tiles}, W,
+                      m, sparse, cap, n_groups, buf, (int)jobs.size(), jobs.data(), noise, work,
+                      work_bytes, (cudaStream_t)stream);
+}
+
+extern "C" size_t pt_extrude_lo_bytes(int W, int m, int n_sparse, int n_groups) {
+  if (W < 1 || m < 1 || n_groups < 1 || n_sparse < 0 || n_sparse > PT_MAX_SPARSE) return 0;
+  return tc_operator_bytes(W, m * W + n_sparse, n_groups, 1);
+}
+
+extern "C" int pt_extrude_lo_prepare(int W, int m, int n_sparse, int n_groups, const float* Mlo,
+                                     void* tiles, size_t tiles_bytes, void* stream) {
+  if (W < 1 || m < 1 || n_groups < 1 || n_sparse < 0 || n_sparse > PT_MAX_SPARSE)
+    return fail(PT_ERR_ARG, "pt_extrude_lo_prepare: bad sizes");
+  if (!Mlo || !tiles) return fail(PT_ERR_ARG, "pt_extrude_lo_prepare: NULL pointer");
+  const int Kz = m * W + n_sparse;
+  if (tiles_bytes < tc_operator_bytes(W, Kz, n_groups, 1))
+    return fail(PT_ERR_ARG, "pt_extrude_lo_prepare: tile buffer too small");
+  if (((uintptr_t)tiles & 255) != 0)
+    return fail(PT_ERR_ARG, "pt_extrude_lo_prepare: tiles must be 256-byte aligned");
+  return tc_prepare_launch(W, Kz, n_groups, Mlo, 1, tiles, (cudaStream_t)stream);
 }
 
 static bool tc_sizes_ok(int W, int m, int n_sparse, int n, int terms) {
@@ -885,7 +975,8 @@ extern "C" int pt_extrude_batch_tc(int W, int m, const pt_sparse_stencil* sparse
   std::vector<pt_extrude_job> jobs;
   if (int rc = batch_jobs("pt_extrude_batch_tc", W, cap, S, group, bscale, key, top, counts, jobs))
     return rc;
-  return extrude_jobs("pt_extrude_batch_tc", ExtrudeForm{terms, nullptr, (const uint8_t*)tiles}, W,
+  return extrude_jobs("pt_extrude_batch_tc",
+                      ExtrudeForm{terms, nullptr, (const uint8_t*)tiles, nullptr}, W,
                       m, sparse, cap, n_groups, buf, (int)jobs.size(), jobs.data(), noise, work,
                       work_bytes, (cudaStream_t)stream);
 }

@@ -126,7 +126,7 @@ template <int TERMS>
 __global__ void __launch_bounds__(128)
 k_tc_gemm(int W, int J, int NP, int nkc, int cps, int stages, const uint8_t* __restrict__ At,
           const uint8_t* __restrict__ Bt, float* __restrict__ partial) {
-  constexpr int NPROD = TERMS == 2 ? 3 : 6;
+  constexpr int NPROD = TERMS == 1 ? 1 : (TERMS == 2 ? 3 : 6);
   constexpr int pa[6] = {0, 0, 1, 0, 2, 1};
   constexpr int pb[6] = {0, 1, 0, 2, 0, 1};
   extern __shared__ uint8_t smraw[];
@@ -241,7 +241,7 @@ TcShape tc_shape(int W, int K, int J, int terms) {
   t.stages = (int)std::min<size_t>(kTcMaxStages, (kTcSmemMax - 2048) / t.stage_bytes);
   return t;
 }
-int tc_max_jobs(int terms) { return terms == 2 ? 192 : 160; }
+int tc_max_jobs(int terms) { return terms == 3 ? 160 : 192; }
 size_t tc_operator_bytes(int W, int K, int G, int terms) {
   const TcShape t = tc_shape(W, K, 1, terms);
   return (size_t)G * t.MT * t.nkc * terms * kTcTileA;
@@ -272,6 +272,21 @@ int tc_gemm_launch(int W, int K, int J, int terms, const uint8_t* At, const uint
   if (t.stages < 2) return fail(PT_ERR_UNSUPPORTED, "extrusion tensor-core form: too many jobs");
   const size_t smem = (size_t)t.stages * t.stage_bytes + 1024;
   dim3 grid(t.MT, t.nz);
+  if (terms == 1) {  // the float32 form's operator correction
+    ProfScope ps("k_tc_gemm_lo", s);
+    static bool attr = false;
+    if (!attr) {
+      if (int rc = check_cuda(cudaFuncSetAttribute(k_tc_gemm<1>,
+                                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                   (int)(kTcSmemMax - 1024)), "k_tc_gemm"))
+        return rc;
+      attr = true;
+    }
+    k_tc_gemm<1><<<grid, 128, smem, s>>>(W, J, t.NP, t.nkc, t.cps, t.stages, At, Bt, partial);
+    count_launch_t();
+    *nz_out = t.nz;
+    return check_launch("k_tc_gemm");
+  }
   ProfScope ps("k_tc_gemm", s);
   if (terms == 2) {
     static bool attr = false;

@@ -262,14 +262,18 @@ __global__ void k_zero_upper(double* __restrict__ a, int n) {
 
 // M (W, Kz + W) float32 = [A | B] from the factored joint matrix (ld N):
 // A = rows [Kz, N), columns [0, Kz); B = rows [Kz, N), columns [Kz, N).
+// Mlo (W, Kz) float32 = A - float(A): what the float32 stencil operator
+// leaves out (its relative size is ~2^-24).
 __global__ void k_pack_operator(int W, int Kz, int N, const double* __restrict__ J,
-                                float* __restrict__ M, double* __restrict__ M64) {
+                                float* __restrict__ M, double* __restrict__ M64,
+                                float* __restrict__ Mlo) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   const int r = blockIdx.y;
   if (c >= N || r >= W) return;
   const double v = J[(size_t)(Kz + r) * N + c];
   if (M) M[(size_t)r * N + c] = (float)v;
   if (M64) M64[(size_t)r * N + c] = v;
+  if (Mlo && c < Kz) Mlo[(size_t)r * Kz + c] = (float)(v - (double)(float)v);
 }
 
 // S (Kz, Kz) float32 = the stencil factor L
@@ -411,8 +415,9 @@ extern "C" size_t pt_aw_workspace_bytes(int W, int m, const pt_sparse_stencil* s
 }
 
 extern "C" int pt_aw_build(int W, int m, const pt_sparse_stencil* sparse, double pixel_scale,
-                           double L0, double jitter, float* M, double* M64, float* seed,
-                           double* sigma, void* work, size_t work_bytes, void* stream) {
+                           double L0, double jitter, float* M, double* M64, float* Mlo,
+                           float* seed, double* sigma, void* work, size_t work_bytes,
+                           void* stream) {
   const char* who = "pt_aw_build";
   if (!(pixel_scale > 0.0) || !(L0 > 0.0) || !std::isfinite(L0))
     return fail(PT_ERR_ARG, std::string(who) + ": pixel_scale and a finite L0 must be positive");
@@ -479,7 +484,7 @@ extern "C" int pt_aw_build(int W, int m, const pt_sparse_stencil* sparse, double
   if (sigma)  // the conditional covariance Ls Ls^T (W x W, FP64)
     if (int rc = dgemm(true, W, W, W, 1.0, Yt + Kz, N, Yt + Kz, N, 0.0, sigma, W, false, s))
       return rc;
-  k_pack_operator<<<dim3((N + 255) / 256, W), 256, 0, s>>>(W, Kz, N, J, M, M64);
+  k_pack_operator<<<dim3((N + 255) / 256, W), 256, 0, s>>>(W, Kz, N, J, M, M64, Mlo);
   count_launch_o();
   if (seed) {
     k_pack_seed<<<dim3((Kz + 255) / 256, Kz), 256, 0, s>>>(Kz, N, J, seed);

@@ -97,14 +97,17 @@ class RingExtruder:
     lists the stencil's sparse points ``(depth, column)`` after its ``m`` full
     rows (none: the reference's rows-only stencil). ``operators`` holds host
     ``(A, B)`` pairs, or ``device_operator`` an existing ``(G, W, K)``
-    float32 CUDA tensor, K = (m + 1) W + len(sparse)."""
+    float32 CUDA tensor, K = (m + 1) W + len(sparse). ``operator_lo``
+    (``(G, W, Kz)`` float32, ``A - float32(A)``) makes the FP32 form add that
+    correction each step, so that the recursion follows the float64
+    operator instead of accumulating the float32 rounding of ``A``."""
 
     FORMS = {"fp32": 0, "bf16x2": 2, "bf16x3": 3}
 
     def __init__(self, W: int, m: int, cap: int, operators: List[Tuple[np.ndarray, np.ndarray]],
                  groups: Sequence[int], bscale: Sequence[float], streams: Sequence[NoiseStream],
                  device_operator=None, form: str = "fp32",
-                 sparse: Sequence[Tuple[int, int]] = ()):
+                 sparse: Sequence[Tuple[int, int]] = (), operator_lo=None):
         torch = torch_module()
         if form not in self.FORMS:
             raise ValueError(f"form must be one of {sorted(self.FORMS)}, got {form!r}")
@@ -131,6 +134,16 @@ class RingExtruder:
             raise ValueError(f"operator shape {tuple(self.M.shape)} does not match W={self.W}, "
                              f"m={self.m} and {self.ns} sparse points")
         self.G = int(self.M.shape[0])
+        self.M_lo = None
+        self.lo_tiles = None
+        if operator_lo is not None and self.terms == 0:
+            self.M_lo = operator_lo if operator_lo.dim() == 3 else operator_lo[None]
+            if self.M_lo.shape != (self.G, self.W, self.m * self.W + self.ns):
+                raise ValueError("operator_lo must be (G, W, m W + sparse points)")
+            nbytes = int(_lib.load().pt_extrude_lo_bytes(self.W, self.m, self.ns, self.G))
+            self.lo_tiles = torch.empty(nbytes, dtype=torch.uint8, device=cuda_device())
+            _lib.call("pt_extrude_lo_prepare", self.W, self.m, self.ns, self.G,
+                      dptr(self.M_lo.contiguous()), dptr(self.lo_tiles), nbytes, stream_handle())
         self.buf = torch.empty((self.S, self.cap, self.W), dtype=torch.float32,
                                device=cuda_device())
         # rows extruded so far per screen (relative virtual rows [0, top))
@@ -189,7 +202,8 @@ class RingExtruder:
                       dptr(self.work), self.work_bytes, stream_handle())
         else:
             _lib.call("pt_extrude_batch", self.W, self.m, self._sp, self.cap, self.G,
-                      dptr(self.M), dptr(self.buf), self.S, ptr(self._group), ptr(self._bscale),
+                      dptr(self.M), dptr(self.lo_tiles), dptr(self.buf), self.S,
+                      ptr(self._group), ptr(self._bscale),
                       ptr(self._key), ptr(self.top), ptr(counts), dptr(noise), dptr(self.work),
                       self.work_bytes, stream_handle())
 
@@ -299,7 +313,8 @@ class ExtrudedAtmosphere:
                 op_index[key] = len(ops)
                 ops.append(build_operator(W, self.m, self.dx, float(L0), self.sparse,
                                           b_factor="eigh" if host_noise is not None
-                                          else "cholesky", want_seed=self.boiling))
+                                          else "cholesky", want_seed=self.boiling,
+                                          want_lo=extrude_form == "fp32"))
             groups.append(op_index[key])
         streams = [NoiseStream(s, host_noise) for s in config.seeds]
         self._streams = streams
@@ -310,9 +325,10 @@ class ExtrudedAtmosphere:
                                           history))
         bscale = [float(r0) ** (-5.0 / 6.0) for r0 in config.layer_r0]
         torch = torch_module()
+        lo = torch.stack([op.Mlo for op in ops]) if extrude_form == "fp32" else None
         self._ring = RingExtruder(W, self.m, self.capacity, [], groups, bscale, streams,
                                   device_operator=torch.stack([op.M for op in ops]),
-                                  form=extrude_form, sparse=self.sparse)
+                                  form=extrude_form, sparse=self.sparse, operator_lo=lo)
         # seed each ring with a von Karman screen from the layer's own stream:
         # a W x W screen for the rows-only stencil (as the reference), a taller
         # one cropped to W columns when sparse points need older rows
@@ -336,7 +352,7 @@ class ExtrudedAtmosphere:
             self._scratch = RingExtruder(
                 W, self.m, self.capacity + self.m, [], [groups[i] for i in self._boil_layers],
                 [bscale[i] for i in self._boil_layers], self._queues,
-                device_operator=self._ring.M, form=extrude_form)
+                device_operator=self._ring.M, form=extrude_form, operator_lo=self._ring.M_lo)
 
     @property
     def _buf(self):

@@ -50,13 +50,14 @@ class InfinitePhaseScreen:
         # FP64 device build at unit r0 (the reference's eigen-square-root B in
         # the parity mode, the build's Cholesky factor otherwise)
         op = build_operator(self.n, self.stencil_rows, self.pixel_scale, self.L0,
-                            b_factor="eigh" if host_noise is not None else "cholesky")
+                            b_factor="eigh" if host_noise is not None else "cholesky",
+                            want_lo=True)
         self._stream = NoiseStream(seed, host_noise)
         self._margin = self.stencil_rows + 6
         self._capacity = self.n + self._margin
         self._ring = RingExtruder(self.n, self.stencil_rows, self._capacity, [], [0],
                                   [self.r0 ** (-5.0 / 6.0)], [self._stream],
-                                  device_operator=op.M)
+                                  device_operator=op.M, operator_lo=op.Mlo)
         gen = PhaseScreen(n=self.n, pixel_scale=self.pixel_scale, r0=self.r0, L0=self.L0,
                           _stream=self._stream, host_noise=host_noise)
         self._ring.seed_rows(0, gen.generate())

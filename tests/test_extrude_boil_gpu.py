@@ -21,20 +21,25 @@ def _frames(tau, seed=5, steps=12):
 
 
 def test_boiling_decorrelates_and_keeps_variance():
-    frozen = _frames(None)
-    boiled = _frames([0.02, 0.02])
-
+    """Averaged over 8 seeds: the spatial variance of one 48^2 frame is
+    dominated by tilt (a few degrees of freedom), so a single realisation
+    scatters by factors of several."""
     def corr(a, b):
         a = a - a.mean()
         b = b - b.mean()
         return float((a * b).sum() / np.sqrt((a * a).sum() * (b * b).sum()))
 
-    c_frozen = np.mean([corr(frozen[k], frozen[k + 6]) for k in range(6)])
-    c_boiled = np.mean([corr(boiled[k], boiled[k + 6]) for k in range(6)])
-    assert c_boiled < c_frozen - 0.2, (c_frozen, c_boiled)
-    v_frozen, v_boiled = frozen.var(axis=(1, 2)).mean(), boiled.var(axis=(1, 2)).mean()
-    assert 0.3 < v_boiled / v_frozen < 3.0
-    assert np.all(np.isfinite(boiled))
+    cf, cb, vf, vb = [], [], [], []
+    for seed in range(5, 13):
+        frozen = _frames(None, seed=seed)
+        boiled = _frames([0.02, 0.02], seed=seed)
+        assert np.all(np.isfinite(boiled))
+        cf += [corr(frozen[k], frozen[k + 6]) for k in range(6)]
+        cb += [corr(boiled[k], boiled[k + 6]) for k in range(6)]
+        vf.append(frozen.var(axis=(1, 2)).mean())
+        vb.append(boiled.var(axis=(1, 2)).mean())
+    assert np.mean(cb) < np.mean(cf) - 0.2, (np.mean(cf), np.mean(cb))
+    assert 0.5 < np.mean(vb) / np.mean(vf) < 2.0, (np.mean(vf), np.mean(vb))
 
 
 def test_frozen_layers_are_untouched_by_other_layers_boiling():

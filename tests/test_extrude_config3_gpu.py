@@ -53,10 +53,10 @@ def test_batched_ring_extrusion_512_steps_vs_float64(columns):
     S, chunk, chunks = 144, 128, 4
     cap = depth + chunk + 64
     bscale = [r ** (-5.0 / 6.0) for r in r0s] * 16
-    op = build_operator(W, m, DX, L0, sparse, b_factor="eigh")
+    op = build_operator(W, m, DX, L0, sparse, b_factor="eigh", want_lo=True)
     ring = RingExtruder(W, m, cap, [], [0] * S, bscale,
                         [NoiseStream(500 + s, np.random.default_rng) for s in range(S)],
-                        device_operator=op.M, sparse=sparse)
+                        device_operator=op.M, sparse=sparse, operator_lo=op.Mlo)
     # von Karman seed rows (device Philox), `depth` rows of history per screen
     seed_rows = []
     for s in range(S):
