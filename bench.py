@@ -224,7 +224,7 @@ def bench_extrude(torch, G, steps: int = 4096):
             ring = RingExtruder(W, 2, cap, [], [0] * S, [r ** (-5.0 / 6.0) for r in r0s] * R,
                                 [NoiseStream(100 + s, None) for s in range(S)],
                                 device_operator=ext._ring.M, form=form, sparse=sparse,
-                                operator_lo=ext._ring.M_lo)
+                                operator_lo=ext._ring.M_lo, anchor=ext._ring.anchor)
             for s in range(S):  # every realisation starts from layer (s % 9)'s seeded rows
                 ring.buf[s].copy_(ext._ring.buf[s % 9])
                 ring.top[s] = ext._ring.top[s % 9]
@@ -458,7 +458,7 @@ def run_case(args) -> None:
 
     import pyturb_gb300 as G
     from pyturb_gb300.backend import NoiseStream, cuda_device
-    from pyturb_gb300.covariance import build_operator
+    from pyturb_gb300.covariance import AnchorTables, build_operator
     from pyturb_gb300.extrude import RingExtruder
 
     torch.cuda.set_device(0)
@@ -475,10 +475,10 @@ def run_case(args) -> None:
         print(f"generate n={args.n} count={args.count}: {dt * 1e6:.1f} us per call")
         return
     W, m, S = args.width, 2, args.screens
-    op = build_operator(W, m, 8.0 / 1024, 25.0, want_lo=True)
+    op = build_operator(W, m, 8.0 / 1024, 25.0, want_lo=True, want_float64=True)
     ring = RingExtruder(W, m, args.case_steps + m + 8, [], [0] * S, [1.0] * S,
                         [NoiseStream(100 + s, None) for s in range(S)], form=args.form,
-                        device_operator=op.M, operator_lo=op.Mlo)
+                        device_operator=op.M, operator_lo=op.Mlo, anchor=AnchorTables([op]))
     for s in range(S):
         ring.seed_rows(s, torch.zeros((m, W), device=cuda_device()))
     ring.extrude(np.ones(S, dtype=np.int32))

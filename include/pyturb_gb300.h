@@ -257,16 +257,35 @@ size_t pt_extrude_workspace_bytes(int W, int m, int n_sparse, int max_jobs_per_s
  * screen s+1, all step-k rows before step k+1). Replaces the per-row loop of
  * _ExtrudeLayer._ensure (src/pyturb/extrude.py:446-449) for all layers and
  * realisations at once. */
+/* Low-order anchor of the float32 form (no reference counterpart). The row
+ * recursion amplifies errors in the smooth modes of a row, so float32
+ * rounding in the product walks them away from the float64 result over
+ * hundreds of rows. With an anchor, each new row's first `modes` (= 32)
+ * DCT-II modes U (orthonormal, U[i][w] = sqrt((2 - [i=0]) / W)
+ * cos(pi i (w + 1/2) / W)) are recomputed in double-float arithmetic and
+ * set: row += U (U^T A z + U^T B (bscale beta) - U^T row). Tables (device
+ * f32, hi + lo = the float64 value): p_hi/p_lo (G, modes, Kz) = U^T A,
+ * p_noise (G, modes, W) = U^T B_unit, u_hi/u_lo (modes, W) = U. */
+typedef struct {
+  int32_t modes;
+  int32_t pad;
+  const float* p_hi;
+  const float* p_lo;
+  const float* p_noise;
+  const float* u_hi;
+  const float* u_lo;
+} pt_extrude_anchor;
+
 int pt_extrude_batch(int W, int m, const pt_sparse_stencil* sparse, int cap, int n_groups,
-                     const float* M, const void* lo_tiles, float* buf, int S,
-                     const int32_t* group, const float* bscale, const uint64_t* key,
-                     int64_t* top, const int32_t* counts, const float* noise, void* work,
-                     size_t work_bytes, void* stream);
+                     const float* M, const void* lo_tiles, const pt_extrude_anchor* anchor,
+                     float* buf, int S, const int32_t* group, const float* bscale,
+                     const uint64_t* key, int64_t* top, const int32_t* counts,
+                     const float* noise, void* work, size_t work_bytes, void* stream);
 
 int pt_extrude_rows(int W, int m, const pt_sparse_stencil* sparse, int cap, int n_groups,
-                    const float* M, const void* lo_tiles, float* buf, int n_jobs,
-                    const pt_extrude_job* jobs, const float* noise, void* work,
-                    size_t work_bytes, void* stream);
+                    const float* M, const void* lo_tiles, const pt_extrude_anchor* anchor,
+                    float* buf, int n_jobs, const pt_extrude_job* jobs, const float* noise,
+                    void* work, size_t work_bytes, void* stream);
 
 /* Operator correction of the float32 form (no reference counterpart): the
  * reference's float32 path multiplies by float32(A), whose rounding is a

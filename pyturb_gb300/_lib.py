@@ -71,6 +71,20 @@ def sparse_stencil(points):
     return st
 
 
+class ExtrudeAnchor(C.Structure):
+    """``pt_extrude_anchor``: device tables of the float32 form's low-order anchor."""
+
+    _fields_ = [
+        ("modes", C.c_int32),
+        ("pad", C.c_int32),
+        ("p_hi", C.c_void_p),
+        ("p_lo", C.c_void_p),
+        ("p_noise", C.c_void_p),
+        ("u_hi", C.c_void_p),
+        ("u_lo", C.c_void_p),
+    ]
+
+
 class ReadoutLayer(C.Structure):
     """``pt_readout_layer``."""
 
@@ -115,10 +129,12 @@ SIGNATURES = {
     "pt_aw_build": (i32, [i32, i32, C.POINTER(SparseStencil), f64, f64, f64, vp, vp, vp, vp, vp,
                           vp, sz, vp]),
     "pt_extrude_workspace_bytes": (sz, [i32, i32, i32, i32]),
-    "pt_extrude_rows": (i32, [i32, i32, C.POINTER(SparseStencil), i32, i32, vp, vp, vp, i32,
-                              C.POINTER(ExtrudeJob), vp, vp, sz, vp]),
-    "pt_extrude_batch": (i32, [i32, i32, C.POINTER(SparseStencil), i32, i32, vp, vp, vp, i32,
-                               vp, vp, vp, vp, vp, vp, vp, sz, vp]),
+    "pt_extrude_rows": (i32, [i32, i32, C.POINTER(SparseStencil), i32, i32, vp, vp,
+                              C.POINTER(ExtrudeAnchor), vp, i32, C.POINTER(ExtrudeJob), vp, vp,
+                              sz, vp]),
+    "pt_extrude_batch": (i32, [i32, i32, C.POINTER(SparseStencil), i32, i32, vp, vp,
+                               C.POINTER(ExtrudeAnchor), vp, i32, vp, vp, vp, vp, vp, vp, vp,
+                               sz, vp]),
     "pt_extrude_lo_bytes": (sz, [i32, i32, i32, i32]),
     "pt_extrude_lo_prepare": (i32, [i32, i32, i32, i32, vp, vp, sz, vp]),
     "pt_readout": (i32, [i32, i32, i32, i32, i32, C.POINTER(ReadoutLayer), vp, f32, vp, vp]),

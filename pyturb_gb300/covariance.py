@@ -32,7 +32,7 @@ from . import _lib
 from .backend import cuda_device, dptr, stream_handle, torch_module
 
 __all__ = ["phase_covariance", "build_operator", "build_extrusion", "seed_factor",
-           "sparse_points", "ExtrusionOperator"]
+           "sparse_points", "ExtrusionOperator", "AnchorTables", "dct_modes"]
 
 _NU = 5.0 / 6.0
 
@@ -175,6 +175,51 @@ def build_operator(width: int, stencil_rows: int, pixel_scale: float, L0: float,
         if M64 is not None:
             M64[:, Kz:] = torch.from_numpy(root).to(device=dev)
     return ExtrusionOperator(W, m, sparse, M, M64, S, Mlo)
+
+
+ANCHOR_MODES = 32
+
+
+def dct_modes(width: int, modes: int = ANCHOR_MODES) -> np.ndarray:
+    """Orthonormal DCT-II basis ``(modes, W)``: ``sqrt((2 - [i=0]) / W)
+    cos(pi i (w + 1/2) / W)``, the smooth modes of a row."""
+    w = (np.arange(width) + 0.5) / width
+    U = np.cos(np.pi * np.arange(modes)[:, None] * w[None, :]) * np.sqrt(2.0 / width)
+    U[0] *= np.sqrt(0.5)
+    return U
+
+
+class AnchorTables:
+    """Device tables of the float32 form's low-order anchor for a stack of
+    operators (one per outer-scale group): ``U^T A`` and ``U`` as (hi, lo)
+    float32 pairs and ``U^T B`` in float32, U the first 32 DCT-II modes."""
+
+    def __init__(self, ops: Sequence["ExtrusionOperator"]):
+        torch = torch_module()
+        dev = cuda_device()
+        W = ops[0].W
+        U = dct_modes(W)
+        p, pb = [], []
+        for op in ops:
+            if op.M64 is None:
+                raise ValueError("the anchor needs the float64 operator (want_float64=True)")
+            full = op.M64.cpu().numpy()
+            p.append(U @ full[:, :op.Kz])
+            pb.append(U @ full[:, op.Kz:])
+        p = np.stack(p)
+
+        def pair(x):
+            hi = x.astype(np.float32)
+            lo = (x - hi.astype(np.float64)).astype(np.float32)
+            return (torch.from_numpy(np.ascontiguousarray(hi)).to(dev),
+                    torch.from_numpy(np.ascontiguousarray(lo)).to(dev))
+
+        self.p_hi, self.p_lo = pair(p)
+        self.u_hi, self.u_lo = pair(U)
+        self.p_noise = torch.from_numpy(np.stack(pb).astype(np.float32)).to(dev)
+        self.struct = _lib.ExtrudeAnchor(modes=ANCHOR_MODES, pad=0, p_hi=dptr(self.p_hi),
+                                         p_lo=dptr(self.p_lo), p_noise=dptr(self.p_noise),
+                                         u_hi=dptr(self.u_hi), u_lo=dptr(self.u_lo))
 
 
 def build_extrusion(width: int, stencil_rows: int, pixel_scale: float, L0: float,

@@ -243,6 +243,112 @@ __global__ void k_lo_operand(const float* __restrict__ X, int J, int K, int Kz, 
   }
 }
 
+// ---------------------------------------------------------------- low-order anchor
+// The row recursion amplifies errors in the smooth, large-scale modes of a row
+// (its extrapolation is marginally stable there), so float32 rounding in the
+// product, random per step, still walks those modes away from the float64
+// result over hundreds of rows. The anchor recomputes the first R DCT-II
+// modes of every new row in double-float arithmetic (float32 pairs, Dekker /
+// Knuth error-free products and sums) from the same operand,
+//   d = U^T A z - U^T new + U^T B (bscale beta),
+// and adds U d to the row: the smooth modes then follow the float64 operator
+// while the rest stays float32. U^T A and U are given as (hi, lo) float32
+// pairs; the noise term is small and enters in float32.
+struct AnchorDev {
+  const float* ph;  // (G, R, Kz) hi parts of U^T A
+  const float* pl;  // (G, R, Kz) lo parts
+  const float* pb;  // (G, R, W) U^T B_unit
+  const float* uh;  // (R, W) hi parts of U
+  const float* ul;  // (R, W) lo parts
+};
+constexpr int kAnchorModes = 32;
+
+// s + h into (s, c): s the rounded sum, c collects the exact rounding error
+// (the _rn intrinsics keep the compiler from contracting or reordering the
+// error-free transformations)
+__device__ __forceinline__ void two_sum_acc(float& s, float& c, float h) {
+  const float t = __fadd_rn(s, h);
+  const float bv = __fsub_rn(t, s);
+  c += __fadd_rn(__fsub_rn(s, __fsub_rn(t, bv)), __fsub_rn(h, bv));
+  s = t;
+}
+
+template <int R>
+__global__ void __launch_bounds__(256)
+k_anchor(int W, int K, int Kz, int cap, int g, const RingDst dst, int J,
+         const float* __restrict__ X, const AnchorDev an, float* __restrict__ buf) {
+  const int j = blockIdx.x;
+  if (j >= J) return;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const float* x = X + (size_t)j * K;
+  float* row = buf + ((size_t)dst.d[j].x * cap + dst.d[j].y) * W;
+  const float* ph = an.ph + (size_t)g * R * Kz;
+  const float* pl = an.pl + (size_t)g * R * Kz;
+  const float* pb = an.pb + (size_t)g * R * W;
+  float s[R], c[R];
+#pragma unroll
+  for (int i = 0; i < R; ++i) s[i] = c[i] = 0.f;
+  for (int k = tid; k < Kz; k += 256) {  // + (U^T A) z
+    const float xv = x[k];
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+      const float a = __ldg(ph + (size_t)i * Kz + k);
+      const float h = __fmul_rn(a, xv);
+      c[i] += fmaf(__ldg(pl + (size_t)i * Kz + k), xv, fmaf(a, xv, -h));
+      two_sum_acc(s[i], c[i], h);
+    }
+  }
+  for (int w = tid; w < W; w += 256) {  // - U^T new + (U^T B) (bscale beta)
+    const float nv = -row[w], bv = x[Kz + w];
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+      const float u = __ldg(an.uh + (size_t)i * W + w);
+      const float h = __fmul_rn(u, nv);
+      c[i] += fmaf(__ldg(an.ul + (size_t)i * W + w), nv, fmaf(u, nv, -h)) +
+              __ldg(pb + (size_t)i * W + w) * bv;
+      two_sum_acc(s[i], c[i], h);
+    }
+  }
+  // fixed-order reduction: butterfly within warps, then the 8 warps in order
+  __shared__ float ws[8][R], wc[8][R];
+  __shared__ float d[R];
+#pragma unroll
+  for (int i = 0; i < R; ++i) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const float so = __shfl_xor_sync(0xffffffffu, s[i], o);
+      const float co = __shfl_xor_sync(0xffffffffu, c[i], o);
+      // the same pair of values in the same order on both lanes
+      const float a = (lane & o) ? so : s[i], b = (lane & o) ? s[i] : so;
+      const float ca = (lane & o) ? co : c[i], cb = (lane & o) ? c[i] : co;
+      float ss = a, cc = __fadd_rn(ca, cb);
+      two_sum_acc(ss, cc, b);
+      s[i] = ss;
+      c[i] = cc;
+    }
+    if (lane == 0) {
+      ws[warp][i] = s[i];
+      wc[warp][i] = c[i];
+    }
+  }
+  __syncthreads();
+  if (tid < R) {
+    float ss = 0.f, cc = 0.f;
+    for (int q = 0; q < 8; ++q) {
+      cc += wc[q][tid];
+      two_sum_acc(ss, cc, ws[q][tid]);
+    }
+    d[tid] = ss + cc;
+  }
+  __syncthreads();
+  for (int w = tid; w < W; w += 256) {
+    float v = 0.f;
+#pragma unroll
+    for (int i = 0; i < R; ++i) v = fmaf(__ldg(an.uh + (size_t)i * W + w), d[i], v);
+    row[w] += v;
+  }
+}
+
 // partial[z][j][r] = sum_{k in slice z} M[r][k] X[j][k]
 __global__ void __launch_bounds__(256)
 k_extrude_gemm(int W, int K, int J, int kslice, const float* __restrict__ M,
@@ -595,6 +701,7 @@ struct ExtrudeForm {
   const float* M;          // (G, W, K) FP32
   const uint8_t* tiles;    // tensor-core operator tiles
   const uint8_t* lo;       // FP32 form: 1-term tiles of A - (float)A, or NULL
+  const pt_extrude_anchor* anchor;  // FP32 form: low-order anchor, or NULL
 };
 
 static int extrude_jobs(const char* who, const ExtrudeForm& form, int W, int m,
@@ -686,7 +793,8 @@ static int extrude_jobs(const char* who, const ExtrudeForm& form, int W, int m,
         for (int q = 0; q < J; ++q) dst.d[q] = make_int2(jp.j[q].screen, jp.j[q].head);
         // FP32 only: the tensor-core gather's threads each make 8 consecutive
         // values, so summing the slices there costs more than the reduce
-        bool fuse = form.terms == 0 && pend.on && pend.J == J;
+        // (with the anchor every new row is anchored before it is read)
+        bool fuse = form.terms == 0 && !form.anchor && pend.on && pend.J == J;
         for (int q = 0; fuse && q < J; ++q)
           fuse = pend.dst.d[q].x == dst.d[q].x && (pend.dst.d[q].y + 1) % cap == dst.d[q].y;
         if (!fuse)
@@ -739,6 +847,16 @@ static int extrude_jobs(const char* who, const ExtrudeForm& form, int W, int m,
         pend.J = J;
         pend.nz = nz;
         pend.dst = dst;
+        if (form.anchor) {
+          if (int rc = flush()) return rc;
+          const AnchorDev an{form.anchor->p_hi, form.anchor->p_lo, form.anchor->p_noise,
+                             form.anchor->u_hi, form.anchor->u_lo};
+          {
+            ProfScope ps("k_anchor", s);
+            k_anchor<kAnchorModes><<<J, 256, 0, s>>>(W, K, Kz, cap, kv.first, dst, J, X, an, buf);
+          }
+          count_launch_e();
+        }
         count_launch_e(form.terms ? 1 : 2);
         if (int rc = check_launch(who)) return rc;
       }
@@ -849,15 +967,26 @@ extern "C" int pt_matmul_nt(int R, int K, int J, const float* M, const float* X,
   return check_launch("pt_matmul_nt");
 }
 
+static int anchor_ok(const char* who, const pt_extrude_anchor* a) {
+  if (!a) return PT_OK;
+  if (a->modes != kAnchorModes)
+    return fail(PT_ERR_ARG, std::string(who) + ": the anchor takes exactly 32 modes");
+  if (!a->p_hi || !a->p_lo || !a->p_noise || !a->u_hi || !a->u_lo)
+    return fail(PT_ERR_ARG, std::string(who) + ": anchor with a NULL table");
+  return PT_OK;
+}
+
 extern "C" int pt_extrude_rows(int W, int m, const pt_sparse_stencil* sparse, int cap, int G,
-                               const float* M, const void* lo_tiles, float* buf, int n_jobs,
+                               const float* M, const void* lo_tiles,
+                               const pt_extrude_anchor* anchor, float* buf, int n_jobs,
                                const pt_extrude_job* jobs, const float* noise, void* work,
                                size_t work_bytes, void* stream) {
   if (lo_tiles && ((uintptr_t)lo_tiles & 255) != 0)
     return fail(PT_ERR_ARG, "pt_extrude_rows: correction tiles must be 256-byte aligned");
-  return extrude_jobs("pt_extrude_rows", ExtrudeForm{0, M, nullptr, (const uint8_t*)lo_tiles}, W,
-                      m, sparse, cap, G, buf, n_jobs, jobs, noise, work, work_bytes,
-                      (cudaStream_t)stream);
+  if (int rc = anchor_ok("pt_extrude_rows", anchor)) return rc;
+  return extrude_jobs("pt_extrude_rows",
+                      ExtrudeForm{0, M, nullptr, (const uint8_t*)lo_tiles, anchor}, W, m, sparse,
+                      cap, G, buf, n_jobs, jobs, noise, work, work_bytes, (cudaStream_t)stream);
 }
 
 // Jobs of `counts[s]` row steps on every screen s, step-major (the order of
@@ -895,19 +1024,21 @@ static int batch_jobs(const char* who, int W, int cap, int S, const int32_t* gro
 }
 
 extern "C" int pt_extrude_batch(int W, int m, const pt_sparse_stencil* sparse, int cap,
-                                int n_groups, const float* M, const void* lo_tiles, float* buf,
-                                int S, const int32_t* group, const float* bscale,
-                                const uint64_t* key, int64_t* top, const int32_t* counts,
-                                const float* noise, void* work, size_t work_bytes,
-                                void* stream) {
+                                int n_groups, const float* M, const void* lo_tiles,
+                                const pt_extrude_anchor* anchor, float* buf, int S,
+                                const int32_t* group, const float* bscale, const uint64_t* key,
+                                int64_t* top, const int32_t* counts, const float* noise,
+                                void* work, size_t work_bytes, void* stream) {
   if (lo_tiles && ((uintptr_t)lo_tiles & 255) != 0)
     return fail(PT_ERR_ARG, "pt_extrude_batch: correction tiles must be 256-byte aligned");
+  if (int rc = anchor_ok("pt_extrude_batch", anchor)) return rc;
   std::vector<pt_extrude_job> jobs;
   if (int rc = batch_jobs("pt_extrude_batch", W, cap, S, group, bscale, key, top, counts, jobs))
     return rc;
-  return extrude_jobs("pt_extrude_batch", ExtrudeForm{0, M, nullptr, (const uint8_t*)lo_tiles}, W,
-                      m, sparse, cap, n_groups, buf, (int)jobs.size(), jobs.data(), noise, work,
-                      work_bytes, (cudaStream_t)stream);
+  return extrude_jobs("pt_extrude_batch",
+                      ExtrudeForm{0, M, nullptr, (const uint8_t*)lo_tiles, anchor}, W, m, sparse,
+                      cap, n_groups, buf, (int)jobs.size(), jobs.data(), noise, work, work_bytes,
+                      (cudaStream_t)stream);
 }
 
 extern "C" size_t pt_extrude_lo_bytes(int W, int m, int n_sparse, int n_groups) {
@@ -976,7 +1107,7 @@ extern "C" int pt_extrude_batch_tc(int W, int m, const pt_sparse_stencil* sparse
   if (int rc = batch_jobs("pt_extrude_batch_tc", W, cap, S, group, bscale, key, top, counts, jobs))
     return rc;
   return extrude_jobs("pt_extrude_batch_tc",
-                      ExtrudeForm{terms, nullptr, (const uint8_t*)tiles, nullptr}, W,
+                      ExtrudeForm{terms, nullptr, (const uint8_t*)tiles, nullptr, nullptr}, W,
                       m, sparse, cap, n_groups, buf, (int)jobs.size(), jobs.data(), noise, work,
                       work_bytes, (cudaStream_t)stream);
 }

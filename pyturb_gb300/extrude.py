@@ -30,7 +30,8 @@ import numpy as np
 from . import _lib
 from .backend import NoiseStream, cuda_device, dptr, stream_handle, torch_module, upload
 from .config import ExtrusionConfig
-from .covariance import build_extrusion, build_operator, phase_covariance, sparse_points
+from .covariance import (AnchorTables, build_extrusion, build_operator, phase_covariance,
+                         sparse_points)
 from .fourier import PhaseScreen
 
 __all__ = ["ExtrudedAtmosphere", "build_extrusion", "phase_covariance", "RingExtruder"]
@@ -100,14 +101,17 @@ class RingExtruder:
     float32 CUDA tensor, K = (m + 1) W + len(sparse). ``operator_lo``
     (``(G, W, Kz)`` float32, ``A - float32(A)``) makes the FP32 form add that
     correction each step, so that the recursion follows the float64
-    operator instead of accumulating the float32 rounding of ``A``."""
+    operator instead of accumulating the float32 rounding of ``A``.
+    ``anchor`` (``AnchorTables``) makes the FP32 form recompute the 32
+    smoothest modes of every new row in double-float arithmetic: the row
+    recursion amplifies float32 rounding in those modes over long runs."""
 
     FORMS = {"fp32": 0, "bf16x2": 2, "bf16x3": 3}
 
     def __init__(self, W: int, m: int, cap: int, operators: List[Tuple[np.ndarray, np.ndarray]],
                  groups: Sequence[int], bscale: Sequence[float], streams: Sequence[NoiseStream],
                  device_operator=None, form: str = "fp32",
-                 sparse: Sequence[Tuple[int, int]] = (), operator_lo=None):
+                 sparse: Sequence[Tuple[int, int]] = (), operator_lo=None, anchor=None):
         torch = torch_module()
         if form not in self.FORMS:
             raise ValueError(f"form must be one of {sorted(self.FORMS)}, got {form!r}")
@@ -134,6 +138,8 @@ class RingExtruder:
             raise ValueError(f"operator shape {tuple(self.M.shape)} does not match W={self.W}, "
                              f"m={self.m} and {self.ns} sparse points")
         self.G = int(self.M.shape[0])
+        self.anchor = anchor if self.terms == 0 else None
+        self._anchor = C.byref(anchor.struct) if self.anchor is not None else None
         self.M_lo = None
         self.lo_tiles = None
         if operator_lo is not None and self.terms == 0:
@@ -202,7 +208,7 @@ class RingExtruder:
                       dptr(self.work), self.work_bytes, stream_handle())
         else:
             _lib.call("pt_extrude_batch", self.W, self.m, self._sp, self.cap, self.G,
-                      dptr(self.M), dptr(self.lo_tiles), dptr(self.buf), self.S,
+                      dptr(self.M), dptr(self.lo_tiles), self._anchor, dptr(self.buf), self.S,
                       ptr(self._group), ptr(self._bscale),
                       ptr(self._key), ptr(self.top), ptr(counts), dptr(noise), dptr(self.work),
                       self.work_bytes, stream_handle())
@@ -314,7 +320,8 @@ class ExtrudedAtmosphere:
                 ops.append(build_operator(W, self.m, self.dx, float(L0), self.sparse,
                                           b_factor="eigh" if host_noise is not None
                                           else "cholesky", want_seed=self.boiling,
-                                          want_lo=extrude_form == "fp32"))
+                                          want_lo=extrude_form == "fp32",
+                                          want_float64=extrude_form == "fp32"))
             groups.append(op_index[key])
         streams = [NoiseStream(s, host_noise) for s in config.seeds]
         self._streams = streams
@@ -326,9 +333,13 @@ class ExtrudedAtmosphere:
         bscale = [float(r0) ** (-5.0 / 6.0) for r0 in config.layer_r0]
         torch = torch_module()
         lo = torch.stack([op.Mlo for op in ops]) if extrude_form == "fp32" else None
+        anchor = AnchorTables(ops) if extrude_form == "fp32" else None
         self._ring = RingExtruder(W, self.m, self.capacity, [], groups, bscale, streams,
                                   device_operator=torch.stack([op.M for op in ops]),
-                                  form=extrude_form, sparse=self.sparse, operator_lo=lo)
+                                  form=extrude_form, sparse=self.sparse, operator_lo=lo,
+                                  anchor=anchor)
+        for op in ops:  # the float64 twins were needed for the anchor only
+            op.M64 = None
         # seed each ring with a von Karman screen from the layer's own stream:
         # a W x W screen for the rows-only stencil (as the reference), a taller
         # one cropped to W columns when sparse points need older rows
@@ -352,7 +363,8 @@ class ExtrudedAtmosphere:
             self._scratch = RingExtruder(
                 W, self.m, self.capacity + self.m, [], [groups[i] for i in self._boil_layers],
                 [bscale[i] for i in self._boil_layers], self._queues,
-                device_operator=self._ring.M, form=extrude_form, operator_lo=self._ring.M_lo)
+                device_operator=self._ring.M, form=extrude_form, operator_lo=self._ring.M_lo,
+                anchor=self._ring.anchor)
 
     @property
     def _buf(self):

@@ -16,7 +16,7 @@ import numpy as np
 from . import _lib
 from .backend import NoiseStream, dptr, stream_handle, torch_module
 from .config import ScreenConfig
-from .covariance import build_operator, phase_covariance
+from .covariance import AnchorTables, build_operator, phase_covariance
 from .extrude import RingExtruder, compact_bounds
 from .fourier import PhaseScreen
 
@@ -51,13 +51,15 @@ class InfinitePhaseScreen:
         # the parity mode, the build's Cholesky factor otherwise)
         op = build_operator(self.n, self.stencil_rows, self.pixel_scale, self.L0,
                             b_factor="eigh" if host_noise is not None else "cholesky",
-                            want_lo=True)
+                            want_lo=True, want_float64=True)
         self._stream = NoiseStream(seed, host_noise)
         self._margin = self.stencil_rows + 6
         self._capacity = self.n + self._margin
         self._ring = RingExtruder(self.n, self.stencil_rows, self._capacity, [], [0],
                                   [self.r0 ** (-5.0 / 6.0)], [self._stream],
-                                  device_operator=op.M, operator_lo=op.Mlo)
+                                  device_operator=op.M, operator_lo=op.Mlo,
+                                  anchor=AnchorTables([op]))
+        op.M64 = None
         gen = PhaseScreen(n=self.n, pixel_scale=self.pixel_scale, r0=self.r0, L0=self.L0,
                           _stream=self._stream, host_noise=host_noise)
         self._ring.seed_rows(0, gen.generate())

@@ -32,8 +32,9 @@ def _layers():
     return r0s, winds, alts
 
 
-@pytest.mark.parametrize("columns", [0, 2])
-def test_batched_ring_extrusion_512_steps_vs_float64(columns):
+@pytest.mark.parametrize("columns,correct", [(0, "anchor+lo"), (2, "anchor+lo"), (0, "lo"),
+                                             (0, "none")])
+def test_batched_ring_extrusion_512_steps_vs_float64(columns, correct):
     import torch
 
     import pyturb_gb300 as G
@@ -53,10 +54,14 @@ def test_batched_ring_extrusion_512_steps_vs_float64(columns):
     S, chunk, chunks = 144, 128, 4
     cap = depth + chunk + 64
     bscale = [r ** (-5.0 / 6.0) for r in r0s] * 16
-    op = build_operator(W, m, DX, L0, sparse, b_factor="eigh", want_lo=True)
+    from pyturb_gb300.covariance import AnchorTables
+
+    op = build_operator(W, m, DX, L0, sparse, b_factor="eigh", want_lo=True, want_float64=True)
     ring = RingExtruder(W, m, cap, [], [0] * S, bscale,
                         [NoiseStream(500 + s, np.random.default_rng) for s in range(S)],
-                        device_operator=op.M, sparse=sparse, operator_lo=op.Mlo)
+                        device_operator=op.M, sparse=sparse,
+                        operator_lo=op.Mlo if "lo" in correct else None,
+                        anchor=AnchorTables([op]) if "anchor" in correct else None)
     # von Karman seed rows (device Philox), `depth` rows of history per screen
     seed_rows = []
     for s in range(S):
@@ -90,10 +95,11 @@ def test_batched_ring_extrusion_512_steps_vs_float64(columns):
         got = ring.buf[subset][:, phys].double().cpu().numpy()
         want = np.stack([R[s][t - chunk:t] for s in subset])
         errs.append(rel_l2(got, want))
-    print(f"sparse points {len(sparse)}: relative L2 per 128-step chunk " +
-          ", ".join(f"{e:.2e}" for e in errs))
+    print(f"sparse points {len(sparse)}, correction {correct}: relative L2 per 128-step chunk "
+          + ", ".join(f"{e:.2e}" for e in errs))
     assert t - depth == 512
-    assert max(errs) < TOL
+    if correct == "anchor+lo":  # the product configuration
+        assert max(errs) < TOL
 
 
 @pytest.mark.parametrize("columns", [0, 2])
