@@ -194,11 +194,13 @@ class AnchorTables:
     operators (one per outer-scale group): ``U^T A`` and ``U`` as (hi, lo)
     float32 pairs and ``U^T B`` in float32, U the first 32 DCT-II modes."""
 
-    def __init__(self, ops: Sequence["ExtrusionOperator"]):
+    def __init__(self, ops: Sequence["ExtrusionOperator"], modes: int = ANCHOR_MODES):
+        if modes not in (32, 64):
+            raise ValueError("the anchor takes 32 or 64 modes")
         torch = torch_module()
         dev = cuda_device()
         W = ops[0].W
-        U = dct_modes(W)
+        U = dct_modes(W, modes)
         p, pb = [], []
         for op in ops:
             if op.M64 is None:
@@ -217,7 +219,8 @@ class AnchorTables:
         self.p_hi, self.p_lo = pair(p)
         self.u_hi, self.u_lo = pair(U)
         self.p_noise = torch.from_numpy(np.stack(pb).astype(np.float32)).to(dev)
-        self.struct = _lib.ExtrudeAnchor(modes=ANCHOR_MODES, pad=0, p_hi=dptr(self.p_hi),
+        self.modes = modes
+        self.struct = _lib.ExtrudeAnchor(modes=modes, pad=0, p_hi=dptr(self.p_hi),
                                          p_lo=dptr(self.p_lo), p_noise=dptr(self.p_noise),
                                          u_hi=dptr(self.u_hi), u_lo=dptr(self.u_lo))
 

@@ -261,7 +261,6 @@ struct AnchorDev {
   const float* uh;  // (R, W) hi parts of U
   const float* ul;  // (R, W) lo parts
 };
-constexpr int kAnchorModes = 32;
 
 // s + h into (s, c): s the rounded sum, c collects the exact rounding error
 // (the _rn intrinsics keep the compiler from contracting or reordering the
@@ -853,7 +852,10 @@ static int extrude_jobs(const char* who, const ExtrudeForm& form, int W, int m,
                              form.anchor->u_hi, form.anchor->u_lo};
           {
             ProfScope ps("k_anchor", s);
-            k_anchor<kAnchorModes><<<J, 256, 0, s>>>(W, K, Kz, cap, kv.first, dst, J, X, an, buf);
+            if (form.anchor->modes == 32)
+              k_anchor<32><<<J, 256, 0, s>>>(W, K, Kz, cap, kv.first, dst, J, X, an, buf);
+            else
+              k_anchor<64><<<J, 256, 0, s>>>(W, K, Kz, cap, kv.first, dst, J, X, an, buf);
           }
           count_launch_e();
         }
@@ -969,8 +971,8 @@ extern "C" int pt_matmul_nt(int R, int K, int J, const float* M, const float* X,
 
 static int anchor_ok(const char* who, const pt_extrude_anchor* a) {
   if (!a) return PT_OK;
-  if (a->modes != kAnchorModes)
-    return fail(PT_ERR_ARG, std::string(who) + ": the anchor takes exactly 32 modes");
+  if (a->modes != 32 && a->modes != 64)
+    return fail(PT_ERR_ARG, std::string(who) + ": the anchor takes 32 or 64 modes");
   if (!a->p_hi || !a->p_lo || !a->p_noise || !a->u_hi || !a->u_lo)
     return fail(PT_ERR_ARG, std::string(who) + ": anchor with a NULL table");
   return PT_OK;
