@@ -272,79 +272,119 @@ __device__ __forceinline__ void two_sum_acc(float& s, float& c, float h) {
   s = t;
 }
 
+// The anchor's projections as one small double-float GEMM over the
+// concatenated columns [stencil (Kz) | noise (W) | new row (W)]:
+//   part[z][j][i] = sum over slice z of P'[i][k] x'_j[k],
+//   P' = [U^T A | U^T B | -U],  x'_j = [X_j[0, Kz) | X_j[Kz, K) | new_j],
+// so d = sum_z part is U^T A z + U^T B (bscale beta) - U^T new. A CTA
+// takes 16 jobs x all R modes over one K slice (each thread one job and
+// R/16 modes), staging 64-column chunks of x' and P' (hi, lo) in shared
+// memory; part holds (s, c) double-float pairs.
 template <int R>
 __global__ void __launch_bounds__(256)
-k_anchor(int W, int K, int Kz, int cap, int g, const RingDst dst, int J,
-         const float* __restrict__ X, const AnchorDev an, float* __restrict__ buf) {
-  const int j = blockIdx.x;
-  if (j >= J) return;
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const float* x = X + (size_t)j * K;
-  float* row = buf + ((size_t)dst.d[j].x * cap + dst.d[j].y) * W;
+k_anchor_gemm(int W, int K, int Kz, int cap, int g, int J, int kslice, const RingDst dst,
+              const float* __restrict__ X, const AnchorDev an, const float* __restrict__ buf,
+              float2* __restrict__ part) {
+  constexpr int KC = 64, MPT = R / 16;
+  __shared__ float xs[16][KC + 1];
+  __shared__ float phs[R][KC + 1], pls[R][KC + 1];
+  const int tid = threadIdx.x;
+  const int j0 = blockIdx.x * 16, z = blockIdx.y;
+  const int Kt = K + W;  // Kz + W + W
+  const int kb = z * kslice, ke = min(Kt, kb + kslice);
+  const int jl = tid >> 4, mi = tid & 15;
   const float* ph = an.ph + (size_t)g * R * Kz;
   const float* pl = an.pl + (size_t)g * R * Kz;
   const float* pb = an.pb + (size_t)g * R * W;
-  float s[R], c[R];
+  float s[MPT], c[MPT];
 #pragma unroll
-  for (int i = 0; i < R; ++i) s[i] = c[i] = 0.f;
-  for (int k = tid; k < Kz; k += 256) {  // + (U^T A) z
-    const float xv = x[k];
-#pragma unroll
-    for (int i = 0; i < R; ++i) {
-      const float a = __ldg(ph + (size_t)i * Kz + k);
-      const float h = __fmul_rn(a, xv);
-      c[i] += fmaf(__ldg(pl + (size_t)i * Kz + k), xv, fmaf(a, xv, -h));
-      two_sum_acc(s[i], c[i], h);
+  for (int u = 0; u < MPT; ++u) s[u] = c[u] = 0.f;
+  for (int k0 = kb; k0 < ke; k0 += KC) {
+    for (int e = tid; e < 16 * KC; e += 256) {
+      const int jj = e / KC, kk = e % KC, k = k0 + kk, j = j0 + jj;
+      float v = 0.f;
+      if (j < J && k < ke) {
+        if (k < K) v = X[(size_t)j * K + k];
+        else v = -buf[((size_t)dst.d[j].x * cap + dst.d[j].y) * W + (k - K)];
+      }
+      xs[jj][kk] = v;
     }
+    for (int e = tid; e < R * KC; e += 256) {
+      const int i = e / KC, kk = e % KC, k = k0 + kk;
+      float h = 0.f, l = 0.f;
+      if (k < ke) {
+        if (k < Kz) {
+          h = ph[(size_t)i * Kz + k];
+          l = pl[(size_t)i * Kz + k];
+        } else if (k < K) {
+          h = pb[(size_t)i * W + (k - Kz)];
+        } else {
+          h = an.uh[(size_t)i * W + (k - K)];
+          l = an.ul[(size_t)i * W + (k - K)];
+        }
+      }
+      phs[i][kk] = h;
+      pls[i][kk] = l;
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int kk = 0; kk < KC; ++kk) {
+      const float xv = xs[jl][kk];
+#pragma unroll
+      for (int u = 0; u < MPT; ++u) {
+        const int i = mi + 16 * u;
+        const float a = phs[i][kk];
+        const float h = __fmul_rn(a, xv);
+        c[u] += fmaf(pls[i][kk], xv, fmaf(a, xv, -h));
+        two_sum_acc(s[u], c[u], h);
+      }
+    }
+    __syncthreads();
   }
-  for (int w = tid; w < W; w += 256) {  // - U^T new + (U^T B) (bscale beta)
-    const float nv = -row[w], bv = x[Kz + w];
+  const int j = j0 + jl;
+  if (j < J)
 #pragma unroll
-    for (int i = 0; i < R; ++i) {
-      const float u = __ldg(an.uh + (size_t)i * W + w);
-      const float h = __fmul_rn(u, nv);
-      c[i] += fmaf(__ldg(an.ul + (size_t)i * W + w), nv, fmaf(u, nv, -h)) +
-              __ldg(pb + (size_t)i * W + w) * bv;
-      two_sum_acc(s[i], c[i], h);
-    }
+    for (int u = 0; u < MPT; ++u)
+      part[((size_t)z * J + j) * R + mi + 16 * u] = make_float2(s[u], c[u]);
+}
+
+// new rows += U d, d[j] = sum over slices of part (fixed order): a CTA takes
+// 16 jobs x 128 pixels with that stretch of U (float32: d is tiny) staged.
+template <int R>
+__global__ void __launch_bounds__(256)
+k_anchor_apply(int W, int cap, int J, int nsplit, const RingDst dst,
+               const float2* __restrict__ part, const float* __restrict__ uh,
+               float* __restrict__ buf) {
+  __shared__ float us[R][128];
+  __shared__ float ds[16][R];
+  const int tid = threadIdx.x;
+  const int w0 = blockIdx.x * 128, j0 = blockIdx.y * 16;
+  for (int e = tid; e < R * 128; e += 256) {
+    const int i = e / 128, w = w0 + e % 128;
+    us[i][e % 128] = w < W ? uh[(size_t)i * W + w] : 0.f;
   }
-  // fixed-order reduction: butterfly within warps, then the 8 warps in order
-  __shared__ float ws[8][R], wc[8][R];
-  __shared__ float d[R];
-#pragma unroll
-  for (int i = 0; i < R; ++i) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      const float so = __shfl_xor_sync(0xffffffffu, s[i], o);
-      const float co = __shfl_xor_sync(0xffffffffu, c[i], o);
-      // the same pair of values in the same order on both lanes
-      const float a = (lane & o) ? so : s[i], b = (lane & o) ? s[i] : so;
-      const float ca = (lane & o) ? co : c[i], cb = (lane & o) ? c[i] : co;
-      float ss = a, cc = __fadd_rn(ca, cb);
-      two_sum_acc(ss, cc, b);
-      s[i] = ss;
-      c[i] = cc;
-    }
-    if (lane == 0) {
-      ws[warp][i] = s[i];
-      wc[warp][i] = c[i];
-    }
-  }
-  __syncthreads();
-  if (tid < R) {
+  for (int e = tid; e < 16 * R; e += 256) {
+    const int jj = e / R, i = e % R, j = j0 + jj;
     float ss = 0.f, cc = 0.f;
-    for (int q = 0; q < 8; ++q) {
-      cc += wc[q][tid];
-      two_sum_acc(ss, cc, ws[q][tid]);
-    }
-    d[tid] = ss + cc;
+    if (j < J)
+      for (int z = 0; z < nsplit; ++z) {
+        const float2 p = part[((size_t)z * J + j) * R + i];
+        cc = __fadd_rn(cc, p.y);
+        two_sum_acc(ss, cc, p.x);
+      }
+    ds[jj][i] = ss + cc;
   }
   __syncthreads();
-  for (int w = tid; w < W; w += 256) {
+  const int wl = tid & 127;
+  const int w = w0 + wl;
+  if (w >= W) return;
+  for (int jj = tid >> 7; jj < 16; jj += 2) {
+    const int j = j0 + jj;
+    if (j >= J) break;
     float v = 0.f;
 #pragma unroll
-    for (int i = 0; i < R; ++i) v = fmaf(__ldg(an.uh + (size_t)i * W + w), d[i], v);
-    row[w] += v;
+    for (int i = 0; i < R; ++i) v = fmaf(us[i][wl], ds[jj][i], v);
+    buf[((size_t)dst.d[j].x * cap + dst.d[j].y) * W + w] += v;
   }
 }
 
@@ -672,9 +712,12 @@ using namespace pt;
 
 // FP32-form workspace: X (J, K) | correction B tiles | partials of the FP32
 // GEMM (up to kMaxSplitTiled slices) followed by those of the correction.
+// (the partials are followed by the anchor's (s, c) pairs: up to
+// kAnchorSplit x J x 64 float2)
+constexpr int kAnchorSplit = 32;
 struct Fp32Work {
   size_t x, lo_tiles, partial, total;
-  int lo_nz;
+  int lo_nz, max_nz;
 };
 static Fp32Work fp32_work(int W, int m, int n_sparse, int J) {
   Fp32Work w{};
@@ -682,8 +725,9 @@ static Fp32Work fp32_work(int W, int m, int n_sparse, int J) {
   w.x = al256((size_t)J * K * sizeof(float));
   w.lo_tiles = al256(tc_btile_bytes(W, Kz, J, 1));
   w.lo_nz = (int)(tc_partial_floats(W, Kz, J, 1) / ((size_t)J * W));
-  w.partial = al256((size_t)(std::max(kMaxSplit, kMaxSplitTiled) + w.lo_nz) * J * W *
-                    sizeof(float));
+  w.max_nz = std::max(kMaxSplit, kMaxSplitTiled) + w.lo_nz;
+  w.partial = al256((size_t)w.max_nz * J * W * sizeof(float)) +
+              al256((size_t)kAnchorSplit * J * 64 * sizeof(float2));
   w.total = w.x + w.lo_tiles + w.partial;
   return w;
 }
@@ -850,14 +894,28 @@ static int extrude_jobs(const char* who, const ExtrudeForm& form, int W, int m,
           if (int rc = flush()) return rc;
           const AnchorDev an{form.anchor->p_hi, form.anchor->p_lo, form.anchor->p_noise,
                              form.anchor->u_hi, form.anchor->u_lo};
+          const int R = form.anchor->modes, Kt = K + W;
+          const int jb = (J + 15) / 16;
+          const int nsplit = std::max(1, std::min(kAnchorSplit, (152 + jb - 1) / jb));
+          const int kslice = ((Kt + nsplit - 1) / nsplit + 63) / 64 * 64;
+          const int nz_a = (Kt + kslice - 1) / kslice;
+          float2* apart =
+              (float2*)((char*)partial + al256((size_t)fw.max_nz * J * W * sizeof(float)));
           {
             ProfScope ps("k_anchor", s);
-            if (form.anchor->modes == 32)
-              k_anchor<32><<<J, 256, 0, s>>>(W, K, Kz, cap, kv.first, dst, J, X, an, buf);
-            else
-              k_anchor<64><<<J, 256, 0, s>>>(W, K, Kz, cap, kv.first, dst, J, X, an, buf);
+            if (R == 32) {
+              k_anchor_gemm<32><<<dim3(jb, nz_a), 256, 0, s>>>(W, K, Kz, cap, kv.first, J, kslice,
+                                                               dst, X, an, buf, apart);
+              k_anchor_apply<32><<<dim3((W + 127) / 128, jb), 256, 0, s>>>(W, cap, J, nz_a, dst,
+                                                                          apart, an.uh, buf);
+            } else {
+              k_anchor_gemm<64><<<dim3(jb, nz_a), 256, 0, s>>>(W, K, Kz, cap, kv.first, J, kslice,
+                                                               dst, X, an, buf, apart);
+              k_anchor_apply<64><<<dim3((W + 127) / 128, jb), 256, 0, s>>>(W, cap, J, nz_a, dst,
+                                                                          apart, an.uh, buf);
+            }
           }
-          count_launch_e();
+          count_launch_e(2);
         }
         count_launch_e(form.terms ? 1 : 2);
         if (int rc = check_launch(who)) return rc;
