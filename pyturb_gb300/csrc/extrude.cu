@@ -296,9 +296,10 @@ k_anchor_gemm(int W, int K, int Kz, int cap, int g, int J, int kslice, const Rin
   const float* ph = an.ph + (size_t)g * R * Kz;
   const float* pl = an.pl + (size_t)g * R * Kz;
   const float* pb = an.pb + (size_t)g * R * W;
-  float s[MPT], c[MPT];
+  // two accumulators per mode (even / odd columns): independent chains
+  float s[2][MPT], c[2][MPT];
 #pragma unroll
-  for (int u = 0; u < MPT; ++u) s[u] = c[u] = 0.f;
+  for (int u = 0; u < MPT; ++u) s[0][u] = c[0][u] = s[1][u] = c[1][u] = 0.f;
   for (int k0 = kb; k0 < ke; k0 += KC) {
     for (int e = tid; e < 16 * KC; e += 256) {
       const int jj = e / KC, kk = e % KC, k = k0 + kk, j = j0 + jj;
@@ -328,15 +329,18 @@ k_anchor_gemm(int W, int K, int Kz, int cap, int g, int J, int kslice, const Rin
     }
     __syncthreads();
 #pragma unroll 4
-    for (int kk = 0; kk < KC; ++kk) {
-      const float xv = xs[jl][kk];
+    for (int kk = 0; kk < KC; kk += 2) {
 #pragma unroll
-      for (int u = 0; u < MPT; ++u) {
-        const int i = mi + 16 * u;
-        const float a = phs[i][kk];
-        const float h = __fmul_rn(a, xv);
-        c[u] += fmaf(pls[i][kk], xv, fmaf(a, xv, -h));
-        two_sum_acc(s[u], c[u], h);
+      for (int q = 0; q < 2; ++q) {
+        const float xv = xs[jl][kk + q];
+#pragma unroll
+        for (int u = 0; u < MPT; ++u) {
+          const int i = mi + 16 * u;
+          const float a = phs[i][kk + q];
+          const float h = __fmul_rn(a, xv);
+          c[q][u] += fmaf(pls[i][kk + q], xv, fmaf(a, xv, -h));
+          two_sum_acc(s[q][u], c[q][u], h);
+        }
       }
     }
     __syncthreads();
@@ -344,8 +348,11 @@ k_anchor_gemm(int W, int K, int Kz, int cap, int g, int J, int kslice, const Rin
   const int j = j0 + jl;
   if (j < J)
 #pragma unroll
-    for (int u = 0; u < MPT; ++u)
-      part[((size_t)z * J + j) * R + mi + 16 * u] = make_float2(s[u], c[u]);
+    for (int u = 0; u < MPT; ++u) {
+      float ss = s[0][u], cc = __fadd_rn(c[0][u], c[1][u]);
+      two_sum_acc(ss, cc, s[1][u]);
+      part[((size_t)z * J + j) * R + mi + 16 * u] = make_float2(ss, cc);
+    }
 }
 
 // new rows += U d, d[j] = sum over slices of part (fixed order): a CTA takes
@@ -714,7 +721,7 @@ using namespace pt;
 // GEMM (up to kMaxSplitTiled slices) followed by those of the correction.
 // (the partials are followed by the anchor's (s, c) pairs: up to
 // kAnchorSplit x J x 64 float2)
-constexpr int kAnchorSplit = 32;
+constexpr int kAnchorSplit = 96;
 struct Fp32Work {
   size_t x, lo_tiles, partial, total;
   int lo_nz, max_nz;
@@ -896,7 +903,8 @@ static int extrude_jobs(const char* who, const ExtrudeForm& form, int W, int m,
                              form.anchor->u_hi, form.anchor->u_lo};
           const int R = form.anchor->modes, Kt = K + W;
           const int jb = (J + 15) / 16;
-          const int nsplit = std::max(1, std::min(kAnchorSplit, (152 + jb - 1) / jb));
+          // about four CTAs per SM: the double-float chains are latency-bound
+          const int nsplit = std::max(1, std::min(kAnchorSplit, (4 * 152 + jb - 1) / jb));
           const int kslice = ((Kt + nsplit - 1) / nsplit + 63) / 64 * 64;
           const int nz_a = (Kt + kslice - 1) / kslice;
           float2* apart =
