@@ -280,14 +280,56 @@ __device__ __forceinline__ void two_sum_acc(float& s, float& c, float h) {
 // takes 16 jobs x all R modes over one K slice (each thread one job and
 // R/16 modes), staging 64-column chunks of x' and P' (hi, lo) in shared
 // memory; part holds (s, c) double-float pairs.
+// packed float32 pairs (two modes per instruction)
+typedef unsigned long long f2p;
+__device__ __forceinline__ f2p pack2(float lo, float hi) {
+  f2p r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+  return r;
+}
+__device__ __forceinline__ void unpack2(f2p v, float& lo, float& hi) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ f2p padd(f2p a, f2p b) {
+  f2p d;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f2p psub(f2p a, f2p b) {
+  f2p d;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f2p pmul(f2p a, f2p b) {
+  f2p d;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f2p pfma(f2p a, f2p b, f2p c) {
+  f2p d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
+}
+// (s, c) += a x for two modes at once: exact product a_hi x = h + e, the
+// lo part a_lo x in float32, h added to s by an error-free two-sum
+__device__ __forceinline__ void pmac(f2p& s, f2p& c, f2p ah, f2p al, f2p x2) {
+  const f2p h = pmul(ah, x2);
+  const f2p e = pfma(ah, x2, h ^ 0x8000000080000000ull);
+  const f2p t = padd(s, h);
+  const f2p bv = psub(t, s);
+  c = padd(c, pfma(al, x2, e));
+  c = padd(c, padd(psub(s, psub(t, bv)), psub(h, bv)));
+  s = t;
+}
+
 template <int R>
 __global__ void __launch_bounds__(256)
 k_anchor_gemm(int W, int K, int Kz, int cap, int g, int J, int kslice, const RingDst dst,
               const float* __restrict__ X, const AnchorDev an, const float* __restrict__ buf,
               float2* __restrict__ part) {
-  constexpr int KC = 64, MPT = R / 16;
+  constexpr int KC = 64, NPAIR = R / 32;  // mode pairs (i, i + 16) per thread
   __shared__ float xs[16][KC + 1];
-  __shared__ float phs[R][KC + 1], pls[R][KC + 1];
+  __shared__ f2p phs[KC][R / 2], pls[KC][R / 2];  // [k][pair p = mi + 16 q]
   const int tid = threadIdx.x;
   const int j0 = blockIdx.x * 16, z = blockIdx.y;
   const int Kt = K + W;  // Kz + W + W
@@ -296,10 +338,24 @@ k_anchor_gemm(int W, int K, int Kz, int cap, int g, int J, int kslice, const Rin
   const float* ph = an.ph + (size_t)g * R * Kz;
   const float* pl = an.pl + (size_t)g * R * Kz;
   const float* pb = an.pb + (size_t)g * R * W;
-  // two accumulators per mode (even / odd columns): independent chains
-  float s[2][MPT], c[2][MPT];
+  auto table = [&](int i, int k, float& h, float& l) {
+    h = 0.f;
+    l = 0.f;
+    if (k >= ke) return;
+    if (k < Kz) {
+      h = ph[(size_t)i * Kz + k];
+      l = pl[(size_t)i * Kz + k];
+    } else if (k < K) {
+      h = pb[(size_t)i * W + (k - Kz)];
+    } else {
+      h = an.uh[(size_t)i * W + (k - K)];
+      l = an.ul[(size_t)i * W + (k - K)];
+    }
+  };
+  // two accumulator chains per pair (even / odd columns)
+  f2p s[2][NPAIR], c[2][NPAIR];
 #pragma unroll
-  for (int u = 0; u < MPT; ++u) s[0][u] = c[0][u] = s[1][u] = c[1][u] = 0.f;
+  for (int q = 0; q < NPAIR; ++q) s[0][q] = c[0][q] = s[1][q] = c[1][q] = 0ull;
   for (int k0 = kb; k0 < ke; k0 += KC) {
     for (int e = tid; e < 16 * KC; e += 256) {
       const int jj = e / KC, kk = e % KC, k = k0 + kk, j = j0 + jj;
@@ -310,37 +366,25 @@ k_anchor_gemm(int W, int K, int Kz, int cap, int g, int J, int kslice, const Rin
       }
       xs[jj][kk] = v;
     }
-    for (int e = tid; e < R * KC; e += 256) {
-      const int i = e / KC, kk = e % KC, k = k0 + kk;
-      float h = 0.f, l = 0.f;
-      if (k < ke) {
-        if (k < Kz) {
-          h = ph[(size_t)i * Kz + k];
-          l = pl[(size_t)i * Kz + k];
-        } else if (k < K) {
-          h = pb[(size_t)i * W + (k - Kz)];
-        } else {
-          h = an.uh[(size_t)i * W + (k - K)];
-          l = an.ul[(size_t)i * W + (k - K)];
-        }
-      }
-      phs[i][kk] = h;
-      pls[i][kk] = l;
+    for (int e = tid; e < (R / 2) * KC; e += 256) {
+      const int p = e / KC, kk = e % KC, k = k0 + kk;
+      const int i0 = (p & 15) + 32 * (p >> 4);  // modes i0 and i0 + 16
+      float h0, l0, h1, l1;
+      table(i0, k, h0, l0);
+      table(i0 + 16, k, h1, l1);
+      phs[kk][p] = pack2(h0, h1);
+      pls[kk][p] = pack2(l0, l1);
     }
     __syncthreads();
 #pragma unroll 4
     for (int kk = 0; kk < KC; kk += 2) {
 #pragma unroll
-      for (int q = 0; q < 2; ++q) {
-        const float xv = xs[jl][kk + q];
+      for (int r = 0; r < 2; ++r) {
+        const float xv = xs[jl][kk + r];
+        const f2p x2 = pack2(xv, xv);
 #pragma unroll
-        for (int u = 0; u < MPT; ++u) {
-          const int i = mi + 16 * u;
-          const float a = phs[i][kk + q];
-          const float h = __fmul_rn(a, xv);
-          c[q][u] += fmaf(pls[i][kk + q], xv, fmaf(a, xv, -h));
-          two_sum_acc(s[q][u], c[q][u], h);
-        }
+        for (int q = 0; q < NPAIR; ++q)
+          pmac(s[r][q], c[r][q], phs[kk + r][mi + 16 * q], pls[kk + r][mi + 16 * q], x2);
       }
     }
     __syncthreads();
@@ -348,10 +392,18 @@ k_anchor_gemm(int W, int K, int Kz, int cap, int g, int J, int kslice, const Rin
   const int j = j0 + jl;
   if (j < J)
 #pragma unroll
-    for (int u = 0; u < MPT; ++u) {
-      float ss = s[0][u], cc = __fadd_rn(c[0][u], c[1][u]);
-      two_sum_acc(ss, cc, s[1][u]);
-      part[((size_t)z * J + j) * R + mi + 16 * u] = make_float2(ss, cc);
+    for (int q = 0; q < NPAIR; ++q) {
+      float s0[2], c0[2], s1[2], c1[2];
+      unpack2(s[0][q], s0[0], s0[1]);
+      unpack2(c[0][q], c0[0], c0[1]);
+      unpack2(s[1][q], s1[0], s1[1]);
+      unpack2(c[1][q], c1[0], c1[1]);
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        float ss = s0[h], cc = __fadd_rn(c0[h], c1[h]);
+        two_sum_acc(ss, cc, s1[h]);
+        part[((size_t)z * J + j) * R + mi + 16 * h + 32 * q] = make_float2(ss, cc);
+      }
     }
 }
 
