@@ -263,17 +263,17 @@ size_t pt_extrude_workspace_bytes(int W, int m, int n_sparse, int max_jobs_per_s
  * hundreds of rows. With an anchor, each new row's first `modes` (32 or 64)
  * DCT-II modes U (orthonormal, U[i][w] = sqrt((2 - [i=0]) / W)
  * cos(pi i (w + 1/2) / W)) are recomputed in double-float arithmetic and
- * set: row += U (U^T A z + U^T B (bscale beta) - U^T row). Tables (device
- * f32, hi + lo = the float64 value): p_hi/p_lo (G, modes, Kz) = U^T A,
- * p_noise (G, modes, W) = U^T B_unit, u_hi/u_lo (modes, W) = U. */
+ * set: row += U (U^T A z + U^T B (bscale beta) - U^T row). Tables (device):
+ * t_hi / t_lo (G, Kt, modes) f32, Kt = K + W, hi + lo = the float64 value:
+ * row k holds column k of [U^T A | U^T B_unit | -U], its modes stored in
+ * pairs (i, i + 16): 0, 16, 1, 17, ..., 15, 31 (then 32, 48, ..., 47, 63);
+ * u (modes, W) f32 = U. 8-byte aligned. */
 typedef struct {
   int32_t modes;
   int32_t pad;
-  const float* p_hi;
-  const float* p_lo;
-  const float* p_noise;
-  const float* u_hi;
-  const float* u_lo;
+  const float* t_hi;
+  const float* t_lo;
+  const float* u;
 } pt_extrude_anchor;
 
 int pt_extrude_batch(int W, int m, const pt_sparse_stencil* sparse, int cap, int n_groups,

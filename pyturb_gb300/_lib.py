@@ -77,11 +77,9 @@ class ExtrudeAnchor(C.Structure):
     _fields_ = [
         ("modes", C.c_int32),
         ("pad", C.c_int32),
-        ("p_hi", C.c_void_p),
-        ("p_lo", C.c_void_p),
-        ("p_noise", C.c_void_p),
-        ("u_hi", C.c_void_p),
-        ("u_lo", C.c_void_p),
+        ("t_hi", C.c_void_p),
+        ("t_lo", C.c_void_p),
+        ("u", C.c_void_p),
     ]
 
 

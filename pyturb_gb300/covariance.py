@@ -189,10 +189,17 @@ def dct_modes(width: int, modes: int = ANCHOR_MODES) -> np.ndarray:
     return U
 
 
+def pair_order(modes: int) -> np.ndarray:
+    """Mode order of an anchor table row: pairs (i, i + 16) of each block of 32."""
+    return np.array([b + q + 16 * h for b in range(0, modes, 32) for q in range(16)
+                     for h in range(2)])
+
+
 class AnchorTables:
     """Device tables of the float32 form's low-order anchor for a stack of
-    operators (one per outer-scale group): ``U^T A`` and ``U`` as (hi, lo)
-    float32 pairs and ``U^T B`` in float32, U the first 32 DCT-II modes."""
+    operators (one per outer-scale group): the columns of
+    ``[U^T A | U^T B | -U]`` as (hi, lo) float32 pairs, modes in pair order,
+    and ``U`` in float32, U the first 32 (or 64) DCT-II modes."""
 
     def __init__(self, ops: Sequence["ExtrusionOperator"], modes: int = ANCHOR_MODES):
         if modes not in (32, 64):
@@ -201,28 +208,23 @@ class AnchorTables:
         dev = cuda_device()
         W = ops[0].W
         U = dct_modes(W, modes)
-        p, pb = [], []
+        order = pair_order(modes)
+        tabs = []
         for op in ops:
             if op.M64 is None:
                 raise ValueError("the anchor needs the float64 operator (want_float64=True)")
-            full = op.M64.cpu().numpy()
-            p.append(U @ full[:, :op.Kz])
-            pb.append(U @ full[:, op.Kz:])
-        p = np.stack(p)
-
-        def pair(x):
-            hi = x.astype(np.float32)
-            lo = (x - hi.astype(np.float64)).astype(np.float32)
-            return (torch.from_numpy(np.ascontiguousarray(hi)).to(dev),
-                    torch.from_numpy(np.ascontiguousarray(lo)).to(dev))
-
-        self.p_hi, self.p_lo = pair(p)
-        self.u_hi, self.u_lo = pair(U)
-        self.p_noise = torch.from_numpy(np.stack(pb).astype(np.float32)).to(dev)
+            full = op.M64.cpu().numpy()                         # (W, K) = [A | B]
+            cols = np.concatenate([U @ full, -U], axis=1)       # (modes, K + W)
+            tabs.append(cols[order].T)                          # (K + W, modes)
+        t = np.ascontiguousarray(np.stack(tabs))
+        hi = t.astype(np.float32)
+        lo = (t - hi.astype(np.float64)).astype(np.float32)
+        self.t_hi = torch.from_numpy(hi).to(dev)
+        self.t_lo = torch.from_numpy(lo).to(dev)
+        self.u = torch.from_numpy(U.astype(np.float32)).to(dev)
         self.modes = modes
-        self.struct = _lib.ExtrudeAnchor(modes=modes, pad=0, p_hi=dptr(self.p_hi),
-                                         p_lo=dptr(self.p_lo), p_noise=dptr(self.p_noise),
-                                         u_hi=dptr(self.u_hi), u_lo=dptr(self.u_lo))
+        self.struct = _lib.ExtrudeAnchor(modes=modes, pad=0, t_hi=dptr(self.t_hi),
+                                         t_lo=dptr(self.t_lo), u=dptr(self.u))
 
 
 def build_extrusion(width: int, stencil_rows: int, pixel_scale: float, L0: float,

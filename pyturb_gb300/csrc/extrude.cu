@@ -254,32 +254,6 @@ __global__ void k_lo_operand(const float* __restrict__ X, int J, int K, int Kz, 
 // and adds U d to the row: the smooth modes then follow the float64 operator
 // while the rest stays float32. U^T A and U are given as (hi, lo) float32
 // pairs; the noise term is small and enters in float32.
-struct AnchorDev {
-  const float* ph;  // (G, R, Kz) hi parts of U^T A
-  const float* pl;  // (G, R, Kz) lo parts
-  const float* pb;  // (G, R, W) U^T B_unit
-  const float* uh;  // (R, W) hi parts of U
-  const float* ul;  // (R, W) lo parts
-};
-
-// s + h into (s, c): s the rounded sum, c collects the exact rounding error
-// (the _rn intrinsics keep the compiler from contracting or reordering the
-// error-free transformations)
-__device__ __forceinline__ void two_sum_acc(float& s, float& c, float h) {
-  const float t = __fadd_rn(s, h);
-  const float bv = __fsub_rn(t, s);
-  c += __fadd_rn(__fsub_rn(s, __fsub_rn(t, bv)), __fsub_rn(h, bv));
-  s = t;
-}
-
-// The anchor's projections as one small double-float GEMM over the
-// concatenated columns [stencil (Kz) | noise (W) | new row (W)]:
-//   part[z][j][i] = sum over slice z of P'[i][k] x'_j[k],
-//   P' = [U^T A | U^T B | -U],  x'_j = [X_j[0, Kz) | X_j[Kz, K) | new_j],
-// so d = sum_z part is U^T A z + U^T B (bscale beta) - U^T new. A CTA
-// takes 16 jobs x all R modes over one K slice (each thread one job and
-// R/16 modes), staging 64-column chunks of x' and P' (hi, lo) in shared
-// memory; part holds (s, c) double-float pairs.
 // packed float32 pairs (two modes per instruction)
 typedef unsigned long long f2p;
 __device__ __forceinline__ f2p pack2(float lo, float hi) {
@@ -322,36 +296,47 @@ __device__ __forceinline__ void pmac(f2p& s, f2p& c, f2p ah, f2p al, f2p x2) {
   s = t;
 }
 
+struct AnchorDev {
+  const f2p* th;   // (G, Kt, R/2) hi parts of [U^T A | U^T B | -U]^T, mode pairs
+  const f2p* tl;   // (G, Kt, R/2) lo parts
+  const float* u;  // (R, W) U in float32 (the correction is tiny)
+};
+
+// s + h into (s, c): s the rounded sum, c collects the exact rounding error
+// (the _rn intrinsics keep the compiler from contracting or reordering the
+// error-free transformations)
+__device__ __forceinline__ void two_sum_acc(float& s, float& c, float h) {
+  const float t = __fadd_rn(s, h);
+  const float bv = __fsub_rn(t, s);
+  c += __fadd_rn(__fsub_rn(s, __fsub_rn(t, bv)), __fsub_rn(h, bv));
+  s = t;
+}
+
+// The anchor's projections as one small double-float GEMM over the
+// concatenated columns [stencil (Kz) | noise (W) | new row (W)]:
+//   part[z][j][i] = sum over slice z of P'[i][k] x'_j[k],
+//   P' = [U^T A | U^T B | -U],  x'_j = [X_j[0, Kz) | X_j[Kz, K) | new_j],
+// so d = sum_z part is U^T A z + U^T B (bscale beta) - U^T new. The table
+// P'^T is prepared once on the host as (hi, lo) float32 rows of R values per
+// column k, the modes of a row stored in pairs (i, i + 16), so a chunk of 64
+// columns is one contiguous copy. A CTA takes 16 jobs x all R modes over one
+// K slice (each thread one job and R/16 modes), staging 64-column chunks of
+// x' and P' in shared memory; part holds (s, c) double-float pairs.
 template <int R>
 __global__ void __launch_bounds__(256)
-k_anchor_gemm(int W, int K, int Kz, int cap, int g, int J, int kslice, const RingDst dst,
+k_anchor_gemm(int W, int K, int cap, int g, int J, int kslice, const RingDst dst,
               const float* __restrict__ X, const AnchorDev an, const float* __restrict__ buf,
               float2* __restrict__ part) {
-  constexpr int KC = 64, NPAIR = R / 32;  // mode pairs (i, i + 16) per thread
+  constexpr int KC = 64, NP2 = R / 2, NPAIR = R / 32;  // mode pairs per thread
   __shared__ float xs[16][KC + 1];
-  __shared__ f2p phs[KC][R / 2], pls[KC][R / 2];  // [k][pair p = mi + 16 q]
+  __shared__ f2p phs[KC][NP2], pls[KC][NP2];
   const int tid = threadIdx.x;
   const int j0 = blockIdx.x * 16, z = blockIdx.y;
-  const int Kt = K + W;  // Kz + W + W
+  const int Kt = K + W;
   const int kb = z * kslice, ke = min(Kt, kb + kslice);
   const int jl = tid >> 4, mi = tid & 15;
-  const float* ph = an.ph + (size_t)g * R * Kz;
-  const float* pl = an.pl + (size_t)g * R * Kz;
-  const float* pb = an.pb + (size_t)g * R * W;
-  auto table = [&](int i, int k, float& h, float& l) {
-    h = 0.f;
-    l = 0.f;
-    if (k >= ke) return;
-    if (k < Kz) {
-      h = ph[(size_t)i * Kz + k];
-      l = pl[(size_t)i * Kz + k];
-    } else if (k < K) {
-      h = pb[(size_t)i * W + (k - Kz)];
-    } else {
-      h = an.uh[(size_t)i * W + (k - K)];
-      l = an.ul[(size_t)i * W + (k - K)];
-    }
-  };
+  const f2p* th = an.th + (size_t)g * Kt * NP2;
+  const f2p* tl = an.tl + (size_t)g * Kt * NP2;
   // two accumulator chains per pair (even / odd columns)
   f2p s[2][NPAIR], c[2][NPAIR];
 #pragma unroll
@@ -360,20 +345,17 @@ k_anchor_gemm(int W, int K, int Kz, int cap, int g, int J, int kslice, const Rin
     for (int e = tid; e < 16 * KC; e += 256) {
       const int jj = e / KC, kk = e % KC, k = k0 + kk, j = j0 + jj;
       float v = 0.f;
-      if (j < J && k < ke) {
-        if (k < K) v = X[(size_t)j * K + k];
-        else v = -buf[((size_t)dst.d[j].x * cap + dst.d[j].y) * W + (k - K)];
-      }
+      if (j < J && k < ke)
+        v = k < K ? X[(size_t)j * K + k]
+                  : buf[((size_t)dst.d[j].x * cap + dst.d[j].y) * W + (k - K)];
       xs[jj][kk] = v;
     }
-    for (int e = tid; e < (R / 2) * KC; e += 256) {
-      const int p = e / KC, kk = e % KC, k = k0 + kk;
-      const int i0 = (p & 15) + 32 * (p >> 4);  // modes i0 and i0 + 16
-      float h0, l0, h1, l1;
-      table(i0, k, h0, l0);
-      table(i0 + 16, k, h1, l1);
-      phs[kk][p] = pack2(h0, h1);
-      pls[kk][p] = pack2(l0, l1);
+    // the table rows k0 .. k0 + 63 are contiguous: straight copies
+    for (int e = tid; e < KC * NP2; e += 256) {
+      const int kk = e / NP2, k = k0 + kk;
+      const bool in = k < ke;
+      phs[kk][e % NP2] = in ? th[(size_t)k0 * NP2 + e] : 0ull;
+      pls[kk][e % NP2] = in ? tl[(size_t)k0 * NP2 + e] : 0ull;
     }
     __syncthreads();
 #pragma unroll 4
@@ -408,11 +390,11 @@ k_anchor_gemm(int W, int K, int Kz, int cap, int g, int J, int kslice, const Rin
 }
 
 // new rows += U d, d[j] = sum over slices of part (fixed order): a CTA takes
-// 16 jobs x 128 pixels with that stretch of U (float32: d is tiny) staged.
+// 16 jobs x 128 pixels with that stretch of U staged.
 template <int R>
 __global__ void __launch_bounds__(256)
 k_anchor_apply(int W, int cap, int J, int nsplit, const RingDst dst,
-               const float2* __restrict__ part, const float* __restrict__ uh,
+               const float2* __restrict__ part, const float* __restrict__ u,
                float* __restrict__ buf) {
   __shared__ float us[R][128];
   __shared__ float ds[16][R];
@@ -420,16 +402,22 @@ k_anchor_apply(int W, int cap, int J, int nsplit, const RingDst dst,
   const int w0 = blockIdx.x * 128, j0 = blockIdx.y * 16;
   for (int e = tid; e < R * 128; e += 256) {
     const int i = e / 128, w = w0 + e % 128;
-    us[i][e % 128] = w < W ? uh[(size_t)i * W + w] : 0.f;
+    us[i][e % 128] = w < W ? u[(size_t)i * W + w] : 0.f;
   }
   for (int e = tid; e < 16 * R; e += 256) {
     const int jj = e / R, i = e % R, j = j0 + jj;
     float ss = 0.f, cc = 0.f;
     if (j < J)
-      for (int z = 0; z < nsplit; ++z) {
-        const float2 p = part[((size_t)z * J + j) * R + i];
-        cc = __fadd_rn(cc, p.y);
-        two_sum_acc(ss, cc, p.x);
+      for (int z0 = 0; z0 < nsplit; z0 += 8) {  // loads of 8 slices in flight at once
+        float2 pz[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+          pz[q] = z0 + q < nsplit ? part[((size_t)(z0 + q) * J + j) * R + i] : make_float2(0.f, 0.f);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          cc = __fadd_rn(cc, pz[q].y);
+          two_sum_acc(ss, cc, pz[q].x);
+        }
       }
     ds[jj][i] = ss + cc;
   }
@@ -437,13 +425,18 @@ k_anchor_apply(int W, int cap, int J, int nsplit, const RingDst dst,
   const int wl = tid & 127;
   const int w = w0 + wl;
   if (w >= W) return;
-  for (int jj = tid >> 7; jj < 16; jj += 2) {
-    const int j = j0 + jj;
-    if (j >= J) break;
-    float v = 0.f;
+  const int jh = tid >> 7;  // this thread's jobs: jh, jh + 2, ..., jh + 14
+  float v[8];
 #pragma unroll
-    for (int i = 0; i < R; ++i) v = fmaf(us[i][wl], ds[jj][i], v);
-    buf[((size_t)dst.d[j].x * cap + dst.d[j].y) * W + w] += v;
+  for (int q = 0; q < 8; ++q) {
+    v[q] = 0.f;
+#pragma unroll
+    for (int i = 0; i < R; ++i) v[q] = fmaf(us[i][wl], ds[jh + 2 * q][i], v[q]);
+  }
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    const int j = j0 + jh + 2 * q;
+    if (j < J) buf[((size_t)dst.d[j].x * cap + dst.d[j].y) * W + w] += v[q];
   }
 }
 
@@ -951,8 +944,8 @@ static int extrude_jobs(const char* who, const ExtrudeForm& form, int W, int m,
         pend.dst = dst;
         if (form.anchor) {
           if (int rc = flush()) return rc;
-          const AnchorDev an{form.anchor->p_hi, form.anchor->p_lo, form.anchor->p_noise,
-                             form.anchor->u_hi, form.anchor->u_lo};
+          const AnchorDev an{(const f2p*)form.anchor->t_hi, (const f2p*)form.anchor->t_lo,
+                             form.anchor->u};
           const int R = form.anchor->modes, Kt = K + W;
           const int jb = (J + 15) / 16;
           // about four CTAs per SM: the double-float chains are latency-bound
@@ -964,15 +957,15 @@ static int extrude_jobs(const char* who, const ExtrudeForm& form, int W, int m,
           {
             ProfScope ps("k_anchor", s);
             if (R == 32) {
-              k_anchor_gemm<32><<<dim3(jb, nz_a), 256, 0, s>>>(W, K, Kz, cap, kv.first, J, kslice,
+              k_anchor_gemm<32><<<dim3(jb, nz_a), 256, 0, s>>>(W, K, cap, kv.first, J, kslice,
                                                                dst, X, an, buf, apart);
               k_anchor_apply<32><<<dim3((W + 127) / 128, jb), 256, 0, s>>>(W, cap, J, nz_a, dst,
-                                                                          apart, an.uh, buf);
+                                                                          apart, an.u, buf);
             } else {
-              k_anchor_gemm<64><<<dim3(jb, nz_a), 256, 0, s>>>(W, K, Kz, cap, kv.first, J, kslice,
+              k_anchor_gemm<64><<<dim3(jb, nz_a), 256, 0, s>>>(W, K, cap, kv.first, J, kslice,
                                                                dst, X, an, buf, apart);
               k_anchor_apply<64><<<dim3((W + 127) / 128, jb), 256, 0, s>>>(W, cap, J, nz_a, dst,
-                                                                          apart, an.uh, buf);
+                                                                          apart, an.u, buf);
             }
           }
           count_launch_e(2);
@@ -1091,8 +1084,10 @@ static int anchor_ok(const char* who, const pt_extrude_anchor* a) {
   if (!a) return PT_OK;
   if (a->modes != 32 && a->modes != 64)
     return fail(PT_ERR_ARG, std::string(who) + ": the anchor takes 32 or 64 modes");
-  if (!a->p_hi || !a->p_lo || !a->p_noise || !a->u_hi || !a->u_lo)
+  if (!a->t_hi || !a->t_lo || !a->u)
     return fail(PT_ERR_ARG, std::string(who) + ": anchor with a NULL table");
+  if ((((uintptr_t)a->t_hi) | ((uintptr_t)a->t_lo)) & 7)
+    return fail(PT_ERR_ARG, std::string(who) + ": anchor tables must be 8-byte aligned");
   return PT_OK;
 }
 

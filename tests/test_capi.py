@@ -45,7 +45,7 @@ def test_struct_layouts_match_header():
     assert C.sizeof(_lib.ExtrudeJob) == 48
     assert C.sizeof(_lib.ReadoutLayer) == 56
     assert C.sizeof(_lib.SparseStencil) == 4 + 2 * 4 * _lib.PT_MAX_SPARSE
-    assert C.sizeof(_lib.ExtrudeAnchor) == 48
+    assert C.sizeof(_lib.ExtrudeAnchor) == 32
 
 
 def _status(name, *args):
