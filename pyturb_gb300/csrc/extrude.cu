@@ -404,22 +404,43 @@ k_anchor_apply(int W, int cap, int J, int nsplit, const RingDst dst,
     const int i = e / 128, w = w0 + e % 128;
     us[i][e % 128] = w < W ? u[(size_t)i * W + w] : 0.f;
   }
-  for (int e = tid; e < 16 * R; e += 256) {
+  // d for the CTA's 16 jobs: warp q takes (job, mode) pairs q, q + 8, ...;
+  // lane l loads slices l, l + 32, ... and the lanes combine in a fixed
+  // butterfly order (deterministic)
+  const int lane = tid & 31, warp = tid >> 5;
+  for (int e = warp; e < 16 * R; e += 8) {
     const int jj = e / R, i = e % R, j = j0 + jj;
     float ss = 0.f, cc = 0.f;
-    if (j < J)
-      for (int z0 = 0; z0 < nsplit; z0 += 8) {  // loads of 8 slices in flight at once
-        float2 pz[8];
+    if (j < J) {
+      float2 pz[3];
 #pragma unroll
-        for (int q = 0; q < 8; ++q)
-          pz[q] = z0 + q < nsplit ? part[((size_t)(z0 + q) * J + j) * R + i] : make_float2(0.f, 0.f);
-#pragma unroll
-        for (int q = 0; q < 8; ++q) {
-          cc = __fadd_rn(cc, pz[q].y);
-          two_sum_acc(ss, cc, pz[q].x);
-        }
+      for (int q = 0; q < 3; ++q) {
+        const int z = lane + 32 * q;
+        pz[q] = z < nsplit ? part[((size_t)z * J + j) * R + i] : make_float2(0.f, 0.f);
       }
-    ds[jj][i] = ss + cc;
+#pragma unroll
+      for (int q = 0; q < 3; ++q) {
+        cc = __fadd_rn(cc, pz[q].y);
+        two_sum_acc(ss, cc, pz[q].x);
+      }
+      for (int z = lane + 96; z < nsplit; z += 32) {
+        const float2 p = part[((size_t)z * J + j) * R + i];
+        cc = __fadd_rn(cc, p.y);
+        two_sum_acc(ss, cc, p.x);
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const float so = __shfl_xor_sync(0xffffffffu, ss, o);
+        const float co = __shfl_xor_sync(0xffffffffu, cc, o);
+        // the same operands in the same order on both lanes of a pair
+        const float a = (lane & o) ? so : ss, b = (lane & o) ? ss : so;
+        float s2 = a, c2 = (lane & o) ? __fadd_rn(co, cc) : __fadd_rn(cc, co);
+        two_sum_acc(s2, c2, b);
+        ss = s2;
+        cc = c2;
+      }
+    }
+    if (lane == 0) ds[jj][i] = ss + cc;
   }
   __syncthreads();
   const int wl = tid & 127;
