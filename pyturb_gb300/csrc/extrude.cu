@@ -324,25 +324,25 @@ __device__ __forceinline__ void two_sum_acc(float& s, float& c, float h) {
 // x' and P' in shared memory; part holds (s, c) double-float pairs.
 template <int R>
 __global__ void __launch_bounds__(256)
-k_anchor_gemm(int W, int K, int cap, int g, int J, int kslice, const RingDst dst,
+k_anchor_gemm(int W, int K, int Kz, int cap, int g, int J, int kslice, const RingDst dst,
               const float* __restrict__ X, const AnchorDev an, const float* __restrict__ buf,
               float2* __restrict__ part) {
-  constexpr int KC = 64, NP2 = R / 2, NPAIR = R / 32;  // mode pairs per thread
-  __shared__ float xs[16][KC + 1];
+  // (64 modes: 32-column chunks keep the static shared memory under 48 KB)
+  constexpr int KC = R == 64 ? 32 : 64, NP2 = R / 2, JT = 64, JPT = JT * NP2 / 256;
+  __shared__ float xs[JT][KC + 1];
   __shared__ f2p phs[KC][NP2], pls[KC][NP2];
   const int tid = threadIdx.x;
-  const int j0 = blockIdx.x * 16, z = blockIdx.y;
+  const int j0 = blockIdx.x * JT, z = blockIdx.y;
   const int Kt = K + W;
   const int kb = z * kslice, ke = min(Kt, kb + kslice);
-  const int jl = tid >> 4, mi = tid & 15;
+  const int p = tid % NP2, jt = (tid / NP2) * JPT;  // this thread: pair p, jobs jt .. jt + JPT - 1
   const f2p* th = an.th + (size_t)g * Kt * NP2;
   const f2p* tl = an.tl + (size_t)g * Kt * NP2;
-  // two accumulator chains per pair (even / odd columns)
-  f2p s[2][NPAIR], c[2][NPAIR];
+  f2p s[JPT], c[JPT];
 #pragma unroll
-  for (int q = 0; q < NPAIR; ++q) s[0][q] = c[0][q] = s[1][q] = c[1][q] = 0ull;
+  for (int q = 0; q < JPT; ++q) s[q] = c[q] = 0ull;
   for (int k0 = kb; k0 < ke; k0 += KC) {
-    for (int e = tid; e < 16 * KC; e += 256) {
+    for (int e = tid; e < JT * KC; e += 256) {
       const int jj = e / KC, kk = e % KC, k = k0 + kk, j = j0 + jj;
       float v = 0.f;
       if (j < J && k < ke)
@@ -350,114 +350,89 @@ k_anchor_gemm(int W, int K, int cap, int g, int J, int kslice, const RingDst dst
                   : buf[((size_t)dst.d[j].x * cap + dst.d[j].y) * W + (k - K)];
       xs[jj][kk] = v;
     }
-    // the table rows k0 .. k0 + 63 are contiguous: straight copies
+    // the table rows k0 .. k0 + KC - 1 are contiguous: straight copies
     for (int e = tid; e < KC * NP2; e += 256) {
-      const int kk = e / NP2, k = k0 + kk;
-      const bool in = k < ke;
-      phs[kk][e % NP2] = in ? th[(size_t)k0 * NP2 + e] : 0ull;
-      pls[kk][e % NP2] = in ? tl[(size_t)k0 * NP2 + e] : 0ull;
+      const bool in = k0 + e / NP2 < ke;
+      phs[e / NP2][e % NP2] = in ? th[(size_t)k0 * NP2 + e] : 0ull;
+      pls[e / NP2][e % NP2] = in ? tl[(size_t)k0 * NP2 + e] : 0ull;
     }
     __syncthreads();
-#pragma unroll 4
-    for (int kk = 0; kk < KC; kk += 2) {
+    const int kn = min(KC, ke - k0);
+    for (int kk = 0; kk < kn; ++kk) {
+      const f2p ah = phs[kk][p];
+      const int k = k0 + kk;
+      if (k >= Kz && k < K) {
+        // noise columns: U^T B (bscale beta) is ~1% of the row and its
+        // rounding random from row to row, so plain float32 suffices
 #pragma unroll
-      for (int r = 0; r < 2; ++r) {
-        const float xv = xs[jl][kk + r];
-        const f2p x2 = pack2(xv, xv);
+        for (int q = 0; q < JPT; ++q) {
+          const float xv = xs[jt + q][kk];
+          c[q] = pfma(ah, pack2(xv, xv), c[q]);
+        }
+      } else {
+        const f2p al = pls[kk][p];
 #pragma unroll
-        for (int q = 0; q < NPAIR; ++q)
-          pmac(s[r][q], c[r][q], phs[kk + r][mi + 16 * q], pls[kk + r][mi + 16 * q], x2);
+        for (int q = 0; q < JPT; ++q) {
+          const float xv = xs[jt + q][kk];
+          pmac(s[q], c[q], ah, al, pack2(xv, xv));
+        }
       }
     }
     __syncthreads();
   }
-  const int j = j0 + jl;
-  if (j < J)
+  // pair p = modes (i0, i0 + 16), i0 = (p & 15) + 32 (p >> 4)
+  const int i0 = (p & 15) + 32 * (p >> 4);
 #pragma unroll
-    for (int q = 0; q < NPAIR; ++q) {
-      float s0[2], c0[2], s1[2], c1[2];
-      unpack2(s[0][q], s0[0], s0[1]);
-      unpack2(c[0][q], c0[0], c0[1]);
-      unpack2(s[1][q], s1[0], s1[1]);
-      unpack2(c[1][q], c1[0], c1[1]);
-#pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        float ss = s0[h], cc = __fadd_rn(c0[h], c1[h]);
-        two_sum_acc(ss, cc, s1[h]);
-        part[((size_t)z * J + j) * R + mi + 16 * h + 32 * q] = make_float2(ss, cc);
-      }
-    }
+  for (int q = 0; q < JPT; ++q) {
+    const int j = j0 + jt + q;
+    if (j >= J) break;
+    float s0, s1, c0, c1;
+    unpack2(s[q], s0, s1);
+    unpack2(c[q], c0, c1);
+    part[((size_t)z * J + j) * R + i0] = make_float2(s0, c0);
+    part[((size_t)z * J + j) * R + i0 + 16] = make_float2(s1, c1);
+  }
 }
 
-// new rows += U d, d[j] = sum over slices of part (fixed order): a CTA takes
-// 16 jobs x 128 pixels with that stretch of U staged.
+// new row += U d, d = sum over the slices of part (fixed order), one CTA per
+// job: warp w reduces modes w, w + 8, ... (lanes over slices, then a fixed
+// butterfly), then every thread corrects its pixels.
 template <int R>
 __global__ void __launch_bounds__(256)
 k_anchor_apply(int W, int cap, int J, int nsplit, const RingDst dst,
                const float2* __restrict__ part, const float* __restrict__ u,
                float* __restrict__ buf) {
-  __shared__ float us[R][128];
-  __shared__ float ds[16][R];
-  const int tid = threadIdx.x;
-  const int w0 = blockIdx.x * 128, j0 = blockIdx.y * 16;
-  for (int e = tid; e < R * 128; e += 256) {
-    const int i = e / 128, w = w0 + e % 128;
-    us[i][e % 128] = w < W ? u[(size_t)i * W + w] : 0.f;
-  }
-  // d for the CTA's 16 jobs: warp q takes (job, mode) pairs q, q + 8, ...;
-  // lane l loads slices l, l + 32, ... and the lanes combine in a fixed
-  // butterfly order (deterministic)
-  const int lane = tid & 31, warp = tid >> 5;
-  for (int e = warp; e < 16 * R; e += 8) {
-    const int jj = e / R, i = e % R, j = j0 + jj;
+  __shared__ float ds[R];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int j = blockIdx.x;
+  if (j >= J) return;
+  for (int i = warp; i < R; i += 8) {
     float ss = 0.f, cc = 0.f;
-    if (j < J) {
-      float2 pz[3];
-#pragma unroll
-      for (int q = 0; q < 3; ++q) {
-        const int z = lane + 32 * q;
-        pz[q] = z < nsplit ? part[((size_t)z * J + j) * R + i] : make_float2(0.f, 0.f);
-      }
-#pragma unroll
-      for (int q = 0; q < 3; ++q) {
-        cc = __fadd_rn(cc, pz[q].y);
-        two_sum_acc(ss, cc, pz[q].x);
-      }
-      for (int z = lane + 96; z < nsplit; z += 32) {
-        const float2 p = part[((size_t)z * J + j) * R + i];
-        cc = __fadd_rn(cc, p.y);
-        two_sum_acc(ss, cc, p.x);
-      }
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        const float so = __shfl_xor_sync(0xffffffffu, ss, o);
-        const float co = __shfl_xor_sync(0xffffffffu, cc, o);
-        // the same operands in the same order on both lanes of a pair
-        const float a = (lane & o) ? so : ss, b = (lane & o) ? ss : so;
-        float s2 = a, c2 = (lane & o) ? __fadd_rn(co, cc) : __fadd_rn(cc, co);
-        two_sum_acc(s2, c2, b);
-        ss = s2;
-        cc = c2;
-      }
+    for (int z = lane; z < nsplit; z += 32) {
+      const float2 q = part[((size_t)z * J + j) * R + i];
+      cc = __fadd_rn(cc, q.y);
+      two_sum_acc(ss, cc, q.x);
     }
-    if (lane == 0) ds[jj][i] = ss + cc;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const float so = __shfl_xor_sync(0xffffffffu, ss, o);
+      const float co = __shfl_xor_sync(0xffffffffu, cc, o);
+      // the same operands in the same order on both lanes of a pair
+      const float a = (lane & o) ? so : ss, b = (lane & o) ? ss : so;
+      float s2 = a, c2 = (lane & o) ? __fadd_rn(co, cc) : __fadd_rn(cc, co);
+      two_sum_acc(s2, c2, b);
+      ss = s2;
+      cc = c2;
+    }
+    if (lane == 0) ds[i] = ss + cc;
   }
   __syncthreads();
-  const int wl = tid & 127;
-  const int w = w0 + wl;
-  if (w >= W) return;
-  const int jh = tid >> 7;  // this thread's jobs: jh, jh + 2, ..., jh + 14
-  float v[8];
+  float* row = buf + ((size_t)dst.d[j].x * cap + dst.d[j].y) * W;
+  for (int w = tid; w < W; w += 256) {
+    float v = 0.f;
 #pragma unroll
-  for (int q = 0; q < 8; ++q) {
-    v[q] = 0.f;
-#pragma unroll
-    for (int i = 0; i < R; ++i) v[q] = fmaf(us[i][wl], ds[jh + 2 * q][i], v[q]);
-  }
-#pragma unroll
-  for (int q = 0; q < 8; ++q) {
-    const int j = j0 + jh + 2 * q;
-    if (j < J) buf[((size_t)dst.d[j].x * cap + dst.d[j].y) * W + w] += v[q];
+    for (int i = 0; i < R; ++i) v = fmaf(__ldg(u + (size_t)i * W + w), ds[i], v);
+    row[w] += v;
   }
 }
 
@@ -968,9 +943,10 @@ static int extrude_jobs(const char* who, const ExtrudeForm& form, int W, int m,
           const AnchorDev an{(const f2p*)form.anchor->t_hi, (const f2p*)form.anchor->t_lo,
                              form.anchor->u};
           const int R = form.anchor->modes, Kt = K + W;
-          const int jb = (J + 15) / 16;
-          // about four CTAs per SM: the double-float chains are latency-bound
-          const int nsplit = std::max(1, std::min(kAnchorSplit, (4 * 152 + jb - 1) / jb));
+          const int jb = (J + 63) / 64;
+          // about two CTAs per SM, chunks of 64 columns
+          const int nsplit = std::max(1, std::min(std::min(kAnchorSplit, (Kt + 63) / 64),
+                                                  (2 * 152 + jb - 1) / jb));
           const int kslice = ((Kt + nsplit - 1) / nsplit + 63) / 64 * 64;
           const int nz_a = (Kt + kslice - 1) / kslice;
           float2* apart =
@@ -978,15 +954,13 @@ static int extrude_jobs(const char* who, const ExtrudeForm& form, int W, int m,
           {
             ProfScope ps("k_anchor", s);
             if (R == 32) {
-              k_anchor_gemm<32><<<dim3(jb, nz_a), 256, 0, s>>>(W, K, cap, kv.first, J, kslice,
-                                                               dst, X, an, buf, apart);
-              k_anchor_apply<32><<<dim3((W + 127) / 128, jb), 256, 0, s>>>(W, cap, J, nz_a, dst,
-                                                                          apart, an.u, buf);
+              k_anchor_gemm<32><<<dim3(jb, nz_a), 256, 0, s>>>(W, K, Kz, cap, kv.first, J,
+                                                               kslice, dst, X, an, buf, apart);
+              k_anchor_apply<32><<<J, 256, 0, s>>>(W, cap, J, nz_a, dst, apart, an.u, buf);
             } else {
-              k_anchor_gemm<64><<<dim3(jb, nz_a), 256, 0, s>>>(W, K, cap, kv.first, J, kslice,
-                                                               dst, X, an, buf, apart);
-              k_anchor_apply<64><<<dim3((W + 127) / 128, jb), 256, 0, s>>>(W, cap, J, nz_a, dst,
-                                                                          apart, an.u, buf);
+              k_anchor_gemm<64><<<dim3(jb, nz_a), 256, 0, s>>>(W, K, Kz, cap, kv.first, J,
+                                                               kslice, dst, X, an, buf, apart);
+              k_anchor_apply<64><<<J, 256, 0, s>>>(W, cap, J, nz_a, dst, apart, an.u, buf);
             }
           }
           count_launch_e(2);
