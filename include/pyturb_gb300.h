@@ -219,13 +219,20 @@ typedef struct {
  *     recursion on the float64 operator (pt_extrude_lo_prepare), or NULL;
  *   seed (Kz, Kz) f32 = L (L L^T = C_zz, Kz = m W + count), or NULL;
  *   sigma (W, W) f64 = Ls Ls^T, or NULL.
+ * With `increments` the stencil part is returned in increment form, the
+ * operand of pt_extrude_* with increments set: the stencil rows become
+ * differences d_i = row_i - row_{i+1} (oldest first) and the newest row r1,
+ * the sparse values s_p - r1[c_p], and the r1 block holds S - I (S = the sum
+ * of the row blocks) plus each sparse weight at its column, so that
+ * new row = r1 + M . operand. The product then forms only a small correction
+ * to r1, and its float32 rounding is small in proportion.
  * `jitter` adds jitter * C(0) to the stencil diagonal. A non-positive pivot
  * of the stencil block returns PT_ERR_NUMERIC; pivots of the conditional
  * block at or below 1e-13 C(0) zero their column. Synchronises `stream`. */
 size_t pt_aw_workspace_bytes(int W, int m, const pt_sparse_stencil* sparse);
 int pt_aw_build(int W, int m, const pt_sparse_stencil* sparse, double pixel_scale, double L0,
-                double jitter, float* M, double* M64, float* Mlo, float* seed, double* sigma,
-                void* work, size_t work_bytes, void* stream);
+                double jitter, int increments, float* M, double* M64, float* Mlo, float* seed,
+                double* sigma, void* work, size_t work_bytes, void* stream);
 
 /* One Assemat-Wilson row step for a set of ring-buffer screens
  * (_ExtrudeLayer._extrude_one, src/pyturb/extrude.py:424-430;
@@ -264,8 +271,9 @@ size_t pt_extrude_workspace_bytes(int W, int m, int n_sparse, int max_jobs_per_s
  * DCT-II modes U (orthonormal, U[i][w] = sqrt((2 - [i=0]) / W)
  * cos(pi i (w + 1/2) / W)) are recomputed in double-float arithmetic and
  * set: row += U (U^T A z + U^T B (bscale beta) - U^T row). Tables (device):
- * t_hi / t_lo (G, Kt, modes) f32, Kt = K + W, hi + lo = the float64 value:
- * row k holds column k of [U^T A | U^T B_unit | -U], its modes stored in
+ * t_hi / t_lo (G, Kt, modes) f32, Kt = K + W (K + 2 W in the increment
+ * form), hi + lo = the float64 value: row k holds column k of
+ * [U^T A | U^T B_unit | -U (| U for r1)], its modes stored in
  * pairs (i, i + 16): 0, 16, 1, 17, ..., 15, 31 (then 32, 48, ..., 47, 63);
  * u (modes, W) f32 = U. 8-byte aligned. */
 typedef struct {
@@ -276,16 +284,24 @@ typedef struct {
   const float* u;
 } pt_extrude_anchor;
 
-int pt_extrude_batch(int W, int m, const pt_sparse_stencil* sparse, int cap, int n_groups,
-                     const float* M, const void* lo_tiles, const pt_extrude_anchor* anchor,
-                     float* buf, int S, const int32_t* group, const float* bscale,
-                     const uint64_t* key, int64_t* top, const int32_t* counts,
-                     const float* noise, void* work, size_t work_bytes, void* stream);
+/* `increments` (no reference counterpart): M is in the increment form of
+ * pt_aw_build, the operand holds row differences and the new row is the
+ * newest stencil row plus the product. The reference multiplies the rows
+ * themselves; the increment form keeps the float32 product a small
+ * correction, so its rounding no longer walks the row recursion away from
+ * the float64 result over long runs. */
+int pt_extrude_batch(int W, int m, const pt_sparse_stencil* sparse, int increments, int cap,
+                     int n_groups, const float* M, const void* lo_tiles,
+                     const pt_extrude_anchor* anchor, float* buf, int S, const int32_t* group,
+                     const float* bscale, const uint64_t* key, int64_t* top,
+                     const int32_t* counts, const float* noise, void* work, size_t work_bytes,
+                     void* stream);
 
-int pt_extrude_rows(int W, int m, const pt_sparse_stencil* sparse, int cap, int n_groups,
-                    const float* M, const void* lo_tiles, const pt_extrude_anchor* anchor,
-                    float* buf, int n_jobs, const pt_extrude_job* jobs, const float* noise,
-                    void* work, size_t work_bytes, void* stream);
+int pt_extrude_rows(int W, int m, const pt_sparse_stencil* sparse, int increments, int cap,
+                    int n_groups, const float* M, const void* lo_tiles,
+                    const pt_extrude_anchor* anchor, float* buf, int n_jobs,
+                    const pt_extrude_job* jobs, const float* noise, void* work,
+                    size_t work_bytes, void* stream);
 
 /* Operator correction of the float32 form (no reference counterpart): the
  * reference's float32 path multiplies by float32(A), whose rounding is a
@@ -354,8 +370,8 @@ size_t pt_extrude_tc_operator_bytes(int W, int m, int n_sparse, int n_groups, in
 int pt_extrude_tc_prepare(int W, int m, int n_sparse, int n_groups, const float* M, int terms,
                           void* tiles, size_t tiles_bytes, void* stream);
 size_t pt_extrude_tc_workspace_bytes(int W, int m, int n_sparse, int max_jobs, int terms);
-int pt_extrude_batch_tc(int W, int m, const pt_sparse_stencil* sparse, int cap, int n_groups,
-                        const void* tiles, int terms, float* buf, int n_screens,
+int pt_extrude_batch_tc(int W, int m, const pt_sparse_stencil* sparse, int increments, int cap,
+                        int n_groups, const void* tiles, int terms, float* buf, int n_screens,
                         const int32_t* group, const float* bscale, const uint64_t* key,
                         int64_t* top, const int32_t* counts, const float* noise, void* work,
                         size_t work_bytes, void* stream);

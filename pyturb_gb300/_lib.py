@@ -124,13 +124,13 @@ SIGNATURES = {
     "pt_lgs_zoom": (i32, [i32, i32, i32, i32, vp, vp, vp, f32, vp, vp]),
     "pt_boil_step": (i32, [vp, i32, vp, vp, vp, vp, vp, vp, f64, vp, vp, u64, u64, vp]),
     "pt_aw_workspace_bytes": (sz, [i32, i32, C.POINTER(SparseStencil)]),
-    "pt_aw_build": (i32, [i32, i32, C.POINTER(SparseStencil), f64, f64, f64, vp, vp, vp, vp, vp,
-                          vp, sz, vp]),
+    "pt_aw_build": (i32, [i32, i32, C.POINTER(SparseStencil), f64, f64, f64, i32, vp, vp, vp, vp,
+                          vp, vp, sz, vp]),
     "pt_extrude_workspace_bytes": (sz, [i32, i32, i32, i32]),
-    "pt_extrude_rows": (i32, [i32, i32, C.POINTER(SparseStencil), i32, i32, vp, vp,
+    "pt_extrude_rows": (i32, [i32, i32, C.POINTER(SparseStencil), i32, i32, i32, vp, vp,
                               C.POINTER(ExtrudeAnchor), vp, i32, C.POINTER(ExtrudeJob), vp, vp,
                               sz, vp]),
-    "pt_extrude_batch": (i32, [i32, i32, C.POINTER(SparseStencil), i32, i32, vp, vp,
+    "pt_extrude_batch": (i32, [i32, i32, C.POINTER(SparseStencil), i32, i32, i32, vp, vp,
                                C.POINTER(ExtrudeAnchor), vp, i32, vp, vp, vp, vp, vp, vp, vp,
                                sz, vp]),
     "pt_extrude_lo_bytes": (sz, [i32, i32, i32, i32]),
@@ -154,8 +154,8 @@ SIGNATURES = {
     "pt_extrude_tc_operator_bytes": (sz, [i32, i32, i32, i32, i32]),
     "pt_extrude_tc_prepare": (i32, [i32, i32, i32, i32, vp, i32, vp, sz, vp]),
     "pt_extrude_tc_workspace_bytes": (sz, [i32, i32, i32, i32, i32]),
-    "pt_extrude_batch_tc": (i32, [i32, i32, C.POINTER(SparseStencil), i32, i32, vp, i32, vp, i32,
-                                  vp, vp, vp, vp, vp, vp, vp, sz, vp]),
+    "pt_extrude_batch_tc": (i32, [i32, i32, C.POINTER(SparseStencil), i32, i32, i32, vp, i32, vp,
+                                  i32, vp, vp, vp, vp, vp, vp, vp, sz, vp]),
     "pt_synth_adj_pack": (i32, [i32, i32, i32, i32, f32, vp, vp, vp]),
     "pt_synth_adj_phasors": (i32, [i32, f64, i32, i32, vp, vp, vp, vp]),
     "pt_synth_adj_spectra": (i32, [i32, i32, i32, vp, vp, vp, vp, vp]),

@@ -111,11 +111,13 @@ class ExtrusionOperator:
     (``(W, Kz)``, ``Kz = m W + len(sparse)``) and the stencil factor ``S``
     (float32 ``(Kz, Kz)``, ``S S^T = C_zz``), all at unit r0."""
 
-    def __init__(self, W: int, m: int, sparse, M, M64=None, S=None, Mlo=None):
+    def __init__(self, W: int, m: int, sparse, M, M64=None, S=None, Mlo=None,
+                 increments: bool = False):
         self.W, self.m = int(W), int(m)
         self.sparse = list(sparse)
         self.Kz = self.m * self.W + len(self.sparse)
         self.M, self.M64, self.S, self.Mlo = M, M64, S, Mlo
+        self.increments = bool(increments)
 
     def host(self, r0: float = 1.0) -> Tuple[np.ndarray, np.ndarray]:
         """``(A, B)`` as float64 host arrays, ``B`` scaled by r0^(-5/6)."""
@@ -127,14 +129,17 @@ class ExtrusionOperator:
 def build_operator(width: int, stencil_rows: int, pixel_scale: float, L0: float,
                    sparse: Sequence[Tuple[int, int]] = (), b_factor: str = "cholesky",
                    want_seed: bool = False, want_float64: bool = False,
-                   want_lo: bool = False) -> ExtrusionOperator:
+                   want_lo: bool = False, increments: bool = False) -> ExtrusionOperator:
     """Build ``[A | B]`` for extruding one ``width``-pixel row from the stencil
     (``stencil_rows`` full rows below it, then the ``sparse`` points) at unit
     r0, in FP64 on the GPU. ``b_factor``: ``"cholesky"`` (the build's own
     factor) or ``"eigh"`` (eigen square root of the same conditional
     covariance, the reference's choice). A stencil covariance that is not
     numerically positive definite is retried with a growing diagonal load
-    (1e-12 ... 1e-8 of the variance), with a warning."""
+    (1e-12 ... 1e-8 of the variance), with a warning. ``increments`` returns
+    the stencil part in increment form (row differences and the newest row;
+    the new row is the newest stencil row plus the product), which keeps a
+    float32 recursion on the float64 one over long runs."""
     if b_factor not in ("cholesky", "eigh"):
         raise ValueError("b_factor must be 'cholesky' or 'eigh'")
     if not np.isfinite(L0):
@@ -157,8 +162,9 @@ def build_operator(width: int, stencil_rows: int, pixel_scale: float, L0: float,
     Mlo = torch.empty((W, Kz), dtype=torch.float32, device=dev) if want_lo else None
     sigma = torch.empty((W, W), dtype=torch.float64, device=dev) if b_factor == "eigh" else None
     for jitter in (0.0, 1e-12, 1e-10, 1e-8):
-        rc = lib.pt_aw_build(W, m, sp, float(pixel_scale), float(L0), jitter, dptr(M), dptr(M64),
-                             dptr(Mlo), dptr(S), dptr(sigma), dptr(work), nbytes, stream_handle())
+        rc = lib.pt_aw_build(W, m, sp, float(pixel_scale), float(L0), jitter, int(increments),
+                             dptr(M), dptr(M64), dptr(Mlo), dptr(S), dptr(sigma), dptr(work),
+                             nbytes, stream_handle())
         if rc == _lib.PT_OK:
             break
         if rc != _lib.PT_ERR_NUMERIC or jitter == 1e-8:
@@ -174,7 +180,7 @@ def build_operator(width: int, stencil_rows: int, pixel_scale: float, L0: float,
         M[:, Kz:] = torch.from_numpy(root).to(device=dev, dtype=torch.float32)
         if M64 is not None:
             M64[:, Kz:] = torch.from_numpy(root).to(device=dev)
-    return ExtrusionOperator(W, m, sparse, M, M64, S, Mlo)
+    return ExtrusionOperator(W, m, sparse, M, M64, S, Mlo, increments)
 
 
 ANCHOR_MODES = 32
@@ -214,7 +220,8 @@ class AnchorTables:
             if op.M64 is None:
                 raise ValueError("the anchor needs the float64 operator (want_float64=True)")
             full = op.M64.cpu().numpy()                         # (W, K) = [A | B]
-            cols = np.concatenate([U @ full, -U], axis=1)       # (modes, K + W)
+            blocks = [U @ full, -U] + ([U] if op.increments else [])  # (+ r1 in increment form)
+            cols = np.concatenate(blocks, axis=1)               # (modes, K + W (+ W))
             tabs.append(cols[order].T)                          # (K + W, modes)
         t = np.ascontiguousarray(np.stack(tabs))
         hi = t.astype(np.float32)

@@ -79,10 +79,15 @@ __device__ __forceinline__ int ring_back(int head, int d, int cap) {
 // m - 1 here is that new row, summed in the order of k_extrude_reduce and
 // written both into the ring and into X (no thread reads that ring row; the
 // sparse points lie deeper than m rows).
+//
+// With `incr` (the increment form, never together with `prev`) stencil row
+// r < m - 1 becomes row_r - row_{r+1}, the newest row stays as it is and a
+// sparse value becomes s_p - r1[c_p]: the operand of an increment-form
+// operator, whose product is added to r1 by the reduce.
 __global__ void k_extrude_gather(int W, int m, int cap, float* __restrict__ buf,
                                  const JobParams jobs, int J, const SparseDev sp,
                                  const float* __restrict__ noise, float* __restrict__ X,
-                                 const float* __restrict__ prev, int prev_nz) {
+                                 const float* __restrict__ prev, int prev_nz, int incr) {
   const int j = blockIdx.z;
   if (j >= J) return;
   const GatherJob& jb = jobs.j[j];
@@ -91,9 +96,12 @@ __global__ void k_extrude_gather(int W, int m, int cap, float* __restrict__ buf,
   const int c = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
   if (r == m + 1) {  // sparse points
     const float* slab = buf + (size_t)jb.screen * cap * W;
+    const float* r1 = slab + (size_t)ring_back(jb.head, 1, cap) * W;
     float* dst = X + (size_t)j * K + (size_t)m * W;
-    for (int e = c; e < c + 2 && e < sp.n; ++e)
-      dst[e] = slab[(size_t)ring_back(jb.head, sp.depth[e], cap) * W + sp.col[e]];
+    for (int e = c; e < c + 2 && e < sp.n; ++e) {
+      const float v = slab[(size_t)ring_back(jb.head, sp.depth[e], cap) * W + sp.col[e]];
+      dst[e] = incr ? v - r1[sp.col[e]] : v;
+    }
     return;
   }
   if (c >= W) return;
@@ -103,7 +111,11 @@ __global__ void k_extrude_gather(int W, int m, int cap, float* __restrict__ buf,
     int phys = jb.head - m + r;
     if (phys < 0) phys += cap;
     float* src = buf + ((size_t)jb.screen * cap + phys) * W + c;
-    if (prev && r == m - 1) {
+    if (incr && r < m - 1) {
+      const float* nxt = buf + ((size_t)jb.screen * cap + (phys + 1 == cap ? 0 : phys + 1)) * W + c;
+      dst[0] = src[0] - nxt[0];
+      if (two) dst[1] = src[1] - nxt[1];
+    } else if (prev && r == m - 1) {
       float s0 = 0.f, s1 = 0.f;
       for (int z = 0; z < prev_nz; ++z) {
         const float* pz = prev + ((size_t)z * J + j) * W + c;
@@ -142,7 +154,7 @@ __global__ void k_extrude_gather(int W, int m, int cap, float* __restrict__ buf,
 __global__ void k_tc_gather(int W, int m, int cap, const float* __restrict__ buf,
                             const JobParams jobs, int J, const SparseDev sp, int NP, int nkc,
                             int terms, const float* __restrict__ noise,
-                            uint8_t* __restrict__ tiles) {
+                            uint8_t* __restrict__ tiles, int incr) {
   constexpr int Kc = tc::kTcKc;
   const int mW = m * W, Kn = mW + sp.n;  // the noise section starts at Kn
   const int K = Kn + W;
@@ -174,6 +186,7 @@ __global__ void k_tc_gather(int W, int m, int cap, const float* __restrict__ buf
         float val = 0.f;
         if (k < mW) {
           val = src[c];
+          if (incr && r < m - 1) val -= row_src(r + 1)[c];
           if (++c == W) {
             c = 0;
             ++r;
@@ -182,6 +195,7 @@ __global__ void k_tc_gather(int W, int m, int cap, const float* __restrict__ buf
         } else if (k < Kn) {
           const int e = k - mW;
           val = slab[(size_t)ring_back(jb.head, sp.depth[e], cap) * W + sp.col[e]];
+          if (incr) val -= slab[(size_t)ring_back(jb.head, 1, cap) * W + sp.col[e]];
         } else if (k < K) {
           const int cn = k - Kn;
           if (noise) {
@@ -324,16 +338,16 @@ __device__ __forceinline__ void two_sum_acc(float& s, float& c, float h) {
 // x' and P' in shared memory; part holds (s, c) double-float pairs.
 template <int R>
 __global__ void __launch_bounds__(256)
-k_anchor_gemm(int W, int K, int Kz, int cap, int g, int J, int kslice, const RingDst dst,
-              const float* __restrict__ X, const AnchorDev an, const float* __restrict__ buf,
-              float2* __restrict__ part) {
+k_anchor_gemm(int W, int K, int Kz, int cap, int g, int J, int kslice, int incr,
+              const RingDst dst, const float* __restrict__ X, const AnchorDev an,
+              const float* __restrict__ buf, float2* __restrict__ part) {
   // (64 modes: 32-column chunks keep the static shared memory under 48 KB)
   constexpr int KC = R == 64 ? 32 : 64, NP2 = R / 2, JT = 64, JPT = JT * NP2 / 256;
   __shared__ float xs[JT][KC + 1];
   __shared__ f2p phs[KC][NP2], pls[KC][NP2];
   const int tid = threadIdx.x;
   const int j0 = blockIdx.x * JT, z = blockIdx.y;
-  const int Kt = K + W;
+  const int Kt = K + (incr ? 2 : 1) * W;  // [operand | new row | r1 (increment form)]
   const int kb = z * kslice, ke = min(Kt, kb + kslice);
   const int p = tid % NP2, jt = (tid / NP2) * JPT;  // this thread: pair p, jobs jt .. jt + JPT - 1
   const f2p* th = an.th + (size_t)g * Kt * NP2;
@@ -345,9 +359,12 @@ k_anchor_gemm(int W, int K, int Kz, int cap, int g, int J, int kslice, const Rin
     for (int e = tid; e < JT * KC; e += 256) {
       const int jj = e / KC, kk = e % KC, k = k0 + kk, j = j0 + jj;
       float v = 0.f;
-      if (j < J && k < ke)
+      if (j < J && k < ke) {
+        const float* slab = buf + (size_t)dst.d[j].x * cap * W;
         v = k < K ? X[(size_t)j * K + k]
-                  : buf[((size_t)dst.d[j].x * cap + dst.d[j].y) * W + (k - K)];
+                  : (k < K + W ? slab[(size_t)dst.d[j].y * W + (k - K)]
+                               : slab[(size_t)ring_back(dst.d[j].y, 1, cap) * W + (k - K - W)]);
+      }
       xs[jj][kk] = v;
     }
     // the table rows k0 .. k0 + KC - 1 are contiguous: straight copies
@@ -573,14 +590,18 @@ k_extrude_gemm_tiled(int W, int K, int J, int kslice, const float* __restrict__ 
   }
 }
 
+// new row = sum of the split-K slices (+ the newest stencil row r1, ring
+// row head - 1, in the increment form: the slices then hold a correction)
 __global__ void k_extrude_reduce(int W, int J, int cap, int nsplit, const float* __restrict__ partial,
-                                 const RingDst dst, float* __restrict__ buf) {
+                                 const RingDst dst, float* __restrict__ buf, int incr) {
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y;
   if (r >= W || j >= J) return;
   float s = 0.f;
   for (int z = 0; z < nsplit; ++z) s += __ldcs(partial + ((size_t)z * J + j) * W + r);
-  buf[((size_t)dst.d[j].x * cap + dst.d[j].y) * W + r] = s;
+  float* slab = buf + (size_t)dst.d[j].x * cap * W;
+  if (incr) s += slab[(size_t)ring_back(dst.d[j].y, 1, cap) * W + r];
+  slab[(size_t)dst.d[j].y * W + r] = s;
 }
 
 // ---------------------------------------------------------------- readout
@@ -793,6 +814,7 @@ struct ExtrudeForm {
   const uint8_t* tiles;    // tensor-core operator tiles
   const uint8_t* lo;       // FP32 form: 1-term tiles of A - (float)A, or NULL
   const pt_extrude_anchor* anchor;  // FP32 form: low-order anchor, or NULL
+  int incr;                // the operator is in increment form
 };
 
 static int extrude_jobs(const char* who, const ExtrudeForm& form, int W, int m,
@@ -800,6 +822,8 @@ static int extrude_jobs(const char* who, const ExtrudeForm& form, int W, int m,
                         const pt_extrude_job* jobs, const float* noise, void* work,
                         size_t work_bytes, cudaStream_t s) {
   if (W < 1 || m < 1 || cap < m + 1 || G < 1) return fail(PT_ERR_ARG, std::string(who) + ": bad sizes");
+  if (form.incr && form.lo)
+    return fail(PT_ERR_ARG, std::string(who) + ": the increment form takes no correction tiles");
   SparseDev sp;
   if (int rc = sparse_dev(who, sparse, W, m, cap, sp)) return rc;
   if ((form.terms == 0 && !form.M) || (form.terms != 0 && !form.tiles) || !buf ||
@@ -857,7 +881,8 @@ static int extrude_jobs(const char* who, const ExtrudeForm& form, int W, int m,
     {
       ProfScope ps("k_extrude_reduce", s);
       k_extrude_reduce<<<dim3((W + 255) / 256, pend.J), 256, 0, s>>>(W, pend.J, cap, pend.nz,
-                                                                    partial, pend.dst, buf);
+                                                                    partial, pend.dst, buf,
+                                                                    form.incr);
     }
     count_launch_e(1);
     pend.on = false;
@@ -885,7 +910,7 @@ static int extrude_jobs(const char* who, const ExtrudeForm& form, int W, int m,
         // FP32 only: the tensor-core gather's threads each make 8 consecutive
         // values, so summing the slices there costs more than the reduce
         // (with the anchor every new row is anchored before it is read)
-        bool fuse = form.terms == 0 && !form.anchor && pend.on && pend.J == J;
+        bool fuse = form.terms == 0 && !form.anchor && !form.incr && pend.on && pend.J == J;
         for (int q = 0; fuse && q < J; ++q)
           fuse = pend.dst.d[q].x == dst.d[q].x && (pend.dst.d[q].y + 1) % cap == dst.d[q].y;
         if (!fuse)
@@ -898,7 +923,7 @@ static int extrude_jobs(const char* who, const ExtrudeForm& form, int W, int m,
           {
             ProfScope ps("k_extrude_gather", s);
             k_extrude_gather<<<dim3((W + 511) / 512, m + 1 + (sp.n > 0), J), 256, 0, s>>>(
-                W, m, cap, buf, jp, J, sp, noise, X, prev, prev_nz);
+                W, m, cap, buf, jp, J, sp, noise, X, prev, prev_nz, form.incr);
           }
           const float* Mg = form.M + (size_t)kv.first * W * K;
           launch_gemm_tiled(W, K, J, Mg, X, partial, &nz, s);
@@ -928,7 +953,7 @@ static int extrude_jobs(const char* who, const ExtrudeForm& form, int W, int m,
           {
             ProfScope ps("k_tc_gather", s);
             k_tc_gather<<<(unsigned)std::min<size_t>((items + 255) / 256, 152 * 8), 256, 0, s>>>(
-                W, m, cap, buf, jp, J, sp, NP, nkc, form.terms, noise, Bt);
+                W, m, cap, buf, jp, J, sp, NP, nkc, form.terms, noise, Bt, form.incr);
           }
           if (int rc = tc_gemm_launch(W, K, J, form.terms, form.tiles + (size_t)kv.first * op_group,
                                       Bt, partial, &nz, s))
@@ -942,7 +967,7 @@ static int extrude_jobs(const char* who, const ExtrudeForm& form, int W, int m,
           if (int rc = flush()) return rc;
           const AnchorDev an{(const f2p*)form.anchor->t_hi, (const f2p*)form.anchor->t_lo,
                              form.anchor->u};
-          const int R = form.anchor->modes, Kt = K + W;
+          const int R = form.anchor->modes, Kt = K + (form.incr ? 2 : 1) * W;
           const int jb = (J + 63) / 64;
           // about two CTAs per SM, chunks of 64 columns
           const int nsplit = std::max(1, std::min(std::min(kAnchorSplit, (Kt + 63) / 64),
@@ -955,11 +980,13 @@ static int extrude_jobs(const char* who, const ExtrudeForm& form, int W, int m,
             ProfScope ps("k_anchor", s);
             if (R == 32) {
               k_anchor_gemm<32><<<dim3(jb, nz_a), 256, 0, s>>>(W, K, Kz, cap, kv.first, J,
-                                                               kslice, dst, X, an, buf, apart);
+                                                               kslice, form.incr, dst, X, an, buf,
+                                                               apart);
               k_anchor_apply<32><<<J, 256, 0, s>>>(W, cap, J, nz_a, dst, apart, an.u, buf);
             } else {
               k_anchor_gemm<64><<<dim3(jb, nz_a), 256, 0, s>>>(W, K, Kz, cap, kv.first, J,
-                                                               kslice, dst, X, an, buf, apart);
+                                                               kslice, form.incr, dst, X, an, buf,
+                                                               apart);
               k_anchor_apply<64><<<J, 256, 0, s>>>(W, cap, J, nz_a, dst, apart, an.u, buf);
             }
           }
@@ -1086,8 +1113,8 @@ static int anchor_ok(const char* who, const pt_extrude_anchor* a) {
   return PT_OK;
 }
 
-extern "C" int pt_extrude_rows(int W, int m, const pt_sparse_stencil* sparse, int cap, int G,
-                               const float* M, const void* lo_tiles,
+extern "C" int pt_extrude_rows(int W, int m, const pt_sparse_stencil* sparse, int increments,
+                               int cap, int G, const float* M, const void* lo_tiles,
                                const pt_extrude_anchor* anchor, float* buf, int n_jobs,
                                const pt_extrude_job* jobs, const float* noise, void* work,
                                size_t work_bytes, void* stream) {
@@ -1095,8 +1122,9 @@ extern "C" int pt_extrude_rows(int W, int m, const pt_sparse_stencil* sparse, in
     return fail(PT_ERR_ARG, "pt_extrude_rows: correction tiles must be 256-byte aligned");
   if (int rc = anchor_ok("pt_extrude_rows", anchor)) return rc;
   return extrude_jobs("pt_extrude_rows",
-                      ExtrudeForm{0, M, nullptr, (const uint8_t*)lo_tiles, anchor}, W, m, sparse,
-                      cap, G, buf, n_jobs, jobs, noise, work, work_bytes, (cudaStream_t)stream);
+                      ExtrudeForm{0, M, nullptr, (const uint8_t*)lo_tiles, anchor, increments != 0},
+                      W, m, sparse, cap, G, buf, n_jobs, jobs, noise, work, work_bytes,
+                      (cudaStream_t)stream);
 }
 
 // Jobs of `counts[s]` row steps on every screen s, step-major (the order of
@@ -1133,8 +1161,8 @@ static int batch_jobs(const char* who, int W, int cap, int S, const int32_t* gro
   return PT_OK;
 }
 
-extern "C" int pt_extrude_batch(int W, int m, const pt_sparse_stencil* sparse, int cap,
-                                int n_groups, const float* M, const void* lo_tiles,
+extern "C" int pt_extrude_batch(int W, int m, const pt_sparse_stencil* sparse, int increments,
+                                int cap, int n_groups, const float* M, const void* lo_tiles,
                                 const pt_extrude_anchor* anchor, float* buf, int S,
                                 const int32_t* group, const float* bscale, const uint64_t* key,
                                 int64_t* top, const int32_t* counts, const float* noise,
@@ -1146,9 +1174,9 @@ extern "C" int pt_extrude_batch(int W, int m, const pt_sparse_stencil* sparse, i
   if (int rc = batch_jobs("pt_extrude_batch", W, cap, S, group, bscale, key, top, counts, jobs))
     return rc;
   return extrude_jobs("pt_extrude_batch",
-                      ExtrudeForm{0, M, nullptr, (const uint8_t*)lo_tiles, anchor}, W, m, sparse,
-                      cap, n_groups, buf, (int)jobs.size(), jobs.data(), noise, work, work_bytes,
-                      (cudaStream_t)stream);
+                      ExtrudeForm{0, M, nullptr, (const uint8_t*)lo_tiles, anchor, increments != 0},
+                      W, m, sparse, cap, n_groups, buf, (int)jobs.size(), jobs.data(), noise, work,
+                      work_bytes, (cudaStream_t)stream);
 }
 
 extern "C" size_t pt_extrude_lo_bytes(int W, int m, int n_sparse, int n_groups) {
@@ -1202,8 +1230,9 @@ extern "C" size_t pt_extrude_tc_workspace_bytes(int W, int m, int n_sparse, int 
   return al256(tc_btile_bytes(W, K, J, terms)) + al256(tc_partial_floats(W, K, J, terms) * sizeof(float));
 }
 
-extern "C" int pt_extrude_batch_tc(int W, int m, const pt_sparse_stencil* sparse, int cap,
-                                   int n_groups, const void* tiles, int terms, float* buf, int S,
+extern "C" int pt_extrude_batch_tc(int W, int m, const pt_sparse_stencil* sparse,
+                                   int increments, int cap, int n_groups, const void* tiles,
+                                   int terms, float* buf, int S,
                                    const int32_t* group, const float* bscale,
                                    const uint64_t* key, int64_t* top, const int32_t* counts,
                                    const float* noise, void* work, size_t work_bytes,
@@ -1217,7 +1246,9 @@ extern "C" int pt_extrude_batch_tc(int W, int m, const pt_sparse_stencil* sparse
   if (int rc = batch_jobs("pt_extrude_batch_tc", W, cap, S, group, bscale, key, top, counts, jobs))
     return rc;
   return extrude_jobs("pt_extrude_batch_tc",
-                      ExtrudeForm{terms, nullptr, (const uint8_t*)tiles, nullptr, nullptr}, W,
+                      ExtrudeForm{terms, nullptr, (const uint8_t*)tiles, nullptr, nullptr,
+                                  increments != 0},
+                      W,
                       m, sparse, cap, n_groups, buf, (int)jobs.size(), jobs.data(), noise, work,
                       work_bytes, (cudaStream_t)stream);
 }

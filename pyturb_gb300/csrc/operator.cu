@@ -260,6 +260,29 @@ __global__ void k_zero_upper(double* __restrict__ a, int n) {
   if (i < n && j < n && j > i) a[(size_t)i * n + j] = 0.0;
 }
 
+// The increment form of A (in place, rows [Kz, N) x columns [0, Kz) of the
+// joint matrix): with d_i = row_i - row_{i+1} (i < m - 1, rows oldest first)
+// and r1 the newest stencil row, A z = S r1 + sum_i (sum_{j <= i} A_j) d_i
+// + sum_p a_p (s_p - r1[c_p]) + sum_p a_p r1[c_p], S = sum_j A_j. The block
+// of r1 holds S - I plus each sparse weight at its column: the caller adds
+// r1 itself exactly, and the product only forms the small correction.
+__global__ void k_aw_increments(int W, int m, int Kz, int N, int ns,
+                                const int* __restrict__ sparse_col, double* __restrict__ J) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  const int r = blockIdx.y;
+  if (c >= W || r >= W) return;
+  double* a = J + (size_t)(Kz + r) * N;
+  double acc = 0.0;
+  for (int j = 0; j < m; ++j) {
+    acc += a[(size_t)j * W + c];
+    if (j < m - 1) a[(size_t)j * W + c] = acc;
+  }
+  double v = acc - (c == r ? 1.0 : 0.0);
+  for (int q = 0; q < ns; ++q)
+    if (sparse_col[q] == c) v += a[(size_t)m * W + q];
+  a[(size_t)(m - 1) * W + c] = v;
+}
+
 // M (W, Kz + W) float32 = [A | B] from the factored joint matrix (ld N):
 // A = rows [Kz, N), columns [0, Kz); B = rows [Kz, N), columns [Kz, N).
 // Mlo (W, Kz) float32 = A - float(A): what the float32 stencil operator
@@ -415,9 +438,9 @@ extern "C" size_t pt_aw_workspace_bytes(int W, int m, const pt_sparse_stencil* s
 }
 
 extern "C" int pt_aw_build(int W, int m, const pt_sparse_stencil* sparse, double pixel_scale,
-                           double L0, double jitter, float* M, double* M64, float* Mlo,
-                           float* seed, double* sigma, void* work, size_t work_bytes,
-                           void* stream) {
+                           double L0, double jitter, int increments, float* M, double* M64,
+                           float* Mlo, float* seed, double* sigma, void* work,
+                           size_t work_bytes, void* stream) {
   const char* who = "pt_aw_build";
   if (!(pixel_scale > 0.0) || !(L0 > 0.0) || !std::isfinite(L0))
     return fail(PT_ERR_ARG, std::string(who) + ": pixel_scale and a finite L0 must be positive");
@@ -484,6 +507,12 @@ extern "C" int pt_aw_build(int W, int m, const pt_sparse_stencil* sparse, double
   if (sigma)  // the conditional covariance Ls Ls^T (W x W, FP64)
     if (int rc = dgemm(true, W, W, W, 1.0, Yt + Kz, N, Yt + Kz, N, 0.0, sigma, W, false, s))
       return rc;
+  if (increments) {
+    // the sparse columns sit in the point list: x of sparse point q is px[m W + q]
+    k_aw_increments<<<dim3((W + 255) / 256, W), 256, 0, s>>>(W, m, Kz, N, Kz - m * W,
+                                                             dpx + (size_t)m * W, J);
+    count_launch_o();
+  }
   k_pack_operator<<<dim3((N + 255) / 256, W), 256, 0, s>>>(W, Kz, N, J, M, M64, Mlo);
   count_launch_o();
   if (seed) {

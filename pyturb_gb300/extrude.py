@@ -111,7 +111,8 @@ class RingExtruder:
     def __init__(self, W: int, m: int, cap: int, operators: List[Tuple[np.ndarray, np.ndarray]],
                  groups: Sequence[int], bscale: Sequence[float], streams: Sequence[NoiseStream],
                  device_operator=None, form: str = "fp32",
-                 sparse: Sequence[Tuple[int, int]] = (), operator_lo=None, anchor=None):
+                 sparse: Sequence[Tuple[int, int]] = (), operator_lo=None, anchor=None,
+                 increments: bool = False):
         torch = torch_module()
         if form not in self.FORMS:
             raise ValueError(f"form must be one of {sorted(self.FORMS)}, got {form!r}")
@@ -138,6 +139,9 @@ class RingExtruder:
             raise ValueError(f"operator shape {tuple(self.M.shape)} does not match W={self.W}, "
                              f"m={self.m} and {self.ns} sparse points")
         self.G = int(self.M.shape[0])
+        self.increments = bool(increments)
+        if self.increments and operator_lo is not None:
+            raise ValueError("the increment form takes no operator correction")
         self.anchor = anchor if self.terms == 0 else None
         self._anchor = C.byref(anchor.struct) if self.anchor is not None else None
         self.M_lo = None
@@ -202,12 +206,14 @@ class RingExtruder:
         self._ensure_work(int((counts > 0).sum()))
         ptr = lambda a: a.ctypes.data  # noqa: E731
         if self.terms:
-            _lib.call("pt_extrude_batch_tc", self.W, self.m, self._sp, self.cap, self.G,
+            _lib.call("pt_extrude_batch_tc", self.W, self.m, self._sp, int(self.increments),
+                      self.cap, self.G,
                       dptr(self.tiles), self.terms, dptr(self.buf), self.S, ptr(self._group),
                       ptr(self._bscale), ptr(self._key), ptr(self.top), ptr(counts), dptr(noise),
                       dptr(self.work), self.work_bytes, stream_handle())
         else:
-            _lib.call("pt_extrude_batch", self.W, self.m, self._sp, self.cap, self.G,
+            _lib.call("pt_extrude_batch", self.W, self.m, self._sp, int(self.increments),
+                      self.cap, self.G,
                       dptr(self.M), dptr(self.lo_tiles), self._anchor, dptr(self.buf), self.S,
                       ptr(self._group), ptr(self._bscale),
                       ptr(self._key), ptr(self.top), ptr(counts), dptr(noise), dptr(self.work),

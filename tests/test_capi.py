@@ -64,23 +64,23 @@ def test_argument_errors_before_device_work():
     assert _status("pt_readout", 0, 8, 8, 1, 1, None, None, 1.0, None, None) == _lib.PT_ERR_ARG
     assert _status("pt_lgs_zoom", 1, 8, 8, 7, None, None, None, 1.0, None, None) == _lib.PT_ERR_ARG
     assert _status("pt_rows_sample", 8, 8, 3, 0, 4, 0.0, None, None, None) == _lib.PT_ERR_ARG
-    assert _status("pt_extrude_rows", 0, 2, None, 8, 1, None, None, None, None, 0, None, None,
+    assert _status("pt_extrude_rows", 0, 2, None, 0, 8, 1, None, None, None, None, 0, None, None,
                    None, 0, None) == _lib.PT_ERR_ARG
     anchor = _lib.ExtrudeAnchor(modes=16)
-    assert _status("pt_extrude_rows", 16, 2, None, 8, 1, C.c_void_p(256), None, C.byref(anchor),
+    assert _status("pt_extrude_rows", 16, 2, None, 0, 8, 1, C.c_void_p(256), None, C.byref(anchor),
                    C.c_void_p(256), 0, None, None, None, 0, None) == _lib.PT_ERR_ARG
     assert "32 or 64 modes" in _lib.last_error()
     # sparse points must lie deeper than the full rows and inside the width
     bad = _lib.sparse_stencil([(2, 5)])
-    assert _status("pt_extrude_batch", 64, 2, C.byref(bad), 128, 1, C.c_void_p(256), None, None,
+    assert _status("pt_extrude_batch", 64, 2, C.byref(bad), 0, 128, 1, C.c_void_p(256), None, None,
                    C.c_void_p(256), 1, None, None, None, None, None, None, None, 0,
                    None) == _lib.PT_ERR_ARG
-    assert _status("pt_aw_build", 0, 2, None, 0.1, 25.0, 0.0, None, None, None, None, None, None,
+    assert _status("pt_aw_build", 0, 2, None, 0.1, 25.0, 0.0, 0, None, None, None, None, None, None,
                    0, None) == _lib.PT_ERR_ARG
-    assert _status("pt_aw_build", 16, 2, None, 0.1, float("inf"), 0.0, C.c_void_p(256), None,
+    assert _status("pt_aw_build", 16, 2, None, 0.1, float("inf"), 0.0, 0, C.c_void_p(256), None,
                    None, None, None, C.c_void_p(256), 1 << 20, None) == _lib.PT_ERR_ARG
     assert "finite L0" in _lib.last_error()
-    assert _status("pt_aw_build", 16, 2, C.byref(bad), 0.1, 25.0, 0.0, C.c_void_p(256), None,
+    assert _status("pt_aw_build", 16, 2, C.byref(bad), 0.1, 25.0, 0.0, 0, C.c_void_p(256), None,
                    None, None, None, C.c_void_p(256), 1 << 20, None) == _lib.PT_ERR_ARG
     assert _status("pt_extrude_lo_prepare", 16, 2, 0, 1, None, None, 0, None) == _lib.PT_ERR_ARG
     assert lib.pt_version() >= 100
