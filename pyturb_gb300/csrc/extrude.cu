@@ -822,8 +822,6 @@ static int extrude_jobs(const char* who, const ExtrudeForm& form, int W, int m,
                         const pt_extrude_job* jobs, const float* noise, void* work,
                         size_t work_bytes, cudaStream_t s) {
   if (W < 1 || m < 1 || cap < m + 1 || G < 1) return fail(PT_ERR_ARG, std::string(who) + ": bad sizes");
-  if (form.incr && form.lo)
-    return fail(PT_ERR_ARG, std::string(who) + ": the increment form takes no correction tiles");
   SparseDev sp;
   if (int rc = sparse_dev(who, sparse, W, m, cap, sp)) return rc;
   if ((form.terms == 0 && !form.M) || (form.terms != 0 && !form.tiles) || !buf ||

@@ -140,8 +140,6 @@ class RingExtruder:
                              f"m={self.m} and {self.ns} sparse points")
         self.G = int(self.M.shape[0])
         self.increments = bool(increments)
-        if self.increments and operator_lo is not None:
-            raise ValueError("the increment form takes no operator correction")
         self.anchor = anchor if self.terms == 0 else None
         self._anchor = C.byref(anchor.struct) if self.anchor is not None else None
         self.M_lo = None
