@@ -184,6 +184,53 @@ def bench_generate(torch, G):
     return reps * 64 / (e0.elapsed_time(e1) / 1000.0)
 
 
+def extrude_accuracy(torch, G, ext, r0s, steps: int = 512, screens: int = 3) -> dict:
+    """Relative L2 error of each extrusion form against a float64 recursion
+    with the same operator and injected noise: `screens` ring screens of the
+    atmosphere's geometry (layers 0, 4, 8), `steps` row steps, compared over
+    the last 128 rows. The float64 operator is the device build's own."""
+    from pyturb_gb300.backend import NoiseStream
+    from pyturb_gb300.covariance import AnchorTables, build_operator
+    from pyturb_gb300.extrude import RingExtruder
+
+    W, cap, sparse, dx = ext.width, ext.capacity, ext.sparse, ext.dx
+    layers = [0, 4, 8][:screens]
+    depth = max([2] + [d for d, _ in sparse])
+    bscale = [r0s[i] ** (-5.0 / 6.0) for i in layers]
+    seed = [ext._ring.buf[i, :depth].clone() for i in layers]  # ring rows 0 .. depth - 1
+    op = build_operator(W, 2, dx, L0, sparse, b_factor="eigh", want_float64=True)
+    a, b = op.host()  # the float64 recursion
+    R = [np.concatenate([x.double().cpu().numpy(), np.empty((steps, W))]) for x in seed]
+    st = [NoiseStream(700 + q, np.random.default_rng) for q in range(len(layers))]
+    for t in range(depth, depth + steps):
+        Z = np.stack([np.concatenate([r[t - 2:t].ravel(), [r[t - d, c] for d, c in sparse]])
+                      for r in R], axis=1)
+        beta = np.stack([st[q].draw((W,)) * bscale[q] for q in range(len(layers))], axis=1)
+        new = a @ Z + b @ beta
+        for q, r in enumerate(R):
+            r[t] = new[:, q]
+    opi = build_operator(W, 2, dx, L0, sparse, b_factor="eigh", increments=True)
+    out = {}
+    for name, form, anchor in (("fp32", "fp32", AnchorTables([op])),
+                               ("fp32_unanchored", "fp32", None), ("bf16x2", "bf16x2", None),
+                               ("bf16x3", "bf16x3", None)):
+        ring = RingExtruder(W, 2, cap, [], [0] * len(layers), bscale,
+                            [NoiseStream(700 + q, np.random.default_rng) for q in range(len(layers))],
+                            device_operator=op.M if form == "fp32" else opi.M, form=form,
+                            sparse=sparse, anchor=anchor, increments=form != "fp32")
+        for q in range(len(layers)):
+            ring.seed_rows(q, seed[q])
+        ring.extrude(np.full(len(layers), steps, dtype=np.int32))
+        torch.cuda.synchronize()
+        top = int(ring.top[0])
+        phys = [(top - k - 1) % cap for k in range(128)][::-1]
+        got = ring.buf[:, phys].double().cpu().numpy()
+        want = np.stack([r[-128:] for r in R])
+        out[name] = float(np.linalg.norm(got - want) / np.linalg.norm(want))
+        del ring
+    return out
+
+
 def bench_extrude(torch, G, steps: int = 4096):
     """Assemat-Wilson extrusion at n = 1024 with the configured stencil (2 full
     rows + 2 sparse columns), 9 layers x 16 realisations = 144 ring screens,
@@ -192,6 +239,7 @@ def bench_extrude(torch, G, steps: int = 4096):
     the fused 9-layer bilinear readout of one realisation at 1024^2."""
     from pyturb_gb300 import _lib
     from pyturb_gb300.backend import NoiseStream, stream_handle
+    from pyturb_gb300.covariance import build_operator
     from pyturb_gb300.extrude import RingExtruder
 
     tab = layer_table()
@@ -218,13 +266,20 @@ def bench_extrude(torch, G, steps: int = 4096):
         W, cap, sparse = ext.width, ext.capacity, ext.sparse
         K = 3 * W + len(sparse)
         flops = 2.0 * W * K * S
+        if columns == 2:
+            accuracy = extrude_accuracy(torch, G, ext, r0s)
         res = {"stencil": f"2 full rows + {columns} sparse columns ({len(sparse)} points)",
                "W": W, "K": K, "host_setup_s": setup_s, "forms": {}}
-        for form in ("fp32", "bf16x2", "bf16x3"):
+        # the tensor-core forms run the increment form of the same operator
+        inc = build_operator(W, 2, DIAM / n, L0, sparse, increments=True).M
+        variants = (("fp32", "fp32", ext._ring.anchor), ("fp32_unanchored", "fp32", None),
+                    ("bf16x2", "bf16x2", None), ("bf16x3", "bf16x3", None))
+        for name, form, anchor in variants:
             ring = RingExtruder(W, 2, cap, [], [0] * S, [r ** (-5.0 / 6.0) for r in r0s] * R,
                                 [NoiseStream(100 + s, None) for s in range(S)],
-                                device_operator=ext._ring.M, form=form, sparse=sparse,
-                                operator_lo=ext._ring.M_lo, anchor=ext._ring.anchor)
+                                device_operator=ext._ring.M if form == "fp32" else inc,
+                                form=form, sparse=sparse, anchor=anchor,
+                                increments=form != "fp32")
             for s in range(S):  # every realisation starts from layer (s % 9)'s seeded rows
                 ring.buf[s].copy_(ext._ring.buf[s % 9])
                 ring.top[s] = ext._ring.top[s % 9]
@@ -246,14 +301,14 @@ def bench_extrude(torch, G, steps: int = 4096):
             g = prof.get("k_tc_gemm" if form != "fp32" else "k_extrude_gemm", (1, float("nan")))
             gemm_s = g[1] / g[0] / 1e3
             products = {"fp32": 1, "bf16x2": 3, "bf16x3": 6}[form]
-            res["forms"][form] = {
+            res["forms"][name] = {
                 "row_steps_per_s": 1.0 / st, "effective_tflops": flops / st / 1e12,
                 "gemm_us": gemm_s * 1e6, "gemm_tflops_issued": products * flops / gemm_s / 1e12,
-                "kernel_share": {k: round(v[1] / max(1e-9, sum(x[1] for x in prof.values())), 4)
-                                 for k, v in prof.items()}}
+                "kernel_us_per_step": {k: round(v[1] / 256 * 1e3, 2) for k, v in prof.items()},
+                "rel_l2_vs_fp64_512_steps": accuracy[name] if columns == 2 else None}
             del ring
-        f32 = res["forms"]["fp32"]
-        f32["gemm_kernel_frac_of_fp32_nominal"] = f32["gemm_tflops_issued"] / 80.5
+        for f32 in (res["forms"]["fp32"], res["forms"]["fp32_unanchored"]):
+            f32["gemm_kernel_frac_of_fp32_nominal"] = f32["gemm_tflops_issued"] / 80.5
         if columns == 2:
             # readout: the 9 layers of one realisation, bilinear, at 1024^2
             o = torch.empty((n, n), dtype=torch.float32, device="cuda")
@@ -279,9 +334,11 @@ def bench_extrude(torch, G, steps: int = 4096):
                         f"W={cfg['W']}, stencil {cfg['stencil']}, {steps} row steps timed per "
                         "form; readout bilinear 9 layers",
             "row_steps_per_s": cfg["forms"]["fp32"]["row_steps_per_s"],
-            "note": "FP32 register-tiled split-K SIMT GEMM is the default form; FP32 nominal "
-                    "80.5 TFLOP/s = 152 SMs x 128 lanes x 2 x 2.07 GHz; operator built in FP64 "
-                    "on the GPU (host_setup_s includes seeding the 9 rings)",
+            "note": "fp32 = register-tiled split-K SIMT FP32 GEMM plus the 32-mode double-float "
+                    "low-order anchor (the default, parity form); fp32_unanchored = the same "
+                    "without it; bf16x2/x3 = split-bf16 tcgen05 products on the increment-form "
+                    "operator. FP32 nominal 80.5 TFLOP/s = 152 SMs x 128 lanes x 2 x 2.07 GHz; "
+                    "operator built in FP64 on the GPU (host_setup_s includes seeding the 9 rings)",
             **out}
 
 
@@ -475,10 +532,12 @@ def run_case(args) -> None:
         print(f"generate n={args.n} count={args.count}: {dt * 1e6:.1f} us per call")
         return
     W, m, S = args.width, 2, args.screens
-    op = build_operator(W, m, 8.0 / 1024, 25.0, want_lo=True, want_float64=True)
+    fp32 = args.form == "fp32"
+    op = build_operator(W, m, 8.0 / 1024, 25.0, want_float64=fp32, increments=not fp32)
     ring = RingExtruder(W, m, args.case_steps + m + 8, [], [0] * S, [1.0] * S,
                         [NoiseStream(100 + s, None) for s in range(S)], form=args.form,
-                        device_operator=op.M, operator_lo=op.Mlo, anchor=AnchorTables([op]))
+                        device_operator=op.M, anchor=AnchorTables([op]) if fp32 else None,
+                        increments=not fp32)
     for s in range(S):
         ring.seed_rows(s, torch.zeros((m, W), device=cuda_device()))
     ring.extrude(np.ones(S, dtype=np.int32))

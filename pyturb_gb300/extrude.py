@@ -104,7 +104,10 @@ class RingExtruder:
     operator instead of accumulating the float32 rounding of ``A``.
     ``anchor`` (``AnchorTables``) makes the FP32 form recompute the 32
     smoothest modes of every new row in double-float arithmetic: the row
-    recursion amplifies float32 rounding in those modes over long runs."""
+    recursion amplifies float32 rounding in those modes over long runs.
+    ``increments``: the operator is in increment form (``build_operator(...,
+    increments=True)``), the operand holds row differences and each new row
+    is the newest stencil row plus the product."""
 
     FORMS = {"fp32": 0, "bf16x2": 2, "bf16x3": 3}
 
@@ -321,11 +324,15 @@ class ExtrudedAtmosphere:
             key = round(float(L0), 9)
             if key not in op_index:
                 op_index[key] = len(ops)
+                # FP32 form: the operator as it is plus the low-order anchor
+                # (float64 twin needed for its tables); tensor-core forms: the
+                # increment form, whose small products keep the bf16 terms'
+                # rounding small
                 ops.append(build_operator(W, self.m, self.dx, float(L0), self.sparse,
                                           b_factor="eigh" if host_noise is not None
                                           else "cholesky", want_seed=self.boiling,
-                                          want_lo=extrude_form == "fp32",
-                                          want_float64=extrude_form == "fp32"))
+                                          want_float64=extrude_form == "fp32",
+                                          increments=extrude_form != "fp32"))
             groups.append(op_index[key])
         streams = [NoiseStream(s, host_noise) for s in config.seeds]
         self._streams = streams
@@ -336,12 +343,11 @@ class ExtrudedAtmosphere:
                                           history))
         bscale = [float(r0) ** (-5.0 / 6.0) for r0 in config.layer_r0]
         torch = torch_module()
-        lo = torch.stack([op.Mlo for op in ops]) if extrude_form == "fp32" else None
         anchor = AnchorTables(ops) if extrude_form == "fp32" else None
         self._ring = RingExtruder(W, self.m, self.capacity, [], groups, bscale, streams,
                                   device_operator=torch.stack([op.M for op in ops]),
-                                  form=extrude_form, sparse=self.sparse, operator_lo=lo,
-                                  anchor=anchor)
+                                  form=extrude_form, sparse=self.sparse, anchor=anchor,
+                                  increments=extrude_form != "fp32")
         for op in ops:  # the float64 twins were needed for the anchor only
             op.M64 = None
         # seed each ring with a von Karman screen from the layer's own stream:
@@ -367,8 +373,8 @@ class ExtrudedAtmosphere:
             self._scratch = RingExtruder(
                 W, self.m, self.capacity + self.m, [], [groups[i] for i in self._boil_layers],
                 [bscale[i] for i in self._boil_layers], self._queues,
-                device_operator=self._ring.M, form=extrude_form, operator_lo=self._ring.M_lo,
-                anchor=self._ring.anchor)
+                device_operator=self._ring.M, form=extrude_form, anchor=self._ring.anchor,
+                increments=self._ring.increments)
 
     @property
     def _buf(self):

@@ -51,14 +51,13 @@ class InfinitePhaseScreen:
         # the parity mode, the build's Cholesky factor otherwise)
         op = build_operator(self.n, self.stencil_rows, self.pixel_scale, self.L0,
                             b_factor="eigh" if host_noise is not None else "cholesky",
-                            want_lo=True, want_float64=True)
+                            want_float64=True)
         self._stream = NoiseStream(seed, host_noise)
         self._margin = self.stencil_rows + 6
         self._capacity = self.n + self._margin
         self._ring = RingExtruder(self.n, self.stencil_rows, self._capacity, [], [0],
                                   [self.r0 ** (-5.0 / 6.0)], [self._stream],
-                                  device_operator=op.M, operator_lo=op.Mlo,
-                                  anchor=AnchorTables([op]))
+                                  device_operator=op.M, anchor=AnchorTables([op]))
         op.M64 = None
         gen = PhaseScreen(n=self.n, pixel_scale=self.pixel_scale, r0=self.r0, L0=self.L0,
                           _stream=self._stream, host_noise=host_noise)

@@ -32,9 +32,11 @@ def _layers():
     return r0s, winds, alts
 
 
-@pytest.mark.parametrize("columns,correct", [(0, "anchor+lo"), (2, "anchor+lo"), (0, "lo"),
-                                             (0, "none")])
+@pytest.mark.parametrize("columns,correct", [(0, "anchor"), (2, "anchor"), (0, "none")])
 def test_batched_ring_extrusion_512_steps_vs_float64(columns, correct):
+    """FP32 form with the low-order anchor (the product configuration) for
+    both stencils; without it (reported, not asserted) the float32 rounding
+    drifts the recursion by ~1e-4 over 512 rows."""
     import torch
 
     import pyturb_gb300 as G
@@ -56,17 +58,16 @@ def test_batched_ring_extrusion_512_steps_vs_float64(columns, correct):
     bscale = [r ** (-5.0 / 6.0) for r in r0s] * 16
     from pyturb_gb300.covariance import AnchorTables
 
-    op = build_operator(W, m, DX, L0, sparse, b_factor="eigh", want_lo=True, want_float64=True)
+    op = build_operator(W, m, DX, L0, sparse, b_factor="eigh", want_float64=True)
     ring = RingExtruder(W, m, cap, [], [0] * S, bscale,
                         [NoiseStream(500 + s, np.random.default_rng) for s in range(S)],
                         device_operator=op.M, sparse=sparse,
-                        operator_lo=op.Mlo if "lo" in correct else None,
-                        anchor=AnchorTables([op]) if "anchor" in correct else None)
+                        anchor=AnchorTables([op]) if correct == "anchor" else None)
     # von Karman seed rows (device Philox), `depth` rows of history per screen
     seed_rows = []
     for s in range(S):
-        gen = G.PhaseScreen(n=1458, pixel_scale=DX, r0=r0s[s % 9], L0=L0, subharmonics=0,
-                            seed=900 + s)
+        gen = G.PhaseScreen(n=1458 if not sparse else 2592, pixel_scale=DX, r0=r0s[s % 9],
+                            L0=L0, subharmonics=0, seed=900 + s)
         rows = gen.generate()[:depth, :W].contiguous()
         ring.seed_rows(s, rows)
         seed_rows.append(rows)
@@ -98,7 +99,7 @@ def test_batched_ring_extrusion_512_steps_vs_float64(columns, correct):
     print(f"sparse points {len(sparse)}, correction {correct}: relative L2 per 128-step chunk "
           + ", ".join(f"{e:.2e}" for e in errs))
     assert t - depth == 512
-    if correct == "anchor+lo":  # the product configuration
+    if correct == "anchor":  # the product configuration
         assert max(errs) < TOL
 
 
