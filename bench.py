@@ -216,8 +216,8 @@ def extrude_accuracy(torch, G, ext, r0s, steps: int = 512, screens: int = 3) -> 
                                ("bf16x3", "bf16x3", None)):
         ring = RingExtruder(W, 2, cap, [], [0] * len(layers), bscale,
                             [NoiseStream(700 + q, np.random.default_rng) for q in range(len(layers))],
-                            device_operator=op.M if form == "fp32" else opi.M, form=form,
-                            sparse=sparse, anchor=anchor, increments=form != "fp32")
+                            device_operator=opi.M if form == "bf16x3" else op.M, form=form,
+                            sparse=sparse, anchor=anchor, increments=form == "bf16x3")
         for q in range(len(layers)):
             ring.seed_rows(q, seed[q])
         ring.extrude(np.full(len(layers), steps, dtype=np.int32))
@@ -270,16 +270,16 @@ def bench_extrude(torch, G, steps: int = 4096):
             accuracy = extrude_accuracy(torch, G, ext, r0s)
         res = {"stencil": f"2 full rows + {columns} sparse columns ({len(sparse)} points)",
                "W": W, "K": K, "host_setup_s": setup_s, "forms": {}}
-        # the tensor-core forms run the increment form of the same operator
+        # bf16x3 runs the increment form of the same operator
         inc = build_operator(W, 2, DIAM / n, L0, sparse, increments=True).M
         variants = (("fp32", "fp32", ext._ring.anchor), ("fp32_unanchored", "fp32", None),
                     ("bf16x2", "bf16x2", None), ("bf16x3", "bf16x3", None))
         for name, form, anchor in variants:
             ring = RingExtruder(W, 2, cap, [], [0] * S, [r ** (-5.0 / 6.0) for r in r0s] * R,
                                 [NoiseStream(100 + s, None) for s in range(S)],
-                                device_operator=ext._ring.M if form == "fp32" else inc,
+                                device_operator=inc if form == "bf16x3" else ext._ring.M,
                                 form=form, sparse=sparse, anchor=anchor,
-                                increments=form != "fp32")
+                                increments=form == "bf16x3")
             for s in range(S):  # every realisation starts from layer (s % 9)'s seeded rows
                 ring.buf[s].copy_(ext._ring.buf[s % 9])
                 ring.top[s] = ext._ring.top[s % 9]
@@ -336,8 +336,8 @@ def bench_extrude(torch, G, steps: int = 4096):
             "row_steps_per_s": cfg["forms"]["fp32"]["row_steps_per_s"],
             "note": "fp32 = register-tiled split-K SIMT FP32 GEMM plus the 32-mode double-float "
                     "low-order anchor (the default, parity form); fp32_unanchored = the same "
-                    "without it; bf16x2/x3 = split-bf16 tcgen05 products on the increment-form "
-                    "operator. FP32 nominal 80.5 TFLOP/s = 152 SMs x 128 lanes x 2 x 2.07 GHz; "
+                    "without it; bf16x2/x3 = split-bf16 tcgen05 products (bf16x3 on the "
+                    "increment-form operator). FP32 nominal 80.5 TFLOP/s = 152 SMs x 128 lanes x 2 x 2.07 GHz; "
                     "operator built in FP64 on the GPU (host_setup_s includes seeding the 9 rings)",
             **out}
 
@@ -532,12 +532,12 @@ def run_case(args) -> None:
         print(f"generate n={args.n} count={args.count}: {dt * 1e6:.1f} us per call")
         return
     W, m, S = args.width, 2, args.screens
-    fp32 = args.form == "fp32"
-    op = build_operator(W, m, 8.0 / 1024, 25.0, want_float64=fp32, increments=not fp32)
+    fp32, inc = args.form == "fp32", args.form == "bf16x3"
+    op = build_operator(W, m, 8.0 / 1024, 25.0, want_float64=fp32, increments=inc)
     ring = RingExtruder(W, m, args.case_steps + m + 8, [], [0] * S, [1.0] * S,
                         [NoiseStream(100 + s, None) for s in range(S)], form=args.form,
                         device_operator=op.M, anchor=AnchorTables([op]) if fp32 else None,
-                        increments=not fp32)
+                        increments=inc)
     for s in range(S):
         ring.seed_rows(s, torch.zeros((m, W), device=cuda_device()))
     ring.extrude(np.ones(S, dtype=np.int32))

@@ -267,10 +267,12 @@ size_t pt_extrude_workspace_bytes(int W, int m, int n_sparse, int max_jobs_per_s
 /* Low-order anchor of the float32 form (no reference counterpart). The row
  * recursion amplifies errors in the smooth modes of a row, so float32
  * rounding in the product walks them away from the float64 result over
- * hundreds of rows. With an anchor, each new row's first `modes` (32 or 64)
- * DCT-II modes U (orthonormal, U[i][w] = sqrt((2 - [i=0]) / W)
- * cos(pi i (w + 1/2) / W)) are recomputed in double-float arithmetic and
- * set: row += U (U^T A z + U^T B (bscale beta) - U^T row). Tables (device):
+ * hundreds of rows. With an anchor, each new row's projection on an
+ * orthonormal basis U of `modes` (32 or 64) row vectors is recomputed in
+ * double-float arithmetic and set: row += U (U^T A z + U^T B (bscale beta)
+ * - U^T row). The package's U is the smoothest DCT-II modes
+ * (U[i][w] = sqrt((2 - [i=0]) / W) cos(pi i (w + 1/2) / W)), with a sparse
+ * stencil the unit vectors of its columns in place of the last ones. Tables (device):
  * t_hi / t_lo (G, Kt, modes) f32, Kt = K + W (K + 2 W in the increment
  * form), hi + lo = the float64 value: row k holds column k of
  * [U^T A | U^T B_unit | -U (| U for r1)], its modes stored in
