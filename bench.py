@@ -198,7 +198,8 @@ def extrude_accuracy(torch, G, ext, r0s, steps: int = 512, screens: int = 3) -> 
     depth = max([2] + [d for d, _ in sparse])
     bscale = [r0s[i] ** (-5.0 / 6.0) for i in layers]
     seed = [ext._ring.buf[i, :depth].clone() for i in layers]  # ring rows 0 .. depth - 1
-    op = build_operator(W, 2, dx, L0, sparse, b_factor="eigh", want_float64=True)
+    op = build_operator(W, 2, dx, L0, sparse, b_factor="eigh", want_float64=True,
+                        want_lo=bool(sparse))
     a, b = op.host()  # the float64 recursion
     R = [np.concatenate([x.double().cpu().numpy(), np.empty((steps, W))]) for x in seed]
     st = [NoiseStream(700 + q, np.random.default_rng) for q in range(len(layers))]
@@ -211,13 +212,15 @@ def extrude_accuracy(torch, G, ext, r0s, steps: int = 512, screens: int = 3) -> 
             r[t] = new[:, q]
     opi = build_operator(W, 2, dx, L0, sparse, b_factor="eigh", increments=True)
     out = {}
-    for name, form, anchor in (("fp32", "fp32", AnchorTables([op])),
+    sp_modes = 64 if sparse else 32
+    for name, form, anchor in (("fp32", "fp32", AnchorTables([op], sp_modes)),
                                ("fp32_unanchored", "fp32", None), ("bf16x2", "bf16x2", None),
                                ("bf16x3", "bf16x3", None)):
         ring = RingExtruder(W, 2, cap, [], [0] * len(layers), bscale,
                             [NoiseStream(700 + q, np.random.default_rng) for q in range(len(layers))],
                             device_operator=opi.M if form == "bf16x3" else op.M, form=form,
-                            sparse=sparse, anchor=anchor, increments=form == "bf16x3")
+                            sparse=sparse, anchor=anchor, increments=form == "bf16x3",
+                            operator_lo=op.Mlo if anchor is not None and sparse else None)
         for q in range(len(layers)):
             ring.seed_rows(q, seed[q])
         ring.extrude(np.full(len(layers), steps, dtype=np.int32))
@@ -279,6 +282,7 @@ def bench_extrude(torch, G, steps: int = 4096):
                                 [NoiseStream(100 + s, None) for s in range(S)],
                                 device_operator=inc if form == "bf16x3" else ext._ring.M,
                                 form=form, sparse=sparse, anchor=anchor,
+                                operator_lo=ext._ring.M_lo if anchor is not None else None,
                                 increments=form == "bf16x3")
             for s in range(S):  # every realisation starts from layer (s % 9)'s seeded rows
                 ring.buf[s].copy_(ext._ring.buf[s % 9])

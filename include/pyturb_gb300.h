@@ -271,8 +271,7 @@ size_t pt_extrude_workspace_bytes(int W, int m, int n_sparse, int max_jobs_per_s
  * orthonormal basis U of `modes` (32 or 64) row vectors is recomputed in
  * double-float arithmetic and set: row += U (U^T A z + U^T B (bscale beta)
  * - U^T row). The package's U is the smoothest DCT-II modes
- * (U[i][w] = sqrt((2 - [i=0]) / W) cos(pi i (w + 1/2) / W)), with a sparse
- * stencil the unit vectors of its columns in place of the last ones. Tables (device):
+ * (U[i][w] = sqrt((2 - [i=0]) / W) cos(pi i (w + 1/2) / W)). Tables (device):
  * t_hi / t_lo (G, Kt, modes) f32, Kt = K + W (K + 2 W in the increment
  * form), hi + lo = the float64 value: row k holds column k of
  * [U^T A | U^T B_unit | -U (| U for r1)], its modes stored in

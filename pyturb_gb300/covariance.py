@@ -205,8 +205,7 @@ class AnchorTables:
     """Device tables of the float32 form's low-order anchor for a stack of
     operators (one per outer-scale group): the columns of
     ``[U^T A | U^T B | -U]`` as (hi, lo) float32 pairs, modes in pair order,
-    and ``U`` in float32, U the first 32 (or 64) DCT-II modes (with a sparse
-    stencil, the unit vectors of its columns in place of the last ones)."""
+    and ``U`` in float32, U the first 32 (or 64) DCT-II modes."""
 
     def __init__(self, ops: Sequence["ExtrusionOperator"], modes: int = ANCHOR_MODES):
         if modes not in (32, 64):
@@ -214,16 +213,7 @@ class AnchorTables:
         torch = torch_module()
         dev = cuda_device()
         W = ops[0].W
-        # a sparse stencil reads single pixels of old rows at its columns, so
-        # those pixels are anchored too: the basis is the smoothest DCT modes
-        # plus the unit vectors of the sparse columns, orthonormalised
-        cols = sorted({c for _, c in ops[0].sparse})
-        U = dct_modes(W, modes - len(cols))
-        if cols:
-            E = np.zeros((len(cols), W))
-            E[np.arange(len(cols)), cols] = 1.0
-            q, r = np.linalg.qr(np.concatenate([U, E]).T)
-            U = q.T * np.sign(np.diag(r))[:, None]
+        U = dct_modes(W, modes)
         order = pair_order(modes)
         tabs = []
         for op in ops:

@@ -332,6 +332,7 @@ class ExtrudedAtmosphere:
                                           b_factor="eigh" if host_noise is not None
                                           else "cholesky", want_seed=self.boiling,
                                           want_float64=extrude_form == "fp32",
+                                          want_lo=extrude_form == "fp32" and bool(self.sparse),
                                           increments=extrude_form == "bf16x3"))
             groups.append(op_index[key])
         streams = [NoiseStream(s, host_noise) for s in config.seeds]
@@ -343,11 +344,18 @@ class ExtrudedAtmosphere:
                                           history))
         bscale = [float(r0) ** (-5.0 / 6.0) for r0 in config.layer_r0]
         torch = torch_module()
-        anchor = AnchorTables(ops) if extrude_form == "fp32" else None
+        # a sparse stencil feeds single pixels of old rows back into new ones
+        # (a longer memory for rounding errors): 64 anchored modes and the
+        # operator correction there, 32 modes for the rows-only stencil
+        anchor, lo = None, None
+        if extrude_form == "fp32":
+            anchor = AnchorTables(ops, 64 if self.sparse else 32)
+            if self.sparse:
+                lo = torch.stack([op.Mlo for op in ops])
         self._ring = RingExtruder(W, self.m, self.capacity, [], groups, bscale, streams,
                                   device_operator=torch.stack([op.M for op in ops]),
                                   form=extrude_form, sparse=self.sparse, anchor=anchor,
-                                  increments=extrude_form == "bf16x3")
+                                  operator_lo=lo, increments=extrude_form == "bf16x3")
         for op in ops:  # the float64 twins were needed for the anchor only
             op.M64 = None
         # seed each ring with a von Karman screen from the layer's own stream:

@@ -58,11 +58,16 @@ def test_batched_ring_extrusion_512_steps_vs_float64(columns, correct):
     bscale = [r ** (-5.0 / 6.0) for r in r0s] * 16
     from pyturb_gb300.covariance import AnchorTables
 
-    op = build_operator(W, m, DX, L0, sparse, b_factor="eigh", want_float64=True)
+    # the product configuration: 32 anchored modes (rows only), 64 plus the
+    # operator correction (sparse stencil)
+    op = build_operator(W, m, DX, L0, sparse, b_factor="eigh", want_float64=True,
+                        want_lo=bool(sparse))
     ring = RingExtruder(W, m, cap, [], [0] * S, bscale,
                         [NoiseStream(500 + s, np.random.default_rng) for s in range(S)],
                         device_operator=op.M, sparse=sparse,
-                        anchor=AnchorTables([op]) if correct == "anchor" else None)
+                        anchor=(AnchorTables([op], 64 if sparse else 32)
+                                if correct == "anchor" else None),
+                        operator_lo=op.Mlo if sparse and correct == "anchor" else None)
     # von Karman seed rows (device Philox), `depth` rows of history per screen
     seed_rows = []
     for s in range(S):
