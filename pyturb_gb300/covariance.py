@@ -32,7 +32,7 @@ from . import _lib
 from .backend import cuda_device, dptr, stream_handle, torch_module
 
 __all__ = ["phase_covariance", "build_operator", "build_extrusion", "seed_factor",
-           "sparse_points", "ExtrusionOperator", "AnchorTables", "dct_modes"]
+           "sparse_points", "ExtrusionOperator", "AnchorTables", "dct_modes", "anchor_modes"]
 
 _NU = 5.0 / 6.0
 
@@ -210,9 +210,11 @@ class AnchorTables:
     def __init__(self, ops: Sequence["ExtrusionOperator"], modes: int = ANCHOR_MODES):
         if modes not in (32, 64):
             raise ValueError("the anchor takes 32 or 64 modes")
+        W = ops[0].W
+        if modes > W // 2:
+            raise ValueError(f"{modes} anchored modes need rows of at least {2 * modes} pixels")
         torch = torch_module()
         dev = cuda_device()
-        W = ops[0].W
         U = dct_modes(W, modes)
         order = pair_order(modes)
         tabs = []
@@ -232,6 +234,15 @@ class AnchorTables:
         self.modes = modes
         self.struct = _lib.ExtrudeAnchor(modes=modes, pad=0, t_hi=dptr(self.t_hi),
                                          t_lo=dptr(self.t_lo), u=dptr(self.u))
+
+
+def anchor_modes(width: int, sparse) -> int:
+    """Anchored modes for a row of ``width`` pixels: 64 with a sparse stencil
+    (its deep points give rounding errors a longer memory), 32 for full rows
+    only, none below 64 pixels (short rows accumulate little)."""
+    if width < 64:
+        return 0
+    return 64 if sparse and width >= 256 else 32
 
 
 def build_extrusion(width: int, stencil_rows: int, pixel_scale: float, L0: float,

@@ -30,8 +30,8 @@ import numpy as np
 from . import _lib
 from .backend import NoiseStream, cuda_device, dptr, stream_handle, torch_module, upload
 from .config import ExtrusionConfig
-from .covariance import (AnchorTables, build_extrusion, build_operator, phase_covariance,
-                         sparse_points)
+from .covariance import (AnchorTables, anchor_modes, build_extrusion, build_operator,
+                         phase_covariance, sparse_points)
 from .fourier import PhaseScreen
 
 __all__ = ["ExtrudedAtmosphere", "build_extrusion", "phase_covariance", "RingExtruder"]
@@ -348,10 +348,11 @@ class ExtrudedAtmosphere:
         # (a longer memory for rounding errors): 64 anchored modes and the
         # operator correction there, 32 modes for the rows-only stencil
         anchor, lo = None, None
-        if extrude_form == "fp32":
-            anchor = AnchorTables(ops, 64 if self.sparse else 32)
-            if self.sparse:
-                lo = torch.stack([op.Mlo for op in ops])
+        modes = anchor_modes(W, self.sparse)
+        if extrude_form == "fp32" and modes:
+            anchor = AnchorTables(ops, modes)
+        if extrude_form == "fp32" and self.sparse:
+            lo = torch.stack([op.Mlo for op in ops])
         self._ring = RingExtruder(W, self.m, self.capacity, [], groups, bscale, streams,
                                   device_operator=torch.stack([op.M for op in ops]),
                                   form=extrude_form, sparse=self.sparse, anchor=anchor,

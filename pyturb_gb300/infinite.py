@@ -16,7 +16,7 @@ import numpy as np
 from . import _lib
 from .backend import NoiseStream, dptr, stream_handle, torch_module
 from .config import ScreenConfig
-from .covariance import AnchorTables, build_operator, phase_covariance
+from .covariance import AnchorTables, anchor_modes, build_operator, phase_covariance
 from .extrude import RingExtruder, compact_bounds
 from .fourier import PhaseScreen
 
@@ -57,7 +57,9 @@ class InfinitePhaseScreen:
         self._capacity = self.n + self._margin
         self._ring = RingExtruder(self.n, self.stencil_rows, self._capacity, [], [0],
                                   [self.r0 ** (-5.0 / 6.0)], [self._stream],
-                                  device_operator=op.M, anchor=AnchorTables([op]))
+                                  device_operator=op.M,
+                                  anchor=(AnchorTables([op], anchor_modes(self.n, ()))
+                                          if anchor_modes(self.n, ()) else None))
         op.M64 = None
         gen = PhaseScreen(n=self.n, pixel_scale=self.pixel_scale, r0=self.r0, L0=self.L0,
                           _stream=self._stream, host_noise=host_noise)
