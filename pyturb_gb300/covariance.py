@@ -211,8 +211,8 @@ class AnchorTables:
         if modes not in (32, 64):
             raise ValueError("the anchor takes 32 or 64 modes")
         W = ops[0].W
-        if modes > W // 2:
-            raise ValueError(f"{modes} anchored modes need rows of at least {2 * modes} pixels")
+        if modes > W:
+            raise ValueError(f"{modes} anchored modes need rows of at least {modes} pixels")
         torch = torch_module()
         dev = cuda_device()
         U = dct_modes(W, modes)
@@ -239,8 +239,8 @@ class AnchorTables:
 def anchor_modes(width: int, sparse) -> int:
     """Anchored modes for a row of ``width`` pixels: 64 with a sparse stencil
     (its deep points give rounding errors a longer memory), 32 for full rows
-    only, none below 64 pixels (short rows accumulate little)."""
-    if width < 64:
+    only, none below 32 pixels."""
+    if width < 32:
         return 0
     return 64 if sparse and width >= 256 else 32
 
