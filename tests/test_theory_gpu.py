@@ -1,0 +1,188 @@
+"""Theory gates at 1% on production noise (in-kernel Philox), through the
+device diagnostics.
+
+"Theory" here is the exact expectation of the discrete spectral model the
+screens are drawn from: the FFT grid plus the 3x3-per-level subharmonics of
+``src/pyturb/fourier.py:174-282`` with the reference's own amplitude tables
+(the float64 oracle's ``build_filters``). A screen is a sum of independent
+components ``Re(c e^{2 pi i f.x})`` with ``c`` complex normal times an
+amplitude ``a``, so every second-order statistic has a closed form:
+
+- structure function: ``D(s) = 2 sum a^2 (1 - cos(2 pi f s dx))``, averaged over
+  both axes (the estimator of ``src/pyturb/utils.py:159-201``);
+- Zernike variances: ``var c_j = sum a^2 |sum_x P_j(x) e^{2 pi i f.x}|^2``, with
+  ``P`` the least-squares projector of ``src/pyturb/analysis.py:129-162``;
+- frozen-flow temporal PSD of one pixel: ``E psd(f) = (2 dt / T) sum a^2
+  |h|^2 (|G(f)|^2 + |G(-f)|^2) / 2`` with ``G`` the DFT of the mean-removed
+  phasor series of the component (the estimator of
+  ``src/pyturb/analysis.py:183-208``; ``h`` is 1 for grid components and
+  ``e^{i theta(x0)} - grid mean`` for subharmonics).
+
+Against these, sampling error is the only error, and the ensembles are sized
+so that 1% is at least three standard deviations. The continuous
+Kolmogorov / von Karman laws are not 1% references for a finite FFT screen
+(the reference itself gates them at 8-15%, ``validation/validate.py:43-138``);
+their deviation is printed, not gated.
+"""
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _tables(n, dx, r0, L0, P):
+    from oracle.spectral import build_filters
+
+    amp, f, levels = build_filters(n, dx, r0, L0, P)
+    return amp, f, levels
+
+
+def _expected_sf(n, dx, r0, L0, P, ms):
+    amp, f, levels = _tables(n, dx, r0, L0, P)
+    s = np.arange(1, ms + 1)[:, None] * dx
+    a2 = amp ** 2
+    # axis 0 carries f[i] (rows of the table), axis 1 f[j]
+    d0 = 2.0 * (a2.sum(1)[None, :] * (1 - np.cos(2 * np.pi * f[None, :] * s))).sum(1)
+    d1 = 2.0 * (a2.sum(0)[None, :] * (1 - np.cos(2 * np.pi * f[None, :] * s))).sum(1)
+    for a, _b, fp in levels:
+        q = a ** 2
+        d0 += 2.0 * (q.sum(1)[None, :] * (1 - np.cos(2 * np.pi * fp[None, :] * s))).sum(1)
+        d1 += 2.0 * (q.sum(0)[None, :] * (1 - np.cos(2 * np.pi * fp[None, :] * s))).sum(1)
+    return 0.5 * (d0 + d1)
+
+
+def test_structure_function_within_1_percent_of_the_model():
+    """16384 Philox screens of 256^2 (D = 8 m, r0 = 0.15 m, L0 = 25 m, 3
+    levels): the device structure function over s = 1..64 px against the
+    model's exact expectation, every separation within 1%."""
+    import torch
+
+    import pyturb_gb300 as G
+    from pyturb_gb300.analysis import structure_function
+
+    n, dx, r0, L0, P, ms = 256, 8.0 / 256, 0.15, 25.0, 3, 64
+    g = G.PhaseScreen(n=n, pixel_scale=dx, r0=r0, L0=L0, subharmonics=P, seed=2024)
+    acc = np.zeros(ms)
+    batches = 8
+    for _ in range(batches):
+        _r, d = structure_function(g.generate(2048), dx, ms)
+        acc += d
+    torch.cuda.synchronize()
+    meas = acc / batches
+    want = _expected_sf(n, dx, r0, L0, P, ms)
+    ratio = meas / want
+    kolmo = 6.88 * (np.arange(1, ms + 1) * dx / r0) ** (5.0 / 3.0)
+    print(f"SF / model: max |dev| {np.abs(ratio - 1).max() * 100:.2f}%, mean "
+          f"{(ratio.mean() - 1) * 100:+.3f}%; model / Kolmogorov at s = 4..64 px "
+          f"{(want[3:] / kolmo[3:]).min():.3f} .. {(want[3:] / kolmo[3:]).max():.3f}")
+    assert np.all(np.abs(ratio - 1) < 0.01)
+
+
+def test_noll_variances_within_1_percent_of_the_model():
+    """262144 Philox screens of 64^2 (D = 4 m, r0 = 0.2 m, L0 = 25 m, 3 levels):
+    the variance of each Noll coefficient j = 2..21 from the device projection
+    within 1% of the model (sampling std sqrt(2/M) = 0.28%)."""
+    import torch
+
+    import pyturb_gb300 as G
+    from pyturb_gb300.analysis import zernike_basis, zernike_decompose
+
+    n, D, r0, L0, P, modes = 64, 4.0, 0.2, 25.0, 3, 21
+    dx = D / n
+    g = G.PhaseScreen(n=n, pixel_scale=dx, r0=r0, L0=L0, subharmonics=P, seed=77)
+    sums = np.zeros(modes)
+    M = 0
+    for _ in range(16):
+        c = zernike_decompose(g.generate(16384), modes)
+        sums += (c ** 2).sum(0)
+        M += c.shape[0]
+    torch.cuda.synchronize()
+    meas = sums / M  # zero-mean coefficients (j >= 2 annihilate the piston)
+    # the model: the same least-squares projector, in float64
+    basis = zernike_basis(modes, n)
+    mask = basis[0] != 0
+    Pj = np.zeros((modes, n * n))
+    Pj[:, mask.ravel()] = np.linalg.pinv(basis[:, mask].T)
+    Pj = Pj.reshape(modes, n, n)
+    amp, f, levels = _tables(n, dx, r0, L0, P)
+    want = (amp[None] ** 2 * np.abs(np.fft.fft2(Pj)) ** 2).sum((1, 2))
+    coords = (np.arange(n) - n / 2.0) * dx
+    for a, _b, fp in levels:
+        e = np.exp(2j * np.pi * fp[:, None] * coords[None, :])  # (3, n)
+        proj = np.einsum("jyx,ay,bx->jab", Pj, e, e)
+        want += (a[None] ** 2 * np.abs(proj) ** 2).sum((1, 2))
+    ratio = meas[1:] / want[1:]
+    print("Noll j = 2..21, measured / model: " + " ".join(f"{x:.4f}" for x in ratio))
+    assert np.all(np.abs(ratio - 1) < 0.01)
+
+
+def test_temporal_psd_slope_and_amplitude_within_1_percent_of_the_model():
+    """Frozen flow past one pixel: 512 single-layer atmospheres (96^2,
+    D = 8 m, r0 = 0.15 m, L0 = 25 m, 3 levels, 10 m/s at 45 degrees, 700
+    frames at 1 ms: no wrap), 36 pixels on a 16-px lattice each; the device
+    temporal PSD over 5-40 Hz against the model: mean amplitude ratio and
+    fitted slope within 1%."""
+    import warnings
+
+    import torch
+
+    import pyturb_gb300 as G
+    from pyturb_gb300.analysis import temporal_psd
+
+    warnings.simplefilter("ignore")
+    n, D, r0, L0, P, v, dt, T = 96, 8.0, 0.15, 25.0, 3, 10.0, 1e-3, 700
+    dx = D / n
+    px = np.arange(8, n, 16)                       # 6 x 6 lattice, symmetric in the axes
+    yy, xx = np.meshgrid(px, px, indexing="ij")
+    yy, xx = yy.ravel(), xx.ravel()
+    iy, ix = torch.as_tensor(yy, device="cuda"), torch.as_tensor(xx, device="cuda")
+    times = np.arange(T) * dt
+    psd_sum, count = None, 0
+    for seed in range(512):
+        atm = G.Atmosphere([G.Layer(0.0, 1.0, v, 45.0, L0)], r0=r0, diameter=D, n=n,
+                           subharmonics=P, seed=seed)
+        frames = atm.render(times, wavelength=500e-9)          # phase [rad], (T, n, n)
+        series = frames[:, iy, ix].T.contiguous()               # (36, T)
+        freq, p = temporal_psd(series, dt)
+        psd_sum = p * len(yy) if psd_sum is None else psd_sum + p * len(yy)
+        count += len(yy)
+    torch.cuda.synchronize()
+    meas = psd_sum / count
+    # the model (wind along the diagonal: the same for either axis convention)
+    amp, f, levels = _tables(n, dx, r0, L0, P)
+    w = v / np.sqrt(2.0)
+    t = np.arange(T)
+    m = np.arange(1, T // 2 + 1)
+
+    def spectrum(freqs2d, a2, h2):
+        # sum over components of a^2 |h|^2 (|G(f)|^2 + |G(-f)|^2) / 2
+        om = 2 * np.pi * freqs2d.ravel() * w * dt
+        g = np.exp(1j * om[:, None] * t[None, :])
+        g -= g.mean(1, keepdims=True)
+        Gf = np.fft.fft(g, axis=1)
+        pw = 0.5 * (np.abs(Gf[:, m]) ** 2 + np.abs(Gf[:, (T - m) % T]) ** 2)
+        return (a2.ravel()[:, None] * h2.ravel()[:, None] * pw).sum(0)
+
+    fsum = f[:, None] + f[None, :]
+    want = spectrum(fsum, amp ** 2, np.ones_like(amp))
+    coords = (np.arange(n) - n / 2.0) * dx
+    for a, _b, fp in levels:
+        mean = np.exp(2j * np.pi * fp[:, None] * coords[None, :]).mean(1)   # (3,)
+        h2 = np.zeros((3, 3))
+        for y0, x0 in zip(yy, xx):
+            e0 = np.exp(2j * np.pi * fp * coords[y0])[:, None] * np.exp(
+                2j * np.pi * fp * coords[x0])[None, :]
+            h2 += np.abs(e0 - mean[:, None] * mean[None, :]) ** 2
+        want += spectrum(fp[:, None] + fp[None, :], a ** 2, h2 / len(yy))
+    want *= 2 * dt / T
+    band = (freq >= 5) & (freq <= 40)
+    amp_ratio = float(np.mean(meas[band] / want[band]))
+    s_meas = np.polyfit(np.log(freq[band]), np.log(meas[band]), 1)[0]
+    s_want = np.polyfit(np.log(freq[band]), np.log(want[band]), 1)[0]
+    kolmo = 0.0774 * r0 ** (-5.0 / 3.0) * v ** (5.0 / 3.0) * freq[band] ** (-8.0 / 3.0)
+    print(f"temporal PSD 5-40 Hz: amplitude / model {amp_ratio:.4f}, slope {s_meas:.4f} "
+          f"(model {s_want:.4f}); model / frozen-flow Kolmogorov median "
+          f"{np.median(want[band] / kolmo):.2f}")
+    assert abs(amp_ratio - 1) < 0.01
+    assert abs(s_meas / s_want - 1) < 0.01
