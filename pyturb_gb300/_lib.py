@@ -116,6 +116,7 @@ SIGNATURES = {
     "pt_grid_set_cols_variant": (i32, [vp, i32]),
     "pt_ifft2": (i32, [vp, vp, vp, i32, vp, sz, vp]),
     "pt_ifft2_noalloc": (i32, [i32, vp, vp, i32, vp]),
+    "pt_ifft2_tc": (i32, [i32, vp, vp, i32, vp]),
     "pt_generate": (i32, [vp, i32, vp, vp, vp, vp, u64, u64, i32, i32, f32, i32, vp, vp, sz, vp]),
     "pt_generate_scaled": (i32, [vp, i32, vp, vp, u64, u64, i32, i32, f32, vp, vp, vp, sz, vp]),
     "pt_layers_fill": (i32, [vp, i32, vp, vp, vp, vp, C.POINTER(C.c_uint64), vp, vp, vp]),
