@@ -184,6 +184,76 @@ def bench_generate(torch, G):
     return reps * 64 / (e0.elapsed_time(e1) / 1000.0)
 
 
+def _dft_calls(torch, n: int, batch: int):
+    """The two inverse 2-D DFT forms over the same (batch, n, n) complex
+    buffers: the tensor-core four-step (pt_ifft2_tc) and the FP32 register FFT
+    (pt_ifft2)."""
+    from pyturb_gb300 import _lib
+    from pyturb_gb300.backend import stream_handle
+    from pyturb_gb300.fourier import Grid
+
+    x = torch.randn((batch, n, n, 2), device="cuda")
+    y = torch.empty_like(x)
+    g = Grid(n, 0.01, np.zeros((0, 3)))
+
+    def tc():
+        _lib.call("pt_ifft2_tc", n, x.data_ptr(), y.data_ptr(), batch, stream_handle())
+
+    def fp32():
+        _lib.call("pt_ifft2", g.handle, x.data_ptr(), y.data_ptr(), batch, g.work.data_ptr(),
+                  g.work_bytes, stream_handle())
+
+    return x, y, {"tc_bf16x3": tc, "fp32_fft": fp32}
+
+
+def bench_tc_dft(torch, batch: int = 96, reps: int = 20) -> dict:
+    """The transform under every 512^2 frame and Monte-Carlo screen, in its two
+    forms: the inverse 2-D DFT of `batch` complex 512^2 images (192 MB in,
+    192 MB out, above the L2) as split-bf16 tensor-core four-step DFTs, and as
+    the FP32 register FFT; transforms/s and relative L2 against float64."""
+    n = 512
+    x, y, forms = _dft_calls(torch, n, batch)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    res = {"workload": f"inverse 2-D DFT of {batch} complex {n}^2 images per call "
+                       "(row pass + column pass), inputs above L2"}
+    # accuracy on a coloured spectrum (steep power law, like the screens')
+    rng = np.random.default_rng(3)
+    f = np.fft.fftfreq(n)
+    amp = (f[:, None] ** 2 + f[None, :] ** 2 + 1e-4) ** (-11.0 / 12.0)
+    z = (rng.standard_normal((2, n, n)) + 1j * rng.standard_normal((2, n, n))) * amp
+    exact = np.fft.ifft2(z) * (n * n)
+    x[:2].copy_(torch.from_numpy(np.stack([z.real, z.imag], -1).astype(np.float32)))
+    for name, fn in forms.items():
+        fn()
+        torch.cuda.synchronize()
+        o = y[:2].double().cpu().numpy()
+        err = float(np.linalg.norm(o[..., 0] + 1j * o[..., 1] - exact) / np.linalg.norm(exact))
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        sec = e0.elapsed_time(e1) / 1000.0 / reps
+        res[name] = {"transforms_per_s": batch / sec, "us_per_transform": sec / batch * 1e6,
+                     "two_pass_gbs": batch * n * n * 8 * 4 / sec / 1e9,
+                     "rel_l2_vs_fp64": err}
+    res["tc_over_fp32"] = res["tc_bf16x3"]["transforms_per_s"] / res["fp32_fft"]["transforms_per_s"]
+    # both pipelines spend one 512^2 complex transform per two real screens or
+    # frames, so the transform rate bounds the screens/s any form of them reaches
+    res["tc_form_bound_screens_or_frames_per_s"] = 2.0 * res["tc_bf16x3"]["transforms_per_s"]
+    res["note"] = ("tc_bf16x3 = 512 = 32 x 16 four-step DFT: per pass, the (line, n2) x 32-point "
+                   "and (line, k1) x 16-point DFT block matrices as tcgen05 kind::f16 products "
+                   "of three-term bf16 splits (six products, fp32 accumulation in tensor "
+                   "memory), twiddles in registers; persistent 256-thread CTAs, two per SM. "
+                   "fp32_fft = the register FFT under generate / sample / frames. The "
+                   "tc bound counts the transform alone (no spectrum fill, no pair "
+                   "extraction): a whole tc-form pipeline is slower than that")
+    return res
+
+
 def extrude_accuracy(torch, G, ext, r0s, steps: int = 512, screens: int = 3) -> dict:
     """Relative L2 error of each extrusion form against a float64 recursion
     with the same operator and injected noise: `screens` ring screens of the
@@ -513,8 +583,10 @@ def run_reference(args, rank: int) -> None:
 
 def run_case(args) -> None:
     """One small, named workload for profiling a kernel family under ncu (no
-    JSON line): ``generate`` (``--n``, ``--count``, ``--calls``) or
-    ``extrude`` (``--width``, ``--screens``, ``--case-steps``, ``--form``)."""
+    JSON line): ``generate`` (``--n``, ``--count``, ``--calls``),
+    ``extrude`` (``--width``, ``--screens``, ``--case-steps``, ``--form``) or
+    ``dft`` (512^2 x ``--count`` inverse DFTs, ``--calls``; ``--form`` fp32 for
+    the FFT, else the tensor-core form)."""
     import torch
 
     import pyturb_gb300 as G
@@ -523,6 +595,18 @@ def run_case(args) -> None:
     from pyturb_gb300.extrude import RingExtruder
 
     torch.cuda.set_device(0)
+    if args.case == "dft":
+        _x, _y, forms = _dft_calls(torch, 512, args.count)
+        fn = forms["tc_bf16x3" if args.form != "fp32" else "fp32_fft"]
+        fn()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.calls):
+            fn()
+        torch.cuda.synchronize()
+        dt = (time.perf_counter() - t0) / max(1, args.calls)
+        print(f"dft 512^2 x {args.count} form={args.form}: {dt * 1e6:.1f} us per call")
+        return
     if args.case == "generate":
         g = G.PhaseScreen(n=args.n, pixel_scale=8.0 / args.n, r0=0.15, L0=25.0,
                           subharmonics=3, seed=1)
@@ -562,7 +646,7 @@ def main() -> None:
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extrude", action="store_true")
     ap.add_argument("--no-diff", action="store_true")
-    ap.add_argument("--case", choices=["generate", "extrude"], default=None,
+    ap.add_argument("--case", choices=["generate", "extrude", "dft"], default=None,
                     help="run one small named workload for profiling and exit")
     ap.add_argument("--n", type=int, default=384)
     ap.add_argument("--count", type=int, default=64)
@@ -789,6 +873,7 @@ def main() -> None:
         "wall_s_timed_region": wall,
     }
     line["generate_256_screens_per_s"] = bench_generate(torch, G)
+    line["dft_512_tc_vs_fp32"] = bench_tc_dft(torch)
     if not args.no_extrude:
         line["extrude_1024"] = bench_extrude(torch, G)
     if not args.no_diff:

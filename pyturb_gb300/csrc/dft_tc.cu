@@ -7,15 +7,17 @@
 //   X[k1 + 32 k2] = sum_{n2} W16^{n2 k2} W512^{n2 k1} sum_{n1} W32^{n1 k1} x[16 n1 + n2],
 // W_N = e^{+2 pi i / N} (the unnormalised inverse transform of numpy.fft.ifft * N).
 //
-// A CTA of 128 threads transforms 8 lines (rows, or columns with a stride).
-// Stage 1: the 128 jobs (line, n2) times the real 64 x 64 block form of the
-// 32-point DFT, M = 128, N = 64, K = 64. Then a twiddle multiply in
-// registers. Stage 2: the 256 jobs (line, k1) times the 32 x 32 block form of
-// the 16-point DFT, two M = 128 tiles, N = 32, K = 32. Operands are split
-// into three bf16 terms (x = hi + mid + lo, 24 bits); the six products with
-// term indices summing to at most 2 accumulate in fp32 in tensor memory. The
-// lines are staged through shared memory, so loads and stores coalesce for
-// both the row and the column pass.
+// A persistent CTA of 256 threads (two per SM) transforms 8 lines at a time
+// (rows, or columns with a stride). Stage 1: the 128 jobs (line, n2) times
+// the real 64 x 64 block form of the 32-point DFT, M = 128, N = 64, K = 64
+// (A K-major). Then a twiddle multiply in registers. Stage 2: the 256 jobs
+// (line, k1) times the 32 x 32 block form of the 16-point DFT, two M = 128
+// tiles, N = 32, K = 32 (A MN-major, so that a thread's 8 consecutive k1 rows
+// are one 16-byte store). Data operands are split into three bf16 terms by
+// truncation (x = hi + mid + lo exactly), the DFT matrices by rounding; the
+// six products with term indices summing to at most 2 accumulate in fp32 in
+// tensor memory. The lines are staged through shared memory, so loads and
+// stores coalesce for both the row and the column pass.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -36,18 +38,21 @@ static inline void count_launch_d(int k = 1) {
 static __device__ int g_dft_error;
 
 namespace dft {
-constexpr int N = 512, N1 = 32, N2 = 16, LINES = 8;
+constexpr int N = 512, N1 = 32, N2 = 16, LINES = 8, THREADS = 256;
 constexpr int A1_TILE = 128 * 64 * 2;   // bytes of one bf16 term of a stage-1 A tile
 constexpr int B1_TILE = 64 * 64 * 2;    // stage-1 B (the 32-point DFT block matrix)
 constexpr int A2_TILE = 128 * 32 * 2;   // one stage-2 A tile, one term
 constexpr int B2_TILE = 32 * 32 * 2;    // stage-2 B (the 16-point DFT block matrix)
 constexpr int TERMS = 3;
-// shared memory: staged lines (fp32 complex) | A (stage 1, reused by stage 2) | B1 | B2
+// shared memory: staged lines (fp32 complex) | A (stage 1, reused by stage 2) |
+// B1 | B2, 110 KB, so that two CTAs share an SM (the twiddles live in
+// registers). Unswizzled operands need 16-byte alignment; the base is rounded
+// up to 128 bytes.
 constexpr int OFF_X = 0;
 constexpr int OFF_A = OFF_X + LINES * N * 8;                       // 32 KB
 constexpr int OFF_B1 = OFF_A + TERMS * A1_TILE;                    // + 48 KB
 constexpr int OFF_B2 = OFF_B1 + TERMS * B1_TILE;                   // + 24 KB
-constexpr int SMEM = OFF_B2 + TERMS * B2_TILE + 1024;              // + 6 KB + alignment
+constexpr int SMEM = OFF_B2 + TERMS * B2_TILE + 128;               // + 6 KB + alignment
 static_assert(2 * TERMS * A2_TILE <= TERMS * A1_TILE, "stage-2 tiles reuse the stage-1 space");
 
 __device__ __forceinline__ void split3(float v, uint16_t* t) {
@@ -58,6 +63,30 @@ __device__ __forceinline__ void split3(float v, uint16_t* t) {
     t[i] = __bfloat16_as_ushort(h);
     r -= __bfloat162float(h);
   }
+}
+
+// v = hi + mid + lo exactly, each a bf16 in the high half of the returned
+// bit pattern: truncate to the 8 leading significant bits, twice (both
+// differences are exact in fp32); the remainder has at most 8 significant
+// bits and so is a bf16 itself.
+__device__ __forceinline__ void split3t(float v, uint32_t* t) {
+  const uint32_t h = __float_as_uint(v) & 0xFFFF0000u;
+  const float r1 = v - __uint_as_float(h);
+  const uint32_t m = __float_as_uint(r1) & 0xFFFF0000u;
+  t[0] = h;
+  t[1] = m;
+  t[2] = __float_as_uint(r1 - __uint_as_float(m));
+}
+// two bf16 (the high halves of a and b) as one 32-bit word, a at the lower address
+__device__ __forceinline__ uint32_t pack_hi(uint32_t a, uint32_t b) { return __byte_perm(a, b, 0x7632); }
+
+// The stage-2 A tiles are MN-major without swizzle: 8 consecutive rows (M) of
+// one K index make a 16-byte core-matrix row, 8 K indices a core matrix; core
+// matrices are 128 bytes apart along M and A2_KCORE apart along K.
+constexpr int A2_KCORE = 16 * 128;
+constexpr uint32_t kMajorMN_A = 1u << 15;  // instruction descriptor: A is MN-major
+__device__ __forceinline__ uint32_t mn_offset(int mcore, int k) {
+  return (uint32_t)(mcore * 128 + (k >> 3) * A2_KCORE + (k & 7) * 16);
 }
 
 // e^{+2 pi i num / den} from the exact fraction (num reduced mod den)
@@ -89,166 +118,229 @@ __device__ void build_dft_b(uint8_t* sb, int tile_bytes) {
 }
 }  // namespace dft
 
-// lines [8 blockIdx.x, +8) of `lines`; line L: image L / 512, index j = L % 512;
-// element n of line (b, j) at in[b * img + j * ls + n * es] (complex units).
-// in and out may alias: a CTA reads all of its lines before it writes them,
-// and no two CTAs touch the same line.
-__global__ void __launch_bounds__(128)
-k_dft512_tc(const float2* in, float2* out, int lines, long long img, int ls, int es) {
+// Persistent CTAs of 256 threads: groups of 8 lines g = blockIdx.x, +
+// gridDim.x, ...; line L: image L / 512, index j = L % 512; element n of line
+// (b, j) at in[b * img + j * 512 + n] (rows) or in[b * img + n * 512 + j]
+// (kCols), complex units. in and out may alias: a CTA reads all of a group's
+// lines before it writes them, and no two CTAs touch the same line. The DFT
+// matrices and the twiddles are built once per CTA. Each phase splits its
+// 128 rows (stage-1 jobs, tensor-memory lanes) between the two halves of the
+// CTA by columns.
+template <bool kCols>
+__global__ void __launch_bounds__(dft::THREADS, 2)
+k_dft512_tc(const float2* in, float2* out, int lines, long long img) {
+  constexpr int ls = kCols ? 1 : dft::N;  // line stride (complex units)
   using namespace dft;
   extern __shared__ uint8_t smraw[];
   __shared__ uint64_t bar;
   __shared__ uint32_t tslot;
-  uint8_t* base = (uint8_t*)(((uintptr_t)smraw + 1023) & ~(uintptr_t)1023);
+  uint8_t* base = (uint8_t*)(((uintptr_t)smraw + 127) & ~(uintptr_t)127);
   float2* xs = (float2*)(base + OFF_X);
   uint8_t* sA = base + OFF_A;
   uint8_t* sB1 = base + OFF_B1;
   uint8_t* sB2 = base + OFF_B2;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int L0 = blockIdx.x * LINES;
-  if (L0 >= lines) return;
-  const long long b = L0 / N;
-  const int j0 = L0 % N;
-  const float2* src = in + b * img + (long long)j0 * ls;
-  float2* dst = out + b * img + (long long)j0 * ls;
+  const int q = tid & 127, half = tid >> 7;  // row (job / TMEM lane) and column half
+  const int groups = lines / LINES;
+  if ((int)blockIdx.x >= groups) return;
 
   if (warp == 0) tc::tmem_alloc(&tslot, 128);
   if (tid == 0) {
     tc::mbar_init(&bar, 1);
     tc::fence_mbar_init();
   }
-  // stage the 8 lines: along the line when it is contiguous, else across the lines
-  if (es == 1) {
-    for (int e = tid; e < LINES * N; e += 128) xs[e] = src[(long long)(e / N) * ls + e % N];
-  } else {
-    for (int e = tid; e < LINES * N; e += 128) {
-      const int n = e / LINES, r = e % LINES;
-      xs[r * N + n] = src[(long long)n * es + (long long)r * ls];
-    }
-  }
   build_dft_b<N1>(sB1, B1_TILE);
   build_dft_b<N2>(sB2, B2_TILE);
-  __syncthreads();
-  // stage-1 A: job q = 16 r + n2, K = [re x[16 n1 + n2] (n1 < 32) | im ...]
-  {
-    const int q = tid, r = q >> 4, n2 = q & 15;
-    for (int g = 0; g < 8; ++g) {  // 8 groups of 8 K values
-      uint32_t w4[TERMS][4];
+  // the twiddles W512^{n2 k1} of this thread's stage-1 row (n2 = q % 16) and
+  // column half (k1 in [16 half, 16 half + 16))
+  float twr[16], twi[16];
 #pragma unroll
-      for (int h = 0; h < 4; ++h) {
-        uint16_t ta[TERMS], tb[TERMS];
-#pragma unroll
-        for (int u = 0; u < 2; ++u) {
-          const int kk = 8 * g + 2 * h + u;
-          const int n1 = kk & 31;
-          const float2 x = xs[r * N + 16 * n1 + n2];
-          split3(kk < 32 ? x.x : x.y, u ? tb : ta);
-        }
-#pragma unroll
-        for (int t = 0; t < TERMS; ++t) w4[t][h] = (uint32_t)ta[t] | ((uint32_t)tb[t] << 16);
-      }
-      const uint32_t off = tc::core_offset(q, 8 * g, 64);
-#pragma unroll
-      for (int t = 0; t < TERMS; ++t)
-        *(uint4*)(sA + t * A1_TILE + off) = make_uint4(w4[t][0], w4[t][1], w4[t][2], w4[t][3]);
-    }
+  for (int i = 0; i < 16; ++i) {
+    const float2 w = unit((q & 15) * (16 * half + i), N);
+    twr[i] = w.x;
+    twi[i] = w.y;
   }
-  tc::fence_proxy_async_smem();
   tc::tc_fence_before();
   __syncthreads();
   tc::tc_fence_after();
   const uint32_t tmem = tslot;
+  // this warp's tensor-memory lane quarter
+  const uint32_t trow = tmem + ((uint32_t)((warp & 3) * 32) << 16);
   constexpr int pa[6] = {0, 0, 1, 0, 2, 1};
   constexpr int pb[6] = {0, 1, 0, 2, 0, 1};
-  if (tid == 0) {
-    const uint32_t idesc = tc::idesc_bf16(128, 64);
-    const uint32_t a0 = tc::smem_u32(sA), b0 = tc::smem_u32(sB1);
-    for (int p = 0; p < 6; ++p)
-      for (int ks = 0; ks < 4; ++ks) {
-        const uint64_t ad = tc::smem_desc(a0 + pa[p] * A1_TILE + ks * 256, 128, 64 * 16);
-        const uint64_t bd = tc::smem_desc(b0 + pb[p] * B1_TILE + ks * 256, 128, 64 * 16);
-        tc::mma_bf16(tmem, ad, bd, idesc, (p | ks) ? 1u : 0u);
-      }
-    tc::mma_commit(&bar);
-  }
-  bool ok = tc::mbar_wait(&bar, 0, &g_dft_error);
-  ok = __all_sync(0xffffffffu, ok);
-  tc::tc_fence_after();
-  __syncthreads();  // every thread is past the wait before stage-1 A is overwritten
-  if (ok) {
-    // row q of D1: Y[r][n2][k1] for k1 < 32 (re in columns 0..31, im 32..63);
-    // twiddle W512^{n2 k1}, then stage-2 A: job (r, k1) -> tile r / 4, row
-    // 32 (r % 4) + k1, K = [re (n2 < 16) | im]
-    const int q = 32 * warp + lane, r = q >> 4, n2 = q & 15;
-    float re[32], im[32];
-    const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
-    tc::tmem_ld16(trow + 0, re);
-    tc::tmem_ld16(trow + 16, re + 16);
-    tc::tmem_ld16(trow + 32, im);
-    tc::tmem_ld16(trow + 48, im + 16);
-    uint8_t* tile = sA + (r >> 2) * (TERMS * A2_TILE);
+  bool alive = true;
+  for (int grp = blockIdx.x; grp < groups && alive; grp += gridDim.x) {
+    const int L0 = grp * LINES;
+    const long long b = L0 / N;
+    const int j0 = L0 % N;
+    const float2* src = in + b * img + (long long)j0 * ls;
+    float2* dst = out + b * img + (long long)j0 * ls;
+    // stage the 8 lines, 16-byte loads, all 8 of a thread in flight before
+    // their stores: rows along the line, columns across the 8 lines (64 bytes
+    // per element index)
+    {
+      float4 v[8];
 #pragma unroll
-    for (int k1 = 0; k1 < 32; ++k1) {
-      const float2 w = dft::unit(n2 * k1, N);
-      const float yr = re[k1] * w.x - im[k1] * w.y;
-      const float yi = re[k1] * w.y + im[k1] * w.x;
-      uint16_t tr[TERMS], ti[TERMS];
-      dft::split3(yr, tr);
-      dft::split3(yi, ti);
-      const int row = 32 * (r & 3) + k1;
-      const uint32_t o_re = tc::core_offset(row, n2, 32), o_im = tc::core_offset(row, 16 + n2, 32);
-#pragma unroll
-      for (int t = 0; t < TERMS; ++t) {
-        *(uint16_t*)(tile + t * A2_TILE + o_re) = tr[t];
-        *(uint16_t*)(tile + t * A2_TILE + o_im) = ti[t];
+      for (int i = 0; i < 8; ++i) {
+        const int e4 = tid + THREADS * i;
+        v[i] = kCols ? *(const float4*)(src + (e4 >> 2) * N + 2 * (e4 & 3))
+                     : *(const float4*)(src + (e4 >> 8) * N + 2 * (e4 & 255));
       }
-    }
-  }
-  tc::fence_proxy_async_smem();
-  tc::tc_fence_before();
-  __syncthreads();
-  tc::tc_fence_after();
-  if (tid == 0 && ok) {
-    const uint32_t idesc = tc::idesc_bf16(128, 32);
-    const uint32_t b0 = tc::smem_u32(sB2);
-    for (int m = 0; m < 2; ++m) {
-      const uint32_t a0 = tc::smem_u32(sA + m * (TERMS * A2_TILE));
-      for (int p = 0; p < 6; ++p)
-        for (int ks = 0; ks < 2; ++ks) {
-          const uint64_t ad = tc::smem_desc(a0 + pa[p] * A2_TILE + ks * 256, 128, 32 * 16);
-          const uint64_t bd = tc::smem_desc(b0 + pb[p] * B2_TILE + ks * 256, 128, 32 * 16);
-          tc::mma_bf16(tmem + 64 + 32 * m, ad, bd, idesc, (p | ks) ? 1u : 0u);
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        const int e4 = tid + THREADS * i;
+        if (kCols) {
+          const int n = e4 >> 2, r = 2 * (e4 & 3);
+          xs[r * N + n] = make_float2(v[i].x, v[i].y);
+          xs[(r + 1) * N + n] = make_float2(v[i].z, v[i].w);
+        } else {
+          *(float4*)(xs + 2 * e4) = v[i];
         }
+      }
     }
-    tc::mma_commit(&bar);
-  }
-  bool ok2 = ok ? tc::mbar_wait(&bar, 1, &g_dft_error) : false;
-  ok2 = __all_sync(0xffffffffu, ok2);
-  tc::tc_fence_after();
-  if (ok2) {
-    // tile m, row 32 warp + lane = job (r = 4 m + warp, k1 = lane): X[r][k1 + 32 k2]
-    const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
-    for (int m = 0; m < 2; ++m) {
+    __syncthreads();
+    // stage-1 A (K-major): job q = 16 r + n2, K = [re x[16 n1 + n2] (n1 < 32) | im ...];
+    // this half: n1 in [16 half, 16 half + 16)
+    {
+      const int r = q >> 4, n2 = q & 15;
+#pragma unroll
+      for (int gg = 0; gg < 2; ++gg) {
+        const int g = 2 * half + gg;  // n1 in [8 g, 8 g + 8): K groups g (re) and g + 4 (im)
+        uint32_t wr[TERMS][4], wi[TERMS][4];
+#pragma unroll
+        for (int h = 0; h < 4; ++h) {
+          const float2 xa = xs[r * N + 16 * (8 * g + 2 * h) + n2];
+          const float2 xb = xs[r * N + 16 * (8 * g + 2 * h + 1) + n2];
+          uint32_t a[TERMS], c[TERMS];
+          split3t(xa.x, a);
+          split3t(xb.x, c);
+#pragma unroll
+          for (int t = 0; t < TERMS; ++t) wr[t][h] = pack_hi(a[t], c[t]);
+          split3t(xa.y, a);
+          split3t(xb.y, c);
+#pragma unroll
+          for (int t = 0; t < TERMS; ++t) wi[t][h] = pack_hi(a[t], c[t]);
+        }
+        const uint32_t o_re = tc::core_offset(q, 8 * g, 64), o_im = tc::core_offset(q, 32 + 8 * g, 64);
+#pragma unroll
+        for (int t = 0; t < TERMS; ++t) {
+          *(uint4*)(sA + t * A1_TILE + o_re) = make_uint4(wr[t][0], wr[t][1], wr[t][2], wr[t][3]);
+          *(uint4*)(sA + t * A1_TILE + o_im) = make_uint4(wi[t][0], wi[t][1], wi[t][2], wi[t][3]);
+        }
+      }
+    }
+    tc::fence_proxy_async_smem();
+    tc::tc_fence_before();
+    __syncthreads();
+    tc::tc_fence_after();
+    if (tid == 0) {
+      const uint32_t idesc = tc::idesc_bf16(128, 64);
+      const uint32_t a0 = tc::smem_u32(sA), b0 = tc::smem_u32(sB1);
+      for (int p = 0; p < 6; ++p)
+        for (int ks = 0; ks < 4; ++ks) {
+          const uint64_t ad = tc::smem_desc(a0 + pa[p] * A1_TILE + ks * 256, 128, 64 * 16);
+          const uint64_t bd = tc::smem_desc(b0 + pb[p] * B1_TILE + ks * 256, 128, 64 * 16);
+          tc::mma_bf16(tmem, ad, bd, idesc, (p | ks) ? 1u : 0u);
+        }
+      tc::mma_commit(&bar);
+    }
+    bool ok = true;  // one warp polls the barrier; the others sleep in the CTA barrier
+    if (warp == 0) ok = tc::mbar_wait(&bar, 0, &g_dft_error);
+    ok = __syncthreads_and(ok);  // also: every thread is past the wait before A is rewritten
+    tc::tc_fence_after();
+    if (!ok) {
+      alive = false;
+      break;
+    }
+    {
+      // row q of D1: Y[r][n2][k1] (re in columns k1, im in 32 + k1), this
+      // half's k1 in [16 half, +16); twiddle W512^{n2 k1}, then stage-2 A
+      // (MN-major): job (r, k1) -> tile r / 4, row 32 (r % 4) + k1, K = [re
+      // (n2 < 16) | im]; 8 consecutive k1 make one 16-byte store
+      const int r = q >> 4, n2 = q & 15;
+      float re[16], im[16];
+      tc::tmem_ld16(trow + 16 * half, re);
+      tc::tmem_ld16(trow + 32 + 16 * half, im);
+      uint8_t* tile = sA + (r >> 2) * (TERMS * A2_TILE);
+#pragma unroll
+      for (int jj = 0; jj < 2; ++jj) {  // rows 32 (r % 4) + 8 j .. + 7, j = 2 half + jj
+        uint32_t wr[TERMS][4], wi[TERMS][4];
+#pragma unroll
+        for (int h = 0; h < 4; ++h) {
+          uint32_t ar[TERMS], br[TERMS], ai[TERMS], bi[TERMS];
+          const int ka = 8 * jj + 2 * h, kb = ka + 1;
+          split3t(re[ka] * twr[ka] - im[ka] * twi[ka], ar);
+          split3t(re[ka] * twi[ka] + im[ka] * twr[ka], ai);
+          split3t(re[kb] * twr[kb] - im[kb] * twi[kb], br);
+          split3t(re[kb] * twi[kb] + im[kb] * twr[kb], bi);
+#pragma unroll
+          for (int t = 0; t < TERMS; ++t) {
+            wr[t][h] = pack_hi(ar[t], br[t]);
+            wi[t][h] = pack_hi(ai[t], bi[t]);
+          }
+        }
+        const int mc = 4 * (r & 3) + 2 * half + jj;  // core matrix along M
+        const uint32_t o_re = mn_offset(mc, n2), o_im = mn_offset(mc, 16 + n2);
+#pragma unroll
+        for (int t = 0; t < TERMS; ++t) {
+          *(uint4*)(tile + t * A2_TILE + o_re) = make_uint4(wr[t][0], wr[t][1], wr[t][2], wr[t][3]);
+          *(uint4*)(tile + t * A2_TILE + o_im) = make_uint4(wi[t][0], wi[t][1], wi[t][2], wi[t][3]);
+        }
+      }
+    }
+    tc::fence_proxy_async_smem();
+    tc::tc_fence_before();
+    __syncthreads();
+    tc::tc_fence_after();
+    if (tid == 0) {
+      const uint32_t idesc = tc::idesc_bf16(128, 32) | kMajorMN_A;
+      const uint32_t b0 = tc::smem_u32(sB2);
+      for (int m = 0; m < 2; ++m) {
+        const uint32_t a0 = tc::smem_u32(sA + m * (TERMS * A2_TILE));
+        for (int p = 0; p < 6; ++p)
+          for (int ks = 0; ks < 2; ++ks) {
+            const uint64_t ad = tc::smem_desc(a0 + pa[p] * A2_TILE + ks * 2 * A2_KCORE, A2_KCORE, 128);
+            const uint64_t bd = tc::smem_desc(b0 + pb[p] * B2_TILE + ks * 256, 128, 32 * 16);
+            tc::mma_bf16(tmem + 64 + 32 * m, ad, bd, idesc, (p | ks) ? 1u : 0u);
+          }
+      }
+      tc::mma_commit(&bar);
+    }
+    bool ok2 = true;
+    if (warp == 0) ok2 = tc::mbar_wait(&bar, 1, &g_dft_error);
+    ok2 = __syncthreads_and(ok2);
+    tc::tc_fence_after();
+    if (!ok2) {
+      alive = false;
+      break;
+    }
+    {
+      // tile m = half, row 32 (warp % 4) + lane = job (r = 4 m + warp % 4, k1 = lane):
+      // X[r][k1 + 32 k2], re in columns k2, im in 16 + k2
       float v[32];
-      tc::tmem_ld16(trow + 64 + 32 * m, v);
-      tc::tmem_ld16(trow + 64 + 32 * m + 16, v + 16);
-      const int r = 4 * m + warp, k1 = lane;
+      tc::tmem_ld16(trow + 64 + 32 * half, v);
+      tc::tmem_ld16(trow + 64 + 32 * half + 16, v + 16);
+      const int r = 4 * half + (warp & 3), k1 = lane;
 #pragma unroll
       for (int k2 = 0; k2 < 16; ++k2) xs[r * N + k1 + 32 * k2] = make_float2(v[k2], v[16 + k2]);
     }
+    tc::tc_fence_before();
+    __syncthreads();
+#pragma unroll 4
+    for (int i = 0; i < 8; ++i) {
+      const int e4 = tid + THREADS * i;
+      if (kCols) {
+        const int n = e4 >> 2, r = 2 * (e4 & 3);
+        const float2 u = xs[r * N + n], w = xs[(r + 1) * N + n];
+        *(float4*)(dst + (e4 >> 2) * N + r) = make_float4(u.x, u.y, w.x, w.y);
+      } else {
+        *(float4*)(dst + (e4 >> 8) * N + 2 * (e4 & 255)) = *(const float4*)(xs + 2 * e4);
+      }
+    }
+    __syncthreads();
   }
   tc::tc_fence_before();
   __syncthreads();
-  if (ok2) {
-    if (es == 1) {
-      for (int e = tid; e < LINES * N; e += 128) dst[(long long)(e / N) * ls + e % N] = xs[e];
-    } else {
-      for (int e = tid; e < LINES * N; e += 128) {
-        const int n = e / LINES, r = e % LINES;
-        dst[(long long)n * es + (long long)r * ls] = xs[r * N + n];
-      }
-    }
-  }
   if (warp == 0) tc::tmem_dealloc(tmem, 128);
 }
 
@@ -266,22 +358,40 @@ extern "C" int pt_ifft2_tc(int ns, const float* in, float* out, int batch, void*
   if ((long long)batch * dft::N / dft::LINES > 0x7fffffffLL)
     return fail(PT_ERR_ARG, "pt_ifft2_tc: batch too large");
   cudaStream_t s = (cudaStream_t)stream;
-  static bool attr = false;
-  if (!attr) {
-    if (int rc = check_cuda(cudaFuncSetAttribute(k_dft512_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                 dft::SMEM),
-                            "pt_ifft2_tc: shared memory"))
-      return rc;
-    attr = true;
+  static int resident = 0;  // CTAs of k_dft512_tc the device holds at once
+  if (!resident) {
+    int dev = 0;
+    if (int rc = check_cuda(cudaGetDevice(&dev), "pt_ifft2_tc: device")) return rc;
+    cudaDeviceProp prop;
+    if (int rc = check_cuda(cudaGetDeviceProperties(&prop, dev), "pt_ifft2_tc: properties")) return rc;
+    // CTAs per SM from the SM's shared memory and registers (the occupancy
+    // calculator does not follow the carveout preference)
+    int per_sm = 4;
+    for (const void* f : {(const void*)k_dft512_tc<false>, (const void*)k_dft512_tc<true>}) {
+      if (int rc = check_cuda(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, dft::SMEM),
+                              "pt_ifft2_tc: shared memory"))
+        return rc;
+      if (int rc = check_cuda(cudaFuncSetAttribute(f, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                                   (int)cudaSharedmemCarveoutMaxShared),
+                              "pt_ifft2_tc: carveout"))
+        return rc;
+      cudaFuncAttributes fa;
+      if (int rc = check_cuda(cudaFuncGetAttributes(&fa, f), "pt_ifft2_tc: attributes")) return rc;
+      const size_t per_cta = (size_t)dft::SMEM + fa.sharedSizeBytes + prop.reservedSharedMemPerBlock;
+      per_sm = std::min(per_sm, (int)(prop.sharedMemPerMultiprocessor / per_cta));
+      per_sm = std::min(per_sm, prop.regsPerMultiprocessor / std::max(1, fa.numRegs * dft::THREADS));
+    }
+    if (per_sm < 1) return fail(PT_ERR_UNSUPPORTED, "pt_ifft2_tc: the kernel does not fit on an SM");
+    resident = prop.multiProcessorCount * per_sm;
   }
   const int lines = batch * dft::N;
   const long long img = (long long)dft::N * dft::N;
-  const dim3 grid((unsigned)(lines / dft::LINES));
+  // persistent: one wave of resident CTAs, each over many groups of 8 lines
+  const dim3 grid((unsigned)std::min(lines / dft::LINES, resident));
   {
     ProfScope ps("k_dft512_tc", s);
-    k_dft512_tc<<<grid, 128, dft::SMEM, s>>>((const float2*)in, (float2*)out, lines, img, dft::N, 1);
-    k_dft512_tc<<<grid, 128, dft::SMEM, s>>>((const float2*)out, (float2*)out, lines, img, 1,
-                                             dft::N);
+    k_dft512_tc<false><<<grid, dft::THREADS, dft::SMEM, s>>>((const float2*)in, (float2*)out, lines, img);
+    k_dft512_tc<true><<<grid, dft::THREADS, dft::SMEM, s>>>((const float2*)out, (float2*)out, lines, img);
   }
   count_launch_d(2);
   return check_launch("pt_ifft2_tc");
