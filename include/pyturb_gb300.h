@@ -413,10 +413,11 @@ int pt_lr_grad_params(int B, int L, int S, int T, int D, int n, const double* ma
                       const float* screens, const float* w, const int64_t* fix,
                       const float* grad_out, float* partial, void* stream);
 /* dL/dscreens (B, L, S, S): the transpose of the gather, as a deterministic
- * gather over screen tiles (every element written once, no atomics). */
+ * gather over screen tiles (every element written once, no atomics); added
+ * to grad_screens when accumulate != 0 (frames taken in chunks). */
 int pt_lr_grad_screens(int B, int L, int S, int T, int D, int n, const double* mag,
                        const float* w, const int64_t* fix, const float* grad_out,
-                       float* grad_screens, void* stream);
+                       int accumulate, float* grad_screens, void* stream);
 
 /* ---- validation diagnostics ---------------------------------------------
  * pyturb.utils.structure_function (src/pyturb/utils.py:159-201): for a stack
@@ -451,28 +452,37 @@ int pt_tc_probe(int N, int K, const uint16_t* A, const uint16_t* B, float* D, vo
 
 /* ---- adjoint of the spectral frame synthesis ---------------------------
  * No counterpart in the reference (it has no gradients). The forward is
- * pt_frames without subharmonics, with per-layer weights folded into the
- * spectra: y_f = scale * crop(Re IDFT(sum_l w_l S_l Phi_lf)), Phi_lf =
- * exp(2 pi i (fx sx[f,l] + fy sy[f,l])) (Atmosphere._integrate,
- * src/pyturb/atmosphere.py:882-938). Backward, for upstream g (F, n_out, n_out):
+ * pt_frames, with per-layer weights folded into the spectra and the
+ * subharmonic coefficients: y_f = scale * crop(Re IDFT(sum_l w_l S_l Phi_lf)
+ * + low_f), Phi_lf = exp(2 pi i (fx sx[f,l] + fy sy[f,l])) (Atmosphere.
+ * _integrate, src/pyturb/atmosphere.py:882-938). Backward, for upstream g
+ * (F, n_out, n_out), frames in any chunks (the spectra gradient accumulates):
  *  1. pt_synth_adj_pack: z (ceil(F/2), ns, ns) complex = scale * conj(g_2p +
  *     i g_2p+1) zero-padded at (crop, crop);
  *  2. pt_ifft2(grid, z, z, ceil(F/2), ...) in place (the forward DFT by
  *     conjugation);
  *  3. pt_synth_adj_phasors: ph (L, F, 2, ns) complex from DEVICE shifts
  *     sx, sy (F, L) f64 [m], the forward's fixed-point ramps;
- *  4. pt_synth_adj_spectra: dL/dS (L, ns, ns) complex (d/dRe + i d/dIm);
+ *  4. pt_synth_adj_spectra: dL/dS (L, ns, ns) complex (d/dRe + i d/dIm),
+ *     added to grad_spectra when accumulate != 0;
  *  5. pt_synth_adj_params: out (L, F, 3) f64 = [dL/dw_l contribution of
- *     frame f, dL/dsx[f,l], dL/dsy[f,l]]. */
+ *     frame f, dL/dsx[f,l], dL/dsy[f,l]];
+ *  6. with subharmonic levels (atmosphere.py:921-935): pt_synth_adj_sh: out
+ *     (F, 18 P + 1) f64 = per frame the projections sum_xy g_f(x, y)
+ *     b_pi(crop + x) b_pj(crop + y) (re, im; p, i, j row-major) on the grid's
+ *     basis rows b_pi(x) = exp(2 pi i f_pi (x - ns/2) dx), then sum_xy g_f;
+ *     the caller forms the level gradients from these (9 P values a frame). */
 int pt_synth_adj_pack(int ns, int F, int crop, int n_out, float scale, const float* g, float* z,
                       void* stream);
 int pt_synth_adj_phasors(int ns, double pixel_scale, int L, int F, const double* sx,
                          const double* sy, float* ph, void* stream);
 int pt_synth_adj_spectra(int ns, int L, int F, const float* w, const float* Z, const float* ph,
-                         float* grad_spectra, void* stream);
+                         int accumulate, float* grad_spectra, void* stream);
 int pt_synth_adj_params(int ns, double pixel_scale, int L, int F, const float* w,
                         const float* spectra, const float* Z, const float* ph, double* out,
                         void* stream);
+int pt_synth_adj_sh(const pt_grid* grid, int F, int crop, int n_out, const float* g, double* out,
+                    void* stream);
 
 #ifdef __cplusplus
 }

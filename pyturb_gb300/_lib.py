@@ -142,7 +142,7 @@ SIGNATURES = {
     "pt_lr_forward": (i32, [i32, i32, i32, i32, i32, i32, dptr, vp, vp, vp, vp, vp]),
     "pt_lr_partial_count": (sz, [i32, i32, i32, i32, i32]),
     "pt_lr_grad_params": (i32, [i32, i32, i32, i32, i32, i32, dptr, vp, vp, vp, vp, vp, vp]),
-    "pt_lr_grad_screens": (i32, [i32, i32, i32, i32, i32, i32, dptr, vp, vp, vp, vp, vp]),
+    "pt_lr_grad_screens": (i32, [i32, i32, i32, i32, i32, i32, dptr, vp, vp, vp, i32, vp, vp]),
     "pt_structure_workspace_bytes": (sz, [i32, i32, i32, i32]),
     "pt_structure_function": (i32, [i32, i32, i32, vp, i32, vp, vp, sz, vp]),
     "pt_matmul_nt_workspace_bytes": (sz, [i32, i32, i32]),
@@ -159,8 +159,9 @@ SIGNATURES = {
                                   i32, vp, vp, vp, vp, vp, vp, vp, sz, vp]),
     "pt_synth_adj_pack": (i32, [i32, i32, i32, i32, f32, vp, vp, vp]),
     "pt_synth_adj_phasors": (i32, [i32, f64, i32, i32, vp, vp, vp, vp]),
-    "pt_synth_adj_spectra": (i32, [i32, i32, i32, vp, vp, vp, vp, vp]),
+    "pt_synth_adj_spectra": (i32, [i32, i32, i32, vp, vp, vp, i32, vp, vp]),
     "pt_synth_adj_params": (i32, [i32, f64, i32, i32, vp, vp, vp, vp, vp, vp]),
+    "pt_synth_adj_sh": (i32, [vp, i32, i32, i32, vp, vp, vp]),
 }
 
 

@@ -34,7 +34,7 @@ static inline void count_launch_r(int k = 1) {
 constexpr int kLrMaxLayers = 32;
 constexpr int kLrMaxMag = 256;   // D * L entries of the magnification table
 constexpr int kLrBand = 64;      // pupil rows per CTA (forward, parameter gradients)
-constexpr int kLrTile = 64;      // screen tile edge (screen gradient)
+constexpr int kLrTile = 64;      // screen tile width (screen gradient); height TR = 64 or 128
 constexpr long long kLrOne = 1ll << 32;
 
 struct LrMag {
@@ -223,32 +223,38 @@ __device__ __forceinline__ long long first_above(long long a, long long p0, long
   return x;
 }
 
-// Screen gradient: CTA = (screen tile, layer, b). For each (t, d) and each
-// wrap image of the tile window, the pupil block that reaches the tile is
-// staged in shared memory, spread along columns into the tile's columns, then
-// along rows into the tile's pixels, accumulated in registers in a fixed
-// order and written once (times w_l). KM bounds the pupil samples whose
-// bilinear footprint covers one screen pixel along one axis: ceil(2 / mag).
-template <int KM>
+// Screen gradient: CTA = (screen tile of TR rows x 64 columns, layer, b). For
+// each (t, d) and each wrap image of the tile window, the pupil block that
+// reaches the tile is staged in shared memory, spread along columns into the
+// tile's columns, then along rows into the tile's pixels, accumulated in
+// registers in a fixed order and written once (times w_l, or added). KM
+// bounds the pupil samples whose bilinear footprint covers one screen pixel
+// along one axis: ceil(2 / mag); ymaxR / ymaxC bound the block's rows /
+// columns. With vec (n a multiple of 4 and g 16-byte aligned) the block is
+// staged with 16-byte copies from the 4-float boundary at or below its first
+// column (sh floats of lead-in); otherwise with 4-byte copies (sh = 0). The
+// stage row stride is ystr = ymaxC + 4 rounded up to a multiple of 4.
+template <int KM, int TR>
 __global__ void __launch_bounds__(256)
-k_lr_grad_screens(int L, int S, int T, int D, int n, int tiles, int ymax,
-                  const float* __restrict__ w, const long long* __restrict__ fix,
-                  const float* __restrict__ g, float* __restrict__ grad) {
+k_lr_grad_screens(int L, int S, int T, int D, int n, int tiles_c, int ymaxR, int ymaxC, int ystr,
+                  int vec, const float* __restrict__ w, const long long* __restrict__ fix,
+                  const float* __restrict__ g, int accumulate, float* __restrict__ grad) {
+  constexpr int NQ = TR / 4;                     // pixels a thread accumulates
   extern __shared__ float smx[];
-  float* gsm = smx;                              // ymax * ymax
-  float* hsm = gsm + (size_t)ymax * ymax;        // ymax * kLrTile
-  float* rw = hsm + (size_t)ymax * kLrTile;      // kLrTile * KM
-  int* ry = (int*)(rw + kLrTile * KM);           // kLrTile
-  const int tile_c = blockIdx.x % tiles, tile_r = blockIdx.x / tiles;
+  float* gsm = smx;                              // ymaxR * ystr (16-byte aligned rows)
+  float* hsm = gsm + (size_t)ymaxR * ystr;       // ymaxR * kLrTile
+  float* rw = hsm + (size_t)ymaxR * kLrTile;     // TR * KM row weights
+  int* rk = (int*)(rw + TR * KM);                // TR * KM: clamped hsm offsets of the taps
+  const int tile_c = blockIdx.x % tiles_c, tile_r = blockIdx.x / tiles_c;
   const int l = blockIdx.y, b = blockIdx.z;
-  const int R0 = tile_r * kLrTile, C0 = tile_c * kLrTile;
-  const int TH = min(kLrTile, S - R0), TW = min(kLrTile, S - C0);
+  const int R0 = tile_r * TR, C0 = tile_c * kLrTile;
+  const int TH = min(TR, S - R0), TW = min(kLrTile, S - C0);
   const int pc = threadIdx.x & (kLrTile - 1), pq = threadIdx.x >> 6;  // 4 row groups
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const long long span = (long long)S * kLrOne;
-  float acc[16];
+  float acc[NQ];
 #pragma unroll
-  for (int q = 0; q < 16; ++q) acc[q] = 0.f;
+  for (int q = 0; q < NQ; ++q) acc[q] = 0.f;
   for (int td = 0; td < T * D; ++td) {
     const long long* fx = fix + ((size_t)td * L + l) * 3;
     const long long p0r = fx[0], p0c = fx[1], m = fx[2];
@@ -262,7 +268,7 @@ k_lr_grad_screens(int L, int S, int T, int D, int n, int tiles, int ymax,
       if (!(wr0 < ur1 && wr1 > p0r)) continue;
       const int ylo = (int)max(0ll, first_above(wr0, p0r, m, inv_m));
       const int yhi = (int)min((long long)n, first_above(wr1 - 1, p0r, m, inv_m));  // exclusive
-      const int ny = min(yhi - ylo, ymax);  // the min cannot bind: ymax bounds the window
+      const int ny = min(yhi - ylo, ymaxR);  // the min cannot bind: ymaxR bounds the window
       if (ny <= 0) continue;
       for (int kc = 0; kc < 2; ++kc) {
         const long long wc0 = (long long)(C0 - 1) * kLrOne + kc * span;
@@ -270,11 +276,12 @@ k_lr_grad_screens(int L, int S, int T, int D, int n, int tiles, int ymax,
         if (!(wc0 < uc1 && wc1 > p0c)) continue;
         const int xlo = (int)max(0ll, first_above(wc0, p0c, m, inv_m));
         const int xhi = (int)min((long long)n, first_above(wc1 - 1, p0c, m, inv_m));
-        const int nx = min(xhi - xlo, ymax);
+        const int nx = min(xhi - xlo, ymaxC);
         if (nx <= 0) continue;
-        // this thread's column taps (registers)
+        const int sh = vec ? (xlo & 3) : 0;  // lead-in floats before xlo in a stage row
+        // this thread's column taps (registers) as stage-row offsets
         float cwt[KM];
-        int cx0;
+        int ci[KM];
         {
           const long long pf = (long long)(C0 + pc) * kLrOne + kc * span;
           const long long xa = first_above(pf - kLrOne, p0c, m, inv_m);
@@ -285,11 +292,11 @@ k_lr_grad_screens(int L, int S, int T, int D, int n, int tiles, int ymax,
             const long long ad = dl < 0 ? -dl : dl;
             const bool in = pc < TW && ad < kLrOne && x >= xlo && x < xlo + nx;
             cwt[k] = in ? 1.f - (float)ad * 2.3283064365386963e-10f : 0.f;
+            ci[k] = sh + min(max((int)(x - xlo), 0), nx - 1);
           }
-          cx0 = (int)(xa - xlo);
         }
-        // row taps of the tile (shared)
-        if (threadIdx.x < kLrTile) {
+        // row taps of the tile (shared): weights and clamped hsm offsets
+        if (threadIdx.x < TR) {
           const int p = threadIdx.x;
           const long long pf = (long long)(R0 + p) * kLrOne + kr * span;
           const long long ya = first_above(pf - kLrOne, p0r, m, inv_m);
@@ -300,46 +307,51 @@ k_lr_grad_screens(int L, int S, int T, int D, int n, int tiles, int ymax,
             const long long ad = dl < 0 ? -dl : dl;
             const bool in = p < TH && ad < kLrOne && y >= ylo && y < ylo + ny;
             rw[p * KM + k] = in ? 1.f - (float)ad * 2.3283064365386963e-10f : 0.f;
+            rk[p * KM + k] = min(max((int)(y - ylo), 0), ny - 1) * kLrTile;
           }
-          ry[p] = (int)(ya - ylo);
         }
         // stage the pupil block with asynchronous copies (all of a thread's
-        // loads in flight at once, one wait)
-        for (int yy = warp; yy < ny; yy += 8) {
-          const float* src = gi + (size_t)(ylo + yy) * n + xlo;
-          for (int xx = lane; xx < nx; xx += 32) {
-            asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(
-                             (uint32_t)__cvta_generic_to_shared(gsm + yy * ymax + xx)),
-                         "l"(src + xx)
+        // copies in flight at once, one wait)
+        if (vec) {
+          const int nq = (sh + nx + 3) >> 2;  // 16-byte pieces a row; ends at or before n
+          for (int e = threadIdx.x; e < ny * nq; e += blockDim.x) {
+            const int yy = e / nq, xq = e - yy * nq;
+            const float* src = gi + (size_t)(ylo + yy) * n + (xlo - sh) + 4 * xq;
+            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(
+                             (uint32_t)__cvta_generic_to_shared(gsm + yy * ystr + 4 * xq)),
+                         "l"(src)
                          : "memory");
+          }
+        } else {
+          for (int yy = warp; yy < ny; yy += 8) {
+            const float* src = gi + (size_t)(ylo + yy) * n + xlo;
+            for (int xx = lane; xx < nx; xx += 32) {
+              asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(
+                               (uint32_t)__cvta_generic_to_shared(gsm + yy * ystr + xx)),
+                           "l"(src + xx)
+                           : "memory");
+            }
           }
         }
         asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
         __syncthreads();
-        // column pass: h[yy][pc] = sum_k cwt[k] g[yy][cx0 + k]
-        int ci[KM];
-#pragma unroll
-        for (int k = 0; k < KM; ++k) ci[k] = min(max(cx0 + k, 0), nx - 1);
+        // column pass: h[yy][pc] = sum_k cwt[k] g[yy][ci[k]]
         for (int yy = pq; yy < ny; yy += 4) {
-          const float* row = gsm + yy * ymax;
+          const float* row = gsm + yy * ystr;
           float h = 0.f;
 #pragma unroll
           for (int k = 0; k < KM; ++k) h = fmaf(cwt[k], row[ci[k]], h);
           hsm[yy * kLrTile + pc] = h;
         }
         __syncthreads();
-        // row pass into the thread's 16 pixels
+        // row pass into the thread's NQ pixels
 #pragma unroll
-        for (int q = 0; q < 16; ++q) {
+        for (int q = 0; q < NQ; ++q) {
           const int r = pq + 4 * q;
-          const int y0 = ry[r];
-          float s = acc[q];
+          float sacc = acc[q];
 #pragma unroll
-          for (int k = 0; k < KM; ++k) {
-            const int yy = min(max(y0 + k, 0), ny - 1);
-            s = fmaf(rw[r * KM + k], hsm[yy * kLrTile + pc], s);
-          }
-          acc[q] = s;
+          for (int k = 0; k < KM; ++k) sacc = fmaf(rw[r * KM + k], hsm[rk[r * KM + k] + pc], sacc);
+          acc[q] = sacc;
         }
         __syncthreads();
       }
@@ -348,9 +360,12 @@ k_lr_grad_screens(int L, int S, int T, int D, int n, int tiles, int ymax,
   const float wl = w[l];
   float* gl = grad + ((size_t)b * L + l) * S * S;
 #pragma unroll
-  for (int q = 0; q < 16; ++q) {
+  for (int q = 0; q < NQ; ++q) {
     const int r = pq + 4 * q;
-    if (r < TH && pc < TW) gl[(size_t)(R0 + r) * S + C0 + pc] = wl * acc[q];
+    if (r < TH && pc < TW) {
+      float* o = gl + (size_t)(R0 + r) * S + C0 + pc;
+      *o = accumulate ? *o + wl * acc[q] : wl * acc[q];
+    }
   }
 }
 
@@ -435,44 +450,64 @@ extern "C" size_t pt_lr_partial_count(int B, int L, int T, int D, int n) {
 
 extern "C" int pt_lr_grad_screens(int B, int L, int S, int T, int D, int n, const double* mag,
                                   const float* weights, const int64_t* fix, const float* grad_out,
-                                  float* grad_screens, void* stream) {
+                                  int accumulate, float* grad_screens, void* stream) {
   if (int rc = lr_check("pt_lr_grad_screens", B, L, S, T, D, n, mag)) return rc;
   if (!weights || !fix || !grad_out || !grad_screens)
     return fail(PT_ERR_ARG, "pt_lr_grad_screens: NULL pointer");
   double mmin = 4.0;
   for (int k = 0; k < D * L; ++k) mmin = std::min(mmin, mag[k]);
-  // pupil samples reaching an open window of kLrTile + 1 screen pixels: at most
-  // ceil((kLrTile + 1) / mag); taps per screen pixel and axis: ceil(2 / mag)
-  const int ymax = (int)std::ceil((kLrTile + 1) / mmin) + 1;
+  // pupil samples reaching an open window of E + 1 screen pixels: at most
+  // ceil((E + 1) / mag); taps per screen pixel and axis: ceil(2 / mag)
   const int km = (int)std::ceil(2.0 / mmin);
   if (km > 8) return fail(PT_ERR_UNSUPPORTED, "pt_lr_grad_screens: magnification too small");
   const int KM = km <= 2 ? 2 : km <= 3 ? 3 : km <= 4 ? 4 : 8;
-  const size_t smem = sizeof(float) * ((size_t)ymax * ymax + (size_t)ymax * kLrTile +
-                                       (size_t)kLrTile * KM) + kLrTile * sizeof(int);
+  const int ymaxC = (int)std::ceil((kLrTile + 1) / mmin) + 1;
+  const int ystr = ((ymaxC + 4) + 3) & ~3;
+  const int vec = (n % 4 == 0) && ((uintptr_t)grad_out % 16 == 0);
+  auto smem_for = [&](int TR, int ymaxR) {
+    return sizeof(float) * ((size_t)ymaxR * ystr + (size_t)ymaxR * kLrTile + (size_t)TR * KM) +
+           (size_t)TR * KM * sizeof(int);
+  };
+  // tiles 128 high when two CTAs still fit an SM (per-tile work amortises the
+  // per-(t, d) window and tap set-up), else 64
+  int TR = 128, ymaxR = (int)std::ceil((128 + 1) / mmin) + 1;
+  if (smem_for(TR, ymaxR) > 110 * 1024) {
+    TR = 64;
+    ymaxR = ymaxC;
+  }
+  const size_t smem = smem_for(TR, ymaxR);
   if (smem > 200 * 1024) return fail(PT_ERR_UNSUPPORTED, "pt_lr_grad_screens: magnification too small");
   if (B > 65535) return fail(PT_ERR_UNSUPPORTED, "pt_lr_grad_screens: B must be <= 65535");
   cudaStream_t s = (cudaStream_t)stream;
-  const int tiles = (S + kLrTile - 1) / kLrTile;
-  dim3 grid(tiles * tiles, L, B);
+  const int tiles_c = (S + kLrTile - 1) / kLrTile, tiles_r = (S + TR - 1) / TR;
+  dim3 grid(tiles_r * tiles_c, L, B);
   const long long* fx = (const long long*)fix;
   ProfScope ps("k_lr_grad_screens", s);
-#define PT_LR_GS(KMV)                                                                          \
+#define PT_LR_GS(KMV, TRV)                                                                     \
   do {                                                                                         \
     static bool attr = false;                                                                  \
     if (!attr) {                                                                               \
-      if (int rc = check_cuda(cudaFuncSetAttribute(k_lr_grad_screens<KMV>,                     \
+      if (int rc = check_cuda(cudaFuncSetAttribute(k_lr_grad_screens<KMV, TRV>,                \
                                                    cudaFuncAttributeMaxDynamicSharedMemorySize, \
                                                    200 * 1024), "pt_lr_grad_screens"))        \
         return rc;                                                                             \
       attr = true;                                                                             \
     }                                                                                          \
-    k_lr_grad_screens<KMV><<<grid, 256, smem, s>>>(L, S, T, D, n, tiles, ymax, weights, fx,    \
-                                                   grad_out, grad_screens);                    \
+    k_lr_grad_screens<KMV, TRV><<<grid, 256, smem, s>>>(L, S, T, D, n, tiles_c, ymaxR, ymaxC,  \
+                                                        ystr, vec, weights, fx, grad_out,      \
+                                                        accumulate, grad_screens);             \
   } while (0)
-  if (KM == 2) PT_LR_GS(2);
-  else if (KM == 3) PT_LR_GS(3);
-  else if (KM == 4) PT_LR_GS(4);
-  else PT_LR_GS(8);
+  if (TR == 128) {
+    if (KM == 2) PT_LR_GS(2, 128);
+    else if (KM == 3) PT_LR_GS(3, 128);
+    else if (KM == 4) PT_LR_GS(4, 128);
+    else PT_LR_GS(8, 128);
+  } else {
+    if (KM == 2) PT_LR_GS(2, 64);
+    else if (KM == 3) PT_LR_GS(3, 64);
+    else if (KM == 4) PT_LR_GS(4, 64);
+    else PT_LR_GS(8, 64);
+  }
 #undef PT_LR_GS
   count_launch_r();
   return check_launch("pt_lr_grad_screens");

@@ -1734,6 +1734,85 @@ __global__ void k_translate_sh(int P, int L, TranslateArgs a, const double* __re
 }
 }  // namespace pt
 
+// ================================================================ adjoint: subharmonics
+// The subharmonic sum of a frame is Re sum_pij C_pij (b_pi(x) b_pj(y) - mean)
+// with b_pi(x) = exp(2 pi i f_pi (x - ns/2) dx) (the grid's basis rows). Its
+// adjoint needs, per frame f of an upstream gradient g (F, n_out, n_out) on the
+// crop window, the projections
+//   out[f][((p*3 + i)*3 + j)*2 + {re, im}] = sum_{x,y} g_f(x, y) b_pi(crop + x) b_pj(crop + y)
+//   out[f][18 P] = sum_{x,y} g_f(x, y)
+// One CTA per frame; thread t owns columns y = t, t + 256, ...; one pass over
+// g per level; float sums along x, double products and a fixed-order reduce.
+__global__ void __launch_bounds__(256)
+k_adj_sh(int ns, int P, int crop, int n_out, const float2* __restrict__ basis,
+         const float* __restrict__ g, double* __restrict__ out) {
+  __shared__ double red[8][19];
+  const int f = blockIdx.x;
+  const float* gf = g + (size_t)f * n_out * n_out;
+  const size_t stride = (size_t)18 * P + 1;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int p = 0; p < P; ++p) {
+    const float2* b0 = basis + (size_t)p * 3 * ns + crop;
+    double acc[19];
+#pragma unroll
+    for (int q = 0; q < 19; ++q) acc[q] = 0.0;
+    for (int y = threadIdx.x; y < n_out; y += blockDim.x) {
+      float2 u[3] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+      float sum = 0.f;
+      for (int x = 0; x < n_out; ++x) {
+        const float v = gf[(size_t)x * n_out + y];
+        sum += v;
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+          const float2 b = __ldg(b0 + (size_t)i * ns + x);
+          u[i].x = fmaf(b.x, v, u[i].x);
+          u[i].y = fmaf(b.y, v, u[i].y);
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        const float2 b = __ldg(b0 + (size_t)j * ns + y);
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+          acc[(i * 3 + j) * 2] += (double)u[i].x * b.x - (double)u[i].y * b.y;
+          acc[(i * 3 + j) * 2 + 1] += (double)u[i].x * b.y + (double)u[i].y * b.x;
+        }
+      }
+      acc[18] += sum;
+    }
+#pragma unroll
+    for (int q = 0; q < 19; ++q) {
+      double v = acc[q];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      if (lane == 0) red[warp][q] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < 19) {
+      const int q = threadIdx.x;
+      double v = 0.0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) v += red[w][q];
+      if (q < 18) out[f * stride + (size_t)p * 18 + q] = v;
+      else if (p == 0) out[f * stride + (size_t)18 * P] = v;
+    }
+    __syncthreads();
+  }
+}
+
+extern "C" int pt_synth_adj_sh(const pt_grid* g, int F, int crop, int n_out, const float* grad,
+                               double* out, void* stream) {
+  if (int rc = check_grid(g, "pt_synth_adj_sh")) return rc;
+  if (g->P < 1) return fail(PT_ERR_ARG, "pt_synth_adj_sh: the grid has no subharmonic levels");
+  if (F < 1 || n_out < 1 || crop < 0 || crop + n_out > g->ns)
+    return fail(PT_ERR_ARG, "pt_synth_adj_sh: crop window outside the grid");
+  if (!grad || !out) return fail(PT_ERR_ARG, "pt_synth_adj_sh: NULL pointer");
+  cudaStream_t s = (cudaStream_t)stream;
+  ProfScope ps("k_adj_sh", s);
+  k_adj_sh<<<F, 256, 0, s>>>(g->ns, g->P, crop, n_out, g->basis, grad, out);
+  count_launch();
+  return check_launch("pt_synth_adj_sh");
+}
+
 extern "C" int pt_layers_translate(const pt_grid* g, int L, const float* spectra_in,
                                    const float* sh_in, const double* sx, const double* sy,
                                    float* spectra_out, float* sh_out, void* stream) {

@@ -73,10 +73,10 @@ __device__ __forceinline__ void split_pair(float2 zk, float2 zn, float2& ga, flo
   gb = make_float2(0.5f * d.y, -0.5f * d.x);         // d / 2i
 }
 
-// grad_S[l][k] = w_l sum_f G_f(k) conj(Phi_lf(k)).
+// grad_S[l][k] (+)= w_l sum_f G_f(k) conj(Phi_lf(k)).
 __global__ void k_adj_spectra(int ns, int L, int F, const float* __restrict__ w,
                               const float2* __restrict__ Z, const float2* __restrict__ ph,
-                              float2* __restrict__ gs) {
+                              int accumulate, float2* __restrict__ gs) {
   const size_t npix = (size_t)ns * ns;
   const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int l = blockIdx.y;
@@ -97,7 +97,12 @@ __global__ void k_adj_spectra(int ns, int L, int F, const float* __restrict__ w,
       acc = cfma(h == 0 ? ga : gb, cconj(phi), acc);
     }
   }
-  gs[(size_t)l * npix + k] = cscale(acc, w[l]);
+  float2 v = cscale(acc, w[l]);
+  if (accumulate) {
+    const float2 o = gs[(size_t)l * npix + k];
+    v = make_float2(o.x + v.x, o.y + v.y);
+  }
+  gs[(size_t)l * npix + k] = v;
 }
 
 // Per (layer, frame pair): [sum Re q, -2 pi w sum fx Im q, -2 pi w sum fy Im q]
@@ -188,7 +193,8 @@ extern "C" int pt_synth_adj_phasors(int ns, double pixel_scale, int L, int F, co
 }
 
 extern "C" int pt_synth_adj_spectra(int ns, int L, int F, const float* w, const float* Z,
-                                    const float* ph, float* grad_spectra, void* stream) {
+                                    const float* ph, int accumulate, float* grad_spectra,
+                                    void* stream) {
   if (ns < 2 || L < 1 || F < 1) return fail(PT_ERR_ARG, "pt_synth_adj_spectra: bad sizes");
   if (!w || !Z || !ph || !grad_spectra) return fail(PT_ERR_ARG, "pt_synth_adj_spectra: NULL pointer");
   if (L > 65535) return fail(PT_ERR_UNSUPPORTED, "pt_synth_adj_spectra: too many layers");
@@ -196,7 +202,7 @@ extern "C" int pt_synth_adj_spectra(int ns, int L, int F, const float* w, const 
   const size_t npix = (size_t)ns * ns;
   ProfScope ps("k_adj_spectra", s);
   k_adj_spectra<<<dim3((unsigned)((npix + 255) / 256), L), 256, 0, s>>>(
-      ns, L, F, w, (const float2*)Z, (const float2*)ph, (float2*)grad_spectra);
+      ns, L, F, w, (const float2*)Z, (const float2*)ph, accumulate, (float2*)grad_spectra);
   count_launch_a();
   return check_launch("pt_synth_adj_spectra");
 }

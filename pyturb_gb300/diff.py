@@ -15,6 +15,12 @@ The reference has no gradients; the adjoints here are hand-written kernels
 deterministic tile gather; ``pt_lr_grad_params``: block reductions for the
 weights and positions) behind :class:`torch.autograd.Function`. Torch carries
 the chain rule from positions to winds (a few hundred float64 scalars).
+
+Checkpointed losses (:func:`readout_mse`, :meth:`DifferentiableSpectralFrames.mse`)
+never hold the whole frame sequence: the forward keeps only the loss, and the
+backward recomputes the frames from the layer state (screens, or spectra =
+amplitude x noise) ``frames_per_chunk`` at a time, so memory is one chunk of
+frames instead of the sequence and its gradient.
 """
 
 from __future__ import annotations
@@ -85,7 +91,7 @@ class _LayerReadoutFn:
                 if ctx.needs_input_grad[0]:
                     gs = torch.empty_like(screens)
                     _lib.call("pt_lr_grad_screens", B, L, S, T, D, n, _lib.as_dptr(magc),
-                              _ptr(weights), _ptr(fix), _ptr(g), _ptr(gs), s)
+                              _ptr(weights), _ptr(fix), _ptr(g), 0, _ptr(gs), s)
                 if ctx.needs_input_grad[1] or ctx.needs_input_grad[2]:
                     cnt = int(_lib.load().pt_lr_partial_count(B, L, T, D, n))
                     part = torch.empty(cnt, dtype=torch.float32, device=dev)
@@ -108,6 +114,106 @@ def layer_readout(screens, weights, pos0, mag, n: int):
     ``weights (L,)`` float32, ``pos0 (T, D, L, 2)`` float64 (device) and the
     host magnification table ``mag (D, L)``; differentiable in the first three."""
     return _LayerReadoutFn.get().apply(screens, weights, pos0, np.asarray(mag, np.float64), int(n))
+
+
+def _lr_chunk(screens, weights, pos0c, magc, n):
+    """Frames (B, Tc, D, n, n) of one time chunk and its fixed-point table."""
+    import torch
+
+    B, L, S, _ = screens.shape
+    Tc, D = pos0c.shape[0], pos0c.shape[1]
+    s = stream_handle()
+    fix = torch.empty(3 * Tc * D * L, dtype=torch.int64, device=screens.device)
+    _lib.call("pt_lr_fix", Tc, D, L, S, n, _ptr(pos0c), _lib.as_dptr(magc), _ptr(fix), s)
+    out = torch.empty((B, Tc, D, n, n), dtype=torch.float32, device=screens.device)
+    _lib.call("pt_lr_forward", B, L, S, Tc, D, n, _lib.as_dptr(magc), _ptr(screens),
+              _ptr(weights), _ptr(fix), _ptr(out), s)
+    return out, fix
+
+
+class _ReadoutMSEFn:
+    """Holder for the checkpointed readout loss (built lazily)."""
+
+    fn = None
+
+    @classmethod
+    def get(cls):
+        if cls.fn is not None:
+            return cls.fn
+        import torch
+
+        class ReadoutMSE(torch.autograd.Function):
+            @staticmethod
+            def forward(ctx, screens, weights, pos0, target, mag, n, chunk):
+                B, L, S, S2 = screens.shape
+                T, D = pos0.shape[0], pos0.shape[1]
+                if S2 != S or tuple(pos0.shape) != (T, D, L, 2) or mag.shape != (D, L):
+                    raise ValueError("readout_mse: inconsistent shapes")
+                if tuple(target.shape) != (B, T, D, n, n) or target.dtype != torch.float32:
+                    raise ValueError("readout_mse: target must be float32 (B, T, D, n, n)")
+                if screens.dtype != torch.float32 or weights.dtype != torch.float32:
+                    raise ValueError("readout_mse: screens and weights must be float32")
+                if pos0.dtype != torch.float64:
+                    raise ValueError("readout_mse: pos0 must be float64")
+                screens, weights, pos0 = screens.contiguous(), weights.contiguous(), pos0.contiguous()
+                magc = np.ascontiguousarray(mag, dtype=np.float64)
+                total = torch.zeros((), dtype=torch.float64, device=screens.device)
+                for t0 in range(0, T, chunk):
+                    t1 = min(T, t0 + chunk)
+                    out, _ = _lr_chunk(screens, weights, pos0[t0:t1], magc, n)
+                    total += (out - target[:, t0:t1]).double().square().sum()
+                ctx.save_for_backward(screens, weights, pos0, target)
+                ctx.mag, ctx.n, ctx.chunk = magc, n, chunk
+                return (total / target.numel()).float()
+
+            @staticmethod
+            def backward(ctx, gl):
+                screens, weights, pos0, target = ctx.saved_tensors
+                magc, n, chunk = ctx.mag, ctx.n, ctx.chunk
+                B, L, S, _ = screens.shape
+                T, D = pos0.shape[0], pos0.shape[1]
+                s = stream_handle()
+                dev = screens.device
+                need_s = ctx.needs_input_grad[0]
+                need_p = ctx.needs_input_grad[1] or ctx.needs_input_grad[2]
+                gs = torch.empty_like(screens) if need_s else None
+                gw = torch.zeros(L, dtype=torch.float64, device=dev)
+                gp = torch.zeros((T, D, L, 2), dtype=torch.float64, device=dev)
+                k = 2.0 / target.numel()
+                nb = (n + 63) // 64
+                for t0 in range(0, T, chunk):
+                    t1 = min(T, t0 + chunk)
+                    Tc = t1 - t0
+                    out, fix = _lr_chunk(screens, weights, pos0[t0:t1], magc, n)
+                    g = ((out - target[:, t0:t1]) * (gl.float() * k)).contiguous()
+                    del out
+                    if need_s:
+                        _lib.call("pt_lr_grad_screens", B, L, S, Tc, D, n, _lib.as_dptr(magc),
+                                  _ptr(weights), _ptr(fix), _ptr(g), int(t0 > 0), _ptr(gs), s)
+                    if need_p:
+                        cnt = int(_lib.load().pt_lr_partial_count(B, L, Tc, D, n))
+                        part = torch.empty(cnt, dtype=torch.float32, device=dev)
+                        _lib.call("pt_lr_grad_params", B, L, S, Tc, D, n, _lib.as_dptr(magc),
+                                  _ptr(screens), _ptr(weights), _ptr(fix), _ptr(g), _ptr(part), s)
+                        pv = part.view(B, Tc * D, nb, L, 3).double()
+                        gw += pv[..., 0].sum(dim=(0, 1, 2))
+                        gp[t0:t1] = pv[..., 1:].sum(dim=(0, 2)).reshape(Tc, D, L, 2)
+                return (gs, gw.float() if ctx.needs_input_grad[1] else None,
+                        gp if ctx.needs_input_grad[2] else None, None, None, None, None)
+
+        cls.fn = ReadoutMSE
+        return cls.fn
+
+
+def readout_mse(screens, weights, pos0, target, mag, n: int, frames_per_chunk: int = 8):
+    """``mean((layer_readout(screens, weights, pos0, mag, n) - target)^2)`` without
+    holding the frames: the forward keeps the loss only and the backward
+    recomputes ``frames_per_chunk`` time steps at a time (the screens stay the
+    checkpoint). Differentiable in ``screens``, ``weights`` and ``pos0``."""
+    if int(frames_per_chunk) < 1:
+        raise ValueError("frames_per_chunk must be >= 1")
+    return _ReadoutMSEFn.get().apply(screens, weights, pos0, target,
+                                     np.asarray(mag, np.float64), int(n), int(frames_per_chunk))
 
 
 class DifferentiableReadout:
@@ -170,6 +276,12 @@ class DifferentiableReadout:
         """``out (B, T, D, n, n)`` float32 OPD in the screens' units."""
         return layer_readout(screens, weights, self.positions(winds), self.mag, self.n)
 
+    def mse(self, screens, weights, winds, target, frames_per_chunk: int = 8):
+        """``mean((self(screens, weights, winds) - target)^2)``, checkpointed
+        (see :func:`readout_mse`)."""
+        return readout_mse(screens, weights, self.positions(winds), target, self.mag, self.n,
+                           frames_per_chunk)
+
 
 def fit_layers(readout: DifferentiableReadout, screens, target, weights0, winds0,
                steps: int = 100, lr: float = 0.01):
@@ -193,10 +305,140 @@ def fit_layers(readout: DifferentiableReadout, screens, target, weights0, winds0
 # ------------------------------------------------------------- spectral synthesis
 
 
+def _synth_frames(grid, sw, shc, sx, sy, crop, n_out, scale):
+    """Frames (F, n_out, n_out) from weighted spectra ``sw`` (L, ns, ns, 2) and
+    weighted subharmonic coefficients ``shc`` (P, L, 3, 3, 2) or None."""
+    import torch
+
+    F, L = sx.shape
+    out = torch.empty((F, n_out, n_out), dtype=torch.float32, device=sw.device)
+    _lib.call("pt_frames", grid.handle, L, _ptr(sw), _ptr(shc) if shc is not None else None, F,
+              _lib.as_dptr(sx), _lib.as_dptr(sy), 0, int(crop), int(n_out), float(scale),
+              _ptr(out), _ptr(grid.work), grid.work_bytes, stream_handle())
+    return out
+
+
+def _sh_beta(grid):
+    """Grid means of the subharmonic basis rows, (P, 3) complex128 (host)."""
+    x = (np.arange(grid.ns) - grid.ns / 2.0) * grid.dx
+    return np.exp(2j * np.pi * grid._freq[:, :, None] * x[None, None, :]).mean(axis=-1)
+
+
+class _SynthAdjoint:
+    """Accumulates the synthesis VJP over chunks of frames (pt_synth_adj_*):
+    spectra, weights, shifts and, with subharmonic levels, the level
+    coefficients."""
+
+    def __init__(self, grid, spectra, weights, sh_coef, shifts, crop, n_out, scale, need):
+        import torch
+
+        self.torch = torch
+        self.grid, self.crop, self.n_out, self.scale = grid, crop, n_out, scale
+        self.L, self.ns = spectra.shape[0], spectra.shape[1]
+        self.F = shifts.shape[0]
+        self.dev = spectra.device
+        self.need_S, self.need_p, self.need_c = need
+        self.w = weights.contiguous()
+        self.sr = torch.view_as_real(spectra.contiguous()).contiguous() if self.need_p else None
+        self.shifts = shifts
+        self.gSr = (torch.empty((self.L, self.ns, self.ns, 2), dtype=torch.float32,
+                                device=self.dev) if self.need_S else None)
+        self.gw = torch.zeros(self.L, dtype=torch.float64, device=self.dev)
+        self.gsh = torch.zeros((self.F, self.L, 2), dtype=torch.float64, device=self.dev)
+        self.sh = sh_coef
+        if sh_coef is not None:
+            self.fp = torch.as_tensor(grid._freq, dtype=torch.float64, device=self.dev)
+            beta = torch.as_tensor(_sh_beta(grid), device=self.dev)
+            self.bb = beta[:, :, None] * beta[:, None, :]                       # (P, 3, 3)
+            self.cl = sh_coef.detach().to(torch.complex128).permute(1, 0, 2, 3)  # (L, P, 3, 3)
+            self.gc = torch.zeros_like(self.cl)
+        self.first = True
+
+    def add(self, f0, g):
+        """The VJP of frames [f0, f0 + len(g)) for upstream ``g`` (Fc, n_out, n_out)."""
+        torch = self.torch
+        grid, ns, L = self.grid, self.ns, self.L
+        Fc = g.shape[0]
+        s = stream_handle()
+        g = g.contiguous()
+        P2 = (Fc + 1) // 2
+        z = torch.empty((P2, ns, ns, 2), dtype=torch.float32, device=self.dev)
+        _lib.call("pt_synth_adj_pack", ns, Fc, self.crop, self.n_out, self.scale, _ptr(g), _ptr(z),
+                  s)
+        _lib.call("pt_ifft2", grid.handle, _ptr(z), _ptr(z), P2, _ptr(grid.work), grid.work_bytes, s)
+        sh = self.shifts[f0:f0 + Fc]
+        sx, sy = sh[..., 0].contiguous(), sh[..., 1].contiguous()
+        ph = torch.empty((L, Fc, 2, ns, 2), dtype=torch.float32, device=self.dev)
+        _lib.call("pt_synth_adj_phasors", ns, grid.dx, L, Fc, _ptr(sx), _ptr(sy), _ptr(ph), s)
+        if self.need_S:
+            _lib.call("pt_synth_adj_spectra", ns, L, Fc, _ptr(self.w), _ptr(z), _ptr(ph),
+                      int(not self.first), _ptr(self.gSr), s)
+        if self.need_p:
+            part = torch.empty((L, Fc, 3), dtype=torch.float64, device=self.dev)
+            _lib.call("pt_synth_adj_params", ns, grid.dx, L, Fc, _ptr(self.w), _ptr(self.sr),
+                      _ptr(z), _ptr(ph), _ptr(part), s)
+            self.gw += part[..., 0].sum(dim=1)
+            self.gsh[f0:f0 + Fc] += part[..., 1:].transpose(0, 1)
+        if self.sh is not None and (self.need_p or self.need_c):
+            P = grid.P
+            proj = torch.empty((Fc, 18 * P + 1), dtype=torch.float64, device=self.dev)
+            _lib.call("pt_synth_adj_sh", grid.handle, Fc, self.crop, self.n_out, _ptr(g),
+                      _ptr(proj), s)
+            G = torch.complex(proj[:, 0:18 * P:2], proj[:, 1:18 * P:2]).reshape(Fc, P, 3, 3)
+            Q = self.scale * (G - self.bb[None] * proj[:, 18 * P, None, None, None])
+            ex = torch.exp(2j * np.pi * sx.double()[:, :, None, None] * self.fp[None, None])
+            ey = torch.exp(2j * np.pi * sy.double()[:, :, None, None] * self.fp[None, None])
+            E = ex[..., :, None] * ey[..., None, :]                             # (Fc, L, P, 3, 3)
+            EQ = E * Q[:, None]
+            if self.need_p:
+                M = self.cl[None] * EQ
+                self.gw += M.real.sum(dim=(0, 2, 3, 4))
+                wMi = (self.w.double()[None, :, None, None, None] * M).imag
+                self.gsh[f0:f0 + Fc, :, 0] -= 2 * np.pi * torch.einsum("pi,flpij->fl", self.fp, wMi)
+                self.gsh[f0:f0 + Fc, :, 1] -= 2 * np.pi * torch.einsum("pj,flpij->fl", self.fp, wMi)
+            if self.need_c:
+                self.gc += torch.conj(self.w.double()[:, None, None, None] * EQ.sum(dim=0))
+        self.first = False
+
+    def grads(self):
+        torch = self.torch
+        gS = torch.view_as_complex(self.gSr) if self.need_S else None
+        gc = (self.gc.permute(1, 0, 2, 3).to(torch.complex64).contiguous()
+              if self.sh is not None and self.need_c else None)
+        return gS, self.gw.float(), self.gsh, gc
+
+
+def _synth_inputs(spectra, weights, sh_coef, shifts, grid, who):
+    import torch
+
+    L, ns, ns2 = spectra.shape
+    F = shifts.shape[0]
+    if ns2 != ns or ns != grid.ns:
+        raise ValueError(f"{who}: spectra must be (L, ns, ns) on the grid")
+    if tuple(shifts.shape) != (F, L, 2) or shifts.dtype != torch.float64:
+        raise ValueError(f"{who}: shifts must be float64 (F, L, 2)")
+    if spectra.dtype != torch.complex64 or weights.dtype != torch.float32:
+        raise ValueError(f"{who}: complex64 spectra, float32 weights")
+    if (sh_coef is None) != (grid.P == 0):
+        raise ValueError(f"{who}: sh_coef (P, L, 3, 3) must be given exactly when the grid "
+                         "has subharmonic levels")
+    if sh_coef is not None and (tuple(sh_coef.shape) != (grid.P, L, 3, 3)
+                                or sh_coef.dtype != torch.complex64):
+        raise ValueError(f"{who}: sh_coef must be complex64 (P, L, 3, 3)")
+    grid.ensure_workspace(L)
+    wc = weights.to(torch.complex64)
+    sw = torch.view_as_real(spectra * wc[:, None, None]).contiguous()
+    shc = (torch.view_as_real(sh_coef * wc[None, :, None, None]).contiguous()
+           if sh_coef is not None else None)
+    sh = shifts.detach().cpu().numpy()
+    return sw, shc, np.ascontiguousarray(sh[..., 0]), np.ascontiguousarray(sh[..., 1])
+
+
 class _SynthFn:
-    """Holder for the spectral-synthesis autograd Function (built lazily)."""
+    """Holder for the spectral-synthesis autograd Functions (built lazily)."""
 
     fn = None
+    mse = None
 
     @classmethod
     def get(cls):
@@ -206,79 +448,107 @@ class _SynthFn:
 
         class SpectralSynthesis(torch.autograd.Function):
             @staticmethod
-            def forward(ctx, spectra, weights, shifts, grid, crop, n_out, scale):
-                L, ns, ns2 = spectra.shape
-                F = shifts.shape[0]
-                if ns2 != ns or ns != grid.ns or grid.P != 0:
-                    raise ValueError("spectral_synthesis: spectra must be (L, ns, ns) on a grid "
-                                     "without subharmonics")
-                if tuple(shifts.shape) != (F, L, 2) or shifts.dtype != torch.float64:
-                    raise ValueError("spectral_synthesis: shifts must be float64 (F, L, 2)")
-                if spectra.dtype != torch.complex64 or weights.dtype != torch.float32:
-                    raise ValueError("spectral_synthesis: complex64 spectra, float32 weights")
-                s = stream_handle()
-                grid.ensure_workspace(L)
-                sw = torch.view_as_real(spectra * weights.to(torch.complex64)[:, None, None])
-                sw = sw.contiguous()
-                sh = shifts.detach().cpu().numpy()
-                sx = np.ascontiguousarray(sh[..., 0])
-                sy = np.ascontiguousarray(sh[..., 1])
-                out = torch.empty((F, n_out, n_out), dtype=torch.float32, device=spectra.device)
-                _lib.call("pt_frames", grid.handle, L, _ptr(sw), None, F, _lib.as_dptr(sx),
-                          _lib.as_dptr(sy), 0, int(crop), int(n_out), float(scale), _ptr(out),
-                          _ptr(grid.work), grid.work_bytes, s)
-                ctx.save_for_backward(spectra, weights, shifts)
+            def forward(ctx, spectra, weights, shifts, sh_coef, grid, crop, n_out, scale, chunk):
+                sw, shc, sx, sy = _synth_inputs(spectra, weights, sh_coef, shifts, grid,
+                                                "spectral_synthesis")
+                out = _synth_frames(grid, sw, shc, sx, sy, crop, n_out, scale)
+                ctx.save_for_backward(spectra, weights, shifts,
+                                      sh_coef if sh_coef is not None else torch.empty(0))
+                ctx.has_sh = sh_coef is not None
                 ctx.grid, ctx.crop, ctx.n_out, ctx.scale = grid, int(crop), int(n_out), float(scale)
+                ctx.chunk = chunk
                 return out
 
             @staticmethod
             def backward(ctx, g):
-                spectra, weights, shifts = ctx.saved_tensors
-                grid = ctx.grid
-                L, ns, _ = spectra.shape
+                spectra, weights, shifts, shc = ctx.saved_tensors
+                need = (ctx.needs_input_grad[0],
+                        ctx.needs_input_grad[1] or ctx.needs_input_grad[2],
+                        ctx.has_sh and ctx.needs_input_grad[3])
+                adj = _SynthAdjoint(ctx.grid, spectra, weights, shc if ctx.has_sh else None,
+                                    shifts, ctx.crop, ctx.n_out, ctx.scale, need)
                 F = shifts.shape[0]
-                dev = g.device
-                s = stream_handle()
-                g = g.contiguous()
-                P2 = (F + 1) // 2
-                z = torch.empty((P2, ns, ns, 2), dtype=torch.float32, device=dev)
-                _lib.call("pt_synth_adj_pack", ns, F, ctx.crop, ctx.n_out, ctx.scale, _ptr(g),
-                          _ptr(z), s)
-                _lib.call("pt_ifft2", grid.handle, _ptr(z), _ptr(z), P2, _ptr(grid.work),
-                          grid.work_bytes, s)
-                sx = shifts[..., 0].contiguous()
-                sy = shifts[..., 1].contiguous()
-                ph = torch.empty((L, F, 2, ns, 2), dtype=torch.float32, device=dev)
-                _lib.call("pt_synth_adj_phasors", ns, grid.dx, L, F, _ptr(sx), _ptr(sy), _ptr(ph), s)
-                w = weights.contiguous()
-                gS = gw = gsh = None
-                if ctx.needs_input_grad[0]:
-                    gSr = torch.empty((L, ns, ns, 2), dtype=torch.float32, device=dev)
-                    _lib.call("pt_synth_adj_spectra", ns, L, F, _ptr(w), _ptr(z), _ptr(ph),
-                              _ptr(gSr), s)
-                    gS = torch.view_as_complex(gSr)
-                if ctx.needs_input_grad[1] or ctx.needs_input_grad[2]:
-                    sr = torch.view_as_real(spectra.contiguous()).contiguous()
-                    part = torch.empty((L, F, 3), dtype=torch.float64, device=dev)
-                    _lib.call("pt_synth_adj_params", ns, grid.dx, L, F, _ptr(w), _ptr(sr), _ptr(z),
-                              _ptr(ph), _ptr(part), s)
-                    if ctx.needs_input_grad[1]:
-                        gw = part[..., 0].sum(dim=1).float()
-                    if ctx.needs_input_grad[2]:
-                        gsh = part[..., 1:].transpose(0, 1).contiguous()
-                return gS, gw, gsh, None, None, None, None
+                for f0 in range(0, F, ctx.chunk):
+                    adj.add(f0, g[f0:f0 + ctx.chunk])
+                gS, gw, gsh, gc = adj.grads()
+                return (gS, gw if ctx.needs_input_grad[1] else None,
+                        gsh if ctx.needs_input_grad[2] else None, gc,
+                        None, None, None, None, None)
+
+        class SynthesisMSE(torch.autograd.Function):
+            @staticmethod
+            def forward(ctx, spectra, weights, shifts, sh_coef, target, grid, crop, n_out, scale,
+                        chunk):
+                F = shifts.shape[0]
+                if tuple(target.shape) != (F, n_out, n_out) or target.dtype != torch.float32:
+                    raise ValueError("synthesis_mse: target must be float32 (F, n_out, n_out)")
+                sw, shc, sx, sy = _synth_inputs(spectra, weights, sh_coef, shifts, grid,
+                                                "synthesis_mse")
+                total = torch.zeros((), dtype=torch.float64, device=spectra.device)
+                for f0 in range(0, F, chunk):
+                    f1 = min(F, f0 + chunk)
+                    out = _synth_frames(grid, sw, shc, sx[f0:f1], sy[f0:f1], crop, n_out, scale)
+                    total += (out - target[f0:f1]).double().square().sum()
+                ctx.save_for_backward(spectra, weights, shifts,
+                                      sh_coef if sh_coef is not None else torch.empty(0), target)
+                ctx.has_sh = sh_coef is not None
+                ctx.grid, ctx.crop, ctx.n_out, ctx.scale = grid, int(crop), int(n_out), float(scale)
+                ctx.chunk = chunk
+                return (total / target.numel()).float()
+
+            @staticmethod
+            def backward(ctx, gl):
+                spectra, weights, shifts, shc, target = ctx.saved_tensors
+                grid, chunk = ctx.grid, ctx.chunk
+                need = (ctx.needs_input_grad[0],
+                        ctx.needs_input_grad[1] or ctx.needs_input_grad[2],
+                        ctx.has_sh and ctx.needs_input_grad[3])
+                sh_coef = shc if ctx.has_sh else None
+                adj = _SynthAdjoint(grid, spectra, weights, sh_coef, shifts, ctx.crop, ctx.n_out,
+                                    ctx.scale, need)
+                sw, shw, sx, sy = _synth_inputs(spectra, weights, sh_coef, shifts, grid,
+                                                "synthesis_mse")
+                k = gl.float() * (2.0 / target.numel())
+                F = shifts.shape[0]
+                for f0 in range(0, F, chunk):   # recompute each chunk of frames
+                    f1 = min(F, f0 + chunk)
+                    out = _synth_frames(grid, sw, shw, sx[f0:f1], sy[f0:f1], ctx.crop, ctx.n_out,
+                                        ctx.scale)
+                    adj.add(f0, (out - target[f0:f1]) * k)
+                gS, gw, gsh, gc = adj.grads()
+                return (gS, gw if ctx.needs_input_grad[1] else None,
+                        gsh if ctx.needs_input_grad[2] else None, gc,
+                        None, None, None, None, None, None)
 
         cls.fn = SpectralSynthesis
+        cls.mse = SynthesisMSE
         return cls.fn
 
 
-def spectral_synthesis(spectra, weights, shifts, grid, crop: int, n_out: int, scale: float = 1.0):
-    """``(F, n_out, n_out)`` frames ``scale * crop(Re IDFT(sum_l w_l S_l Phi_fl))`` (no
-    subharmonics), differentiable in ``spectra (L, ns, ns)`` complex64, ``weights (L,)``
-    and ``shifts (F, L, 2)`` float64 [m] (x along axis 0). ``grid`` is a
-    :class:`pyturb_gb300.fourier.Grid` built with no subharmonic levels."""
-    return _SynthFn.get().apply(spectra, weights, shifts, grid, int(crop), int(n_out),
-                                float(scale))
+def spectral_synthesis(spectra, weights, shifts, grid, crop: int, n_out: int, scale: float = 1.0,
+                       sh_coef=None, frames_per_chunk: int = 64):
+    """``(F, n_out, n_out)`` frames ``scale * crop(Re IDFT(sum_l w_l S_l Phi_fl) + low_f)``,
+    differentiable in ``spectra (L, ns, ns)`` complex64, ``weights (L,)``,
+    ``shifts (F, L, 2)`` float64 [m] (x along axis 0) and, on a grid with
+    subharmonic levels, ``sh_coef (P, L, 3, 3)`` complex64 (``low_f`` the
+    zero-mean low-order sum of the reference, ``atmosphere.py:921-935``). The
+    backward runs ``frames_per_chunk`` frames at a time."""
+    if int(frames_per_chunk) < 1:
+        raise ValueError("frames_per_chunk must be >= 1")
+    return _SynthFn.get().apply(spectra, weights, shifts, sh_coef, grid, int(crop), int(n_out),
+                                float(scale), int(frames_per_chunk))
+
+
+def synthesis_mse(spectra, weights, shifts, target, grid, crop: int, n_out: int,
+                  scale: float = 1.0, sh_coef=None, frames_per_chunk: int = 16):
+    """``mean((spectral_synthesis(...) - target)^2)`` without holding the frames:
+    the forward keeps the loss only, and the backward recomputes the frames
+    from the spectra ``frames_per_chunk`` at a time."""
+    if int(frames_per_chunk) < 1:
+        raise ValueError("frames_per_chunk must be >= 1")
+    _SynthFn.get()
+    return _SynthFn.mse.apply(spectra, weights, shifts, sh_coef, target, grid, int(crop),
+                              int(n_out), float(scale), int(frames_per_chunk))
 
 
 class DifferentiableSpectralFrames:
@@ -287,24 +557,28 @@ class DifferentiableSpectralFrames:
 
     The layers share one ``n_screen`` grid at ``pixel_scale`` and the von
     Karman amplitude of ``r0`` / ``L0`` (``fourier.py:174-228`` of the
-    reference, without subharmonic levels); layer ``l``'s spectrum is
-    ``amplitude * noise[l]`` with ``noise`` complex N(0, 1). Frame ``(t, d)``
-    displaces layer ``l`` by ``v_l t + alt_l theta_d`` (``atmosphere.py:
-    1012-1015``) and is cropped to the central ``n x n`` pupil.
+    reference); layer ``l``'s spectrum is ``amplitude * noise[l]`` with
+    ``noise`` complex N(0, 1), and with ``subharmonics = P`` levels its
+    low-order coefficients are ``sh_amp * sh_noise[l]`` (``sh_noise (L, P, 3,
+    3)`` complex). Frame ``(t, d)`` displaces layer ``l`` by ``v_l t + alt_l
+    theta_d`` (``atmosphere.py:1012-1015``) and is cropped to the central
+    ``n x n`` pupil.
     """
 
     def __init__(self, n: int, n_screen: int, pixel_scale: float, r0: float, L0: float,
                  altitudes: Sequence[float], times, directions=None, scale: float = 1.0,
-                 device: str = "gpu") -> None:
+                 subharmonics: int = 0, device: str = "gpu") -> None:
         import torch
 
-        from .fourier import Grid, amplitude_table
+        from .fourier import Grid, amplitude_table, subharmonic_tables
 
         check_device(device)
         self.device = cuda_device()
         self.n, self.n_screen = int(n), int(n_screen)
         if not 1 <= self.n <= self.n_screen:
             raise ValueError("need 1 <= n <= n_screen")
+        if not 0 <= int(subharmonics) <= 16:
+            raise ValueError("subharmonics must be in [0, 16]")
         self.pixel_scale = float(pixel_scale)
         self.altitudes = np.asarray(altitudes, np.float64).reshape(-1)
         self.times = np.asarray(times, np.float64).reshape(-1)
@@ -312,9 +586,15 @@ class DifferentiableSpectralFrames:
         self.directions = dirs.reshape(-1, 2)
         self.scale = float(scale)
         self.crop = (self.n_screen - self.n) // 2
-        self.grid = Grid(self.n_screen, self.pixel_scale, np.zeros((0, 3)), n_layers=1)
+        self.P = int(subharmonics)
+        freqs, sh_amp = subharmonic_tables(self.n_screen, self.pixel_scale, r0, L0, self.P)
+        self.grid = Grid(self.n_screen, self.pixel_scale, freqs if self.P else np.zeros((0, 3)),
+                         n_layers=1)
         amp = amplitude_table(self.n_screen, self.pixel_scale, r0, L0)
         self.amplitude = torch.as_tensor(amp, dtype=torch.float32, device=self.device)
+        self.sh_amp = (torch.as_tensor(np.asarray(sh_amp).reshape(self.P, 3, 3),
+                                       dtype=torch.float32, device=self.device)
+                       if self.P else None)
         dev = self.device
         self._t = torch.as_tensor(self.times, dtype=torch.float64, device=dev)
         self._alt_th = torch.as_tensor(
@@ -331,7 +611,26 @@ class DifferentiableSpectralFrames:
         """``amplitude * noise`` for complex ``noise (L, ns, ns)``."""
         return noise * self.amplitude.to(noise.dtype)[None]
 
-    def __call__(self, noise, weights, winds):
+    def sh_coef(self, sh_noise):
+        """``(P, L, 3, 3)`` level coefficients ``sh_amp * sh_noise`` for
+        ``sh_noise (L, P, 3, 3)`` complex, or None without levels."""
+        if not self.P:
+            if sh_noise is not None:
+                raise ValueError("sh_noise given, but the frames have no subharmonic levels")
+            return None
+        if sh_noise is None:
+            raise ValueError("sh_noise (L, P, 3, 3) is required with subharmonic levels")
+        return (sh_noise * self.sh_amp.to(sh_noise.dtype)[None]).permute(1, 0, 2, 3)
+
+    def __call__(self, noise, weights, winds, sh_noise=None):
         """``(T * D, n, n)`` frames, frame index ``t * D + d``."""
         return spectral_synthesis(self.spectra(noise), weights, self.shifts(winds), self.grid,
-                                  self.crop, self.n, self.scale)
+                                  self.crop, self.n, self.scale, self.sh_coef(sh_noise))
+
+    def mse(self, noise, weights, winds, target, sh_noise=None, frames_per_chunk: int = 16):
+        """``mean((self(noise, weights, winds, sh_noise) - target)^2)``, checkpointed:
+        the frames are recomputed from the noise in the backward
+        ``frames_per_chunk`` at a time (see :func:`synthesis_mse`)."""
+        return synthesis_mse(self.spectra(noise), weights, self.shifts(winds), target, self.grid,
+                             self.crop, self.n, self.scale, self.sh_coef(sh_noise),
+                             frames_per_chunk)

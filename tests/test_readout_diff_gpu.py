@@ -135,3 +135,38 @@ def test_physical_readout_and_adam_fit_recover_winds_and_weights():
     assert losses[-1] < 1e-3 * losses[0]
     np.testing.assert_allclose(w.cpu().numpy(), w_true.cpu().numpy(), rtol=0.02)
     np.testing.assert_allclose(v.cpu().numpy(), v_true.cpu().numpy(), atol=0.25)
+
+
+def test_checkpointed_readout_loss_matches_the_materialised_one():
+    """readout_mse (frames recomputed 3 time steps at a time) equals torch's MSE
+    of the materialised frames: value and the screen, weight and wind gradients."""
+    import torch
+
+    from pyturb_gb300.diff import DifferentiableReadout
+
+    rng = np.random.default_rng(13)
+    B, L, S, n, T = 2, 3, 96, 40, 7
+    dirs = [[0.0, 0.0], [2e-5, -1e-5]]
+    ro = DifferentiableReadout(n, S, 0.02, [0.0, 4000.0, 9000.0], dirs, np.arange(T) * 1e-3,
+                               source_altitudes=[None, 90e3])
+    dev = torch.device("cuda")
+    s0 = torch.tensor(rng.standard_normal((B, L, S, S)), dtype=torch.float32, device=dev)
+    w0 = torch.tensor([0.9, 0.6, 0.4], device=dev)
+    v0 = torch.tensor([[5.0, 1.0], [-8.0, 4.0], [12.0, -3.0]], dtype=torch.float64, device=dev)
+    with torch.no_grad():
+        target = ro(s0, w0 * 1.2, v0 + 1.0)
+    grads = []
+    for mode in ("materialised", "checkpointed"):
+        sc = s0.clone().requires_grad_(True)
+        w = w0.clone().requires_grad_(True)
+        v = v0.clone().requires_grad_(True)
+        if mode == "materialised":
+            loss = torch.nn.functional.mse_loss(ro(sc, w, v), target)
+        else:
+            loss = ro.mse(sc, w, v, target, frames_per_chunk=3)
+        loss.backward()
+        grads.append([loss.detach(), sc.grad, w.grad, v.grad])
+    for a, b in zip(*grads):
+        a, b = a.cpu().numpy().astype(np.float64), b.cpu().numpy().astype(np.float64)
+        assert np.linalg.norm(a - b) <= 1e-5 * np.linalg.norm(a)
+

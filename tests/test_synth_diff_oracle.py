@@ -76,3 +76,67 @@ def test_vjp_matches_torch_autograd():
     np.testing.assert_allclose(tw.grad.numpy(), gw, rtol=1e-10)
     np.testing.assert_allclose(tsx.grad.numpy(), gsx, rtol=1e-9, atol=1e-8)
     np.testing.assert_allclose(tsy.grad.numpy(), gsy, rtol=1e-9, atol=1e-8)
+
+
+def sh_case(seed=6, L=2, ns=18, F=3, P=2):
+    rng = np.random.default_rng(seed)
+    coef = rng.standard_normal((P, L, 3, 3)) + 1j * rng.standard_normal((P, L, 3, 3))
+    dx = 0.1
+    df = 1.0 / (ns * dx)
+    freqs = np.array([[-1.0, 0.0, 1.0]]) * df / 3.0 ** np.arange(1, P + 1)[:, None]
+    return coef, freqs
+
+
+def test_subharmonic_forward_follows_the_reference_layout():
+    # low = Re(basis^T (shifted @ basis)) - mean, shifted = sum_l c px py (atmosphere.py:921-935)
+    S, w, sx, sy, dx, crop, n_out, scale, g = case(seed=3)
+    coef, freqs = sh_case(L=S.shape[0], ns=S.shape[-1])
+    ns = S.shape[-1]
+    with_sh = sd.synth_frames(S, w, sx, sy, dx, crop, n_out, scale, sh=(coef, freqs))
+    without = sd.synth_frames(S, w, sx, sy, dx, crop, n_out, scale)
+    x = (np.arange(ns) - ns / 2.0) * dx
+    basis = np.exp(2j * np.pi * freqs[:, :, None] * x[None, None, :])
+    for f in range(sx.shape[0]):
+        px = np.exp(2j * np.pi * sx[f][None, :, None] * freqs[:, None, :])
+        py = np.exp(2j * np.pi * sy[f][None, :, None] * freqs[:, None, :])
+        shifted = ((coef * w[None, :, None, None]) * px[:, :, :, None] * py[:, :, None, :]).sum(1)
+        m = np.matmul(shifted, basis).reshape(-1, ns)
+        low = (basis.reshape(-1, ns).T @ m).real
+        low -= low.mean()
+        np.testing.assert_allclose(with_sh[f] - without[f],
+                                   scale * low[crop:crop + n_out, crop:crop + n_out],
+                                   rtol=1e-10, atol=1e-12)
+
+
+def test_subharmonic_vjp_matches_central_differences():
+    S, w, sx, sy, dx, crop, n_out, scale, g = case(seed=8, L=2, ns=18, n_out=13)
+    coef, freqs = sh_case(L=2)
+    sh = (coef, freqs)
+    gS, gw, gsx, gsy, gc = sd.synth_vjp(S, w, sx, sy, dx, crop, n_out, scale, g, sh=sh)
+
+    def val(w_=w, sx_=sx, sy_=sy, c_=coef):
+        return float(np.sum(sd.synth_frames(S, w_, sx_, sy_, dx, crop, n_out, scale,
+                                            sh=(c_, freqs)) * g))
+
+    eps = 1e-6
+    for l in range(w.size):
+        wp, wm = w.copy(), w.copy()
+        wp[l] += eps
+        wm[l] -= eps
+        assert (val(w_=wp) - val(w_=wm)) / (2 * eps) == pytest.approx(gw[l], rel=1e-6)
+    for idx in [(0, 0), (2, 1), (1, 0)]:
+        for name, arr, gref in (("x", sx, gsx), ("y", sy, gsy)):
+            ap, am = arr.copy(), arr.copy()
+            ap[idx] += eps
+            am[idx] -= eps
+            kw = "sx_" if name == "x" else "sy_"
+            fd = (val(**{kw: ap}) - val(**{kw: am})) / (2 * eps)
+            assert fd == pytest.approx(gref[idx], rel=1e-5, abs=1e-6)
+    for idx in [(0, 0, 0, 1), (1, 1, 2, 2), (0, 1, 1, 0)]:
+        for part, unit in (("re", 1.0), ("im", 1j)):
+            cp, cm = coef.copy(), coef.copy()
+            cp[idx] += eps * unit
+            cm[idx] -= eps * unit
+            fd = (val(c_=cp) - val(c_=cm)) / (2 * eps)
+            want = gc[idx].real if part == "re" else gc[idx].imag
+            assert fd == pytest.approx(want, rel=1e-6, abs=1e-7)
