@@ -284,9 +284,11 @@ class DifferentiableReadout:
 
 
 def fit_layers(readout: DifferentiableReadout, screens, target, weights0, winds0,
-               steps: int = 100, lr: float = 0.01):
+               steps: int = 100, lr: float = 0.01, frames_per_chunk: Optional[int] = None):
     """Adam fit of the per-layer weights and winds to a target OPD sequence
-    (mean-squared error). Returns ``(weights, winds, losses)``."""
+    (mean-squared error). With ``frames_per_chunk`` the loss is the
+    checkpointed :meth:`DifferentiableReadout.mse`. Returns ``(weights, winds,
+    losses)``."""
     import torch
 
     w = weights0.detach().clone().float().requires_grad_(True)
@@ -295,7 +297,10 @@ def fit_layers(readout: DifferentiableReadout, screens, target, weights0, winds0
     losses = []
     for _ in range(int(steps)):
         opt.zero_grad(set_to_none=True)
-        loss = torch.nn.functional.mse_loss(readout(screens, w, v), target)
+        if frames_per_chunk:
+            loss = readout.mse(screens, w, v, target, frames_per_chunk=int(frames_per_chunk))
+        else:
+            loss = torch.nn.functional.mse_loss(readout(screens, w, v), target)
         loss.backward()
         opt.step()
         losses.append(float(loss.detach()))
