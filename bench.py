@@ -401,6 +401,11 @@ def bench_extrude(torch, G, steps: int = 4096):
             ro_s = e0.elapsed_time(e1) / 1000.0 / reps
             res["readout_frames_per_s"] = 1.0 / ro_s
             res["readout_gbs_out"] = n * n * 4 / ro_s / 1e9
+            # one bilinear tap set (2 x 2 samples) per pixel and layer; the 9
+            # rings (W x cap floats each) stay L2-resident across frames, so
+            # DRAM sees little beyond the frame written
+            res["readout_pixel_layers_per_s"] = 9 * n * n / ro_s
+            res["readout_bytes_per_frame_algorithmic"] = n * n * 4 + 9 * n * n * 4
         out["configured" if columns == 2 else "rows_only"] = res
         del ext
     cfg = out["configured"]
@@ -611,10 +616,12 @@ def run_case(args) -> None:
     JSON line): ``generate`` (``--n``, ``--count``, ``--calls``),
     ``extrude`` (``--width``, ``--screens``, ``--case-steps``, ``--form``) or
     ``dft`` (512^2 x ``--count`` inverse DFTs, ``--calls``; ``--form`` fp32 for
-    the FFT, else the tensor-core form)."""
+    the FFT, else the tensor-core form) or ``readout`` (the 9-layer bilinear
+    extruder readout at ``--n``, ``--calls`` frames)."""
     import torch
 
     import pyturb_gb300 as G
+    from pyturb_gb300 import _lib
     from pyturb_gb300.backend import NoiseStream, cuda_device
     from pyturb_gb300.covariance import AnchorTables, build_operator
     from pyturb_gb300.extrude import RingExtruder
@@ -631,6 +638,33 @@ def run_case(args) -> None:
         torch.cuda.synchronize()
         dt = (time.perf_counter() - t0) / max(1, args.calls)
         print(f"dft 512^2 x {args.count} form={args.form}: {dt * 1e6:.1f} us per call")
+        return
+    if args.case == "readout":
+        # the 9-layer bilinear readout of one realisation at n = --n (1024 in the bench)
+        from pyturb_gb300.backend import stream_handle
+
+        n = args.n
+        tab = layer_table()
+        cos_z = np.cos(np.deg2rad(ZENITH))
+        frac = np.array(FRACTIONS) / np.sum(FRACTIONS)
+        r0s = [R0 * cos_z ** 0.6 * f ** (-0.6) for f in frac]
+        winds = [(v * np.cos(np.deg2rad(d)), v * np.sin(np.deg2rad(d))) for _, _, v, d in tab]
+        ext = G.ExtrudedAtmosphere(n=n, pixel_scale=DIAM / n, layer_r0=r0s, layer_L0=[L0] * 9,
+                                   layer_wind=winds,
+                                   layer_altitude_los=[h / cos_z for h in HEIGHTS],
+                                   interp="linear", seeds=list(range(9)))
+        o = torch.empty((n, n), dtype=torch.float32, device="cuda")
+        ext.set_time(0.01)
+        params = ext.readout_params()
+        ext.integrate(out=o)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.calls):
+            _lib.call("pt_readout", n, ext.width, ext.capacity, 0, 9, params,
+                      ext._buf.data_ptr(), 1.0, o.data_ptr(), stream_handle())
+        torch.cuda.synchronize()
+        dt = (time.perf_counter() - t0) / max(1, args.calls)
+        print(f"readout n={n} 9 layers: {dt * 1e6:.1f} us per frame")
         return
     if args.case == "generate":
         g = G.PhaseScreen(n=args.n, pixel_scale=8.0 / args.n, r0=0.15, L0=25.0,
@@ -671,7 +705,7 @@ def main() -> None:
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extrude", action="store_true")
     ap.add_argument("--no-diff", action="store_true")
-    ap.add_argument("--case", choices=["generate", "extrude", "dft"], default=None,
+    ap.add_argument("--case", choices=["generate", "extrude", "dft", "readout"], default=None,
                     help="run one small named workload for profiling and exit")
     ap.add_argument("--n", type=int, default=384)
     ap.add_argument("--count", type=int, default=64)

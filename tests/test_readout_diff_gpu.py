@@ -170,3 +170,33 @@ def test_checkpointed_readout_loss_matches_the_materialised_one():
         a, b = a.cpu().numpy().astype(np.float64), b.cpu().numpy().astype(np.float64)
         assert np.linalg.norm(a - b) <= 1e-5 * np.linalg.norm(a)
 
+
+
+def test_config4_geometry_matches_oracle():
+    """The benchmark geometry at full size for one batch element and two
+    frames: 9 layers of 768^2, 8 NGS directions in a 60" disc + 1 LGS at
+    90 km, pupil 512^2, frozen-flow winds; forward and every gradient against
+    the float64 oracle."""
+    rng = np.random.default_rng(44)
+    L, S, n, T = 9, 768, 512, 2
+    heights = np.array([0.0, 500.0, 1000.0, 2000.0, 4000.0, 6000.0, 8000.0, 12000.0, 16000.0])
+    rad = np.deg2rad(60.0 / 3600.0) * np.sqrt(rng.uniform(0, 1, 8))
+    ang = rng.uniform(0, 2 * np.pi, 8)
+    dirs = np.concatenate([np.stack([rad * np.cos(ang), rad * np.sin(ang)], 1), [[0.0, 0.0]]])
+    D = dirs.shape[0]
+    mag = np.ones((D, L))
+    mag[-1] = 1.0 - heights / 90e3
+    winds = rng.uniform(-25, 25, (L, 2))
+    dx = 8.0 / n
+    pos0 = rd.positions(n, S, dx, heights, dirs, mag, winds, np.arange(T) * 1e-3)
+    screens = rng.standard_normal((1, L, S, S)).astype(np.float32)
+    w = rng.uniform(0.2, 0.6, L).astype(np.float32)
+    g = rng.standard_normal((1, T, D, n, n)).astype(np.float32)
+    out, gs, gw, gp = run_gpu(screens, w, pos0, mag, n, g)
+    ref = rd.layer_readout(screens.astype(np.float64), w.astype(np.float64), pos0, mag, n)
+    rgs, rgw, rgp = rd.layer_readout_vjp(screens, w.astype(np.float64), pos0, mag, n, g)
+    errs = [rel(out, ref), rel(gs, rgs), rel(gw, rgw), rel(gp, rgp)]
+    print("config-4 geometry rel-L2: forward %.2e, screens %.2e, weights %.2e, positions %.2e"
+          % tuple(errs))
+    assert errs[0] < TOL_FWD
+    assert max(errs[1:]) < TOL_GRAD

@@ -80,11 +80,12 @@ def test_vjp_matches_torch_autograd():
     out = torch.stack(out, dim=1).reshape(B, T, D, n, n)
     (out * torch.tensor(g)).sum().backward()
     gs, gw, gp = rd.layer_readout_vjp(screens, w, pos0, mag, n, g)
+    # the oracle rounds positions to the device's 2^-32 px fixed point
     np.testing.assert_allclose(out.detach().numpy(), rd.layer_readout(screens, w, pos0, mag, n),
-                               rtol=1e-12, atol=1e-12)
-    np.testing.assert_allclose(ts.grad.numpy(), gs, rtol=1e-10, atol=1e-12)
-    np.testing.assert_allclose(tw.grad.numpy(), gw, rtol=1e-10)
-    np.testing.assert_allclose(tp.grad.numpy(), gp, rtol=1e-10, atol=1e-12)
+                               rtol=1e-7, atol=1e-8)
+    np.testing.assert_allclose(ts.grad.numpy(), gs, rtol=1e-7, atol=1e-8)
+    np.testing.assert_allclose(tw.grad.numpy(), gw, rtol=1e-7)
+    np.testing.assert_allclose(tp.grad.numpy(), gp, rtol=1e-7, atol=1e-7)
 
 
 def test_positions_follow_the_reference_geometry():
@@ -100,3 +101,20 @@ def test_positions_follow_the_reference_geometry():
             mid = pos0[t, 0, l] + m * (n - 1) / 2
             disp = np.array(v) * tt + alt * np.array([1e-4, -2e-4])
             np.testing.assert_allclose(mid, centre + disp / dx, rtol=0, atol=1e-12)
+
+
+def test_samples_on_grid_lines_take_the_fixed_point_cell():
+    # mag = 37/45 (an LGS at 90 km over a layer at 16 km) puts samples exactly on
+    # grid lines; the cell (and so the one-sided position derivative) is the
+    # one the 32.32 fixed-point position selects, as on the device
+    S, n = 64, 48
+    m = 1.0 - 16000.0 / 90000.0
+    p0 = (S - 1) / 2.0 - m * (n - 1) / 2.0
+    i0, i1, f = rd._axis(p0, m, n, S)
+    one = 2 ** 32
+    v = int(np.rint(p0 * one)) + np.arange(n, dtype=np.int64) * int(np.rint(m * one))
+    np.testing.assert_array_equal(i0, v >> 32)
+    np.testing.assert_allclose(f, (v & (one - 1)) / one, rtol=0, atol=0)
+    exact = (p0 + m * np.arange(n))
+    assert np.max(np.abs(i0 + f - exact)) < 1e-8
+
