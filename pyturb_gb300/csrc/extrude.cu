@@ -299,14 +299,17 @@ __device__ __forceinline__ f2p pfma(f2p a, f2p b, f2p c) {
   return d;
 }
 // (s, c) += a x for two modes at once: exact product a_hi x = h + e, the
-// lo part a_lo x in float32, h added to s by an error-free two-sum
-__device__ __forceinline__ void pmac(f2p& s, f2p& c, f2p ah, f2p al, f2p x2) {
-  const f2p h = pmul(ah, x2);
-  const f2p e = pfma(ah, x2, h ^ 0x8000000080000000ull);
-  const f2p t = padd(s, h);
+// lo part a_lo x in float32, h added to s by an error-free two-sum. The
+// caller passes nah = -a_hi, so the product comes out negated (nh = -h,
+// exact) and no sign flip is needed per product: t = s - nh = s + h and
+// h - bv = -(nh + bv) round identically.
+__device__ __forceinline__ void pmac(f2p& s, f2p& c, f2p ah, f2p nah, f2p al, f2p x2) {
+  const f2p nh = pmul(nah, x2);
+  const f2p e = pfma(ah, x2, nh);
+  const f2p t = psub(s, nh);
   const f2p bv = psub(t, s);
   c = padd(c, pfma(al, x2, e));
-  c = padd(c, padd(psub(s, psub(t, bv)), psub(h, bv)));
+  c = padd(c, psub(psub(s, psub(t, bv)), padd(nh, bv)));
   s = t;
 }
 
@@ -341,9 +344,10 @@ __global__ void __launch_bounds__(256)
 k_anchor_gemm(int W, int K, int Kz, int cap, int g, int J, int kslice, int incr,
               const RingDst dst, const float* __restrict__ X, const AnchorDev an,
               const float* __restrict__ buf, float2* __restrict__ part) {
-  // (64 modes: 32-column chunks keep the static shared memory under 48 KB)
-  constexpr int KC = R == 64 ? 32 : 64, NP2 = R / 2, JT = 64, JPT = JT * NP2 / 256;
-  __shared__ float xs[JT][KC + 1];
+  // 32-column chunks keep the static shared memory under 48 KB; the operand
+  // is staged as (x, x) pairs, ready for the packed products
+  constexpr int KC = 32, NP2 = R / 2, JT = 64, JPT = JT * NP2 / 256;
+  __shared__ f2p xs[JT][KC + 1];
   __shared__ f2p phs[KC][NP2], pls[KC][NP2];
   const int tid = threadIdx.x;
   const int j0 = blockIdx.x * JT, z = blockIdx.y;
@@ -365,7 +369,7 @@ k_anchor_gemm(int W, int K, int Kz, int cap, int g, int J, int kslice, int incr,
                   : (k < K + W ? slab[(size_t)dst.d[j].y * W + (k - K)]
                                : slab[(size_t)ring_back(dst.d[j].y, 1, cap) * W + (k - K - W)]);
       }
-      xs[jj][kk] = v;
+      xs[jj][kk] = pack2(v, v);
     }
     // the table rows k0 .. k0 + KC - 1 are contiguous: straight copies
     for (int e = tid; e < KC * NP2; e += 256) {
@@ -382,17 +386,12 @@ k_anchor_gemm(int W, int K, int Kz, int cap, int g, int J, int kslice, int incr,
         // noise columns: U^T B (bscale beta) is ~1% of the row and its
         // rounding random from row to row, so plain float32 suffices
 #pragma unroll
-        for (int q = 0; q < JPT; ++q) {
-          const float xv = xs[jt + q][kk];
-          c[q] = pfma(ah, pack2(xv, xv), c[q]);
-        }
+        for (int q = 0; q < JPT; ++q) c[q] = pfma(ah, xs[jt + q][kk], c[q]);
       } else {
         const f2p al = pls[kk][p];
+        const f2p nah = ah ^ 0x8000000080000000ull;
 #pragma unroll
-        for (int q = 0; q < JPT; ++q) {
-          const float xv = xs[jt + q][kk];
-          pmac(s[q], c[q], ah, al, pack2(xv, xv));
-        }
+        for (int q = 0; q < JPT; ++q) pmac(s[q], c[q], ah, nah, al, xs[jt + q][kk]);
       }
     }
     __syncthreads();
@@ -783,7 +782,7 @@ using namespace pt;
 // GEMM (up to kMaxSplitTiled slices) followed by those of the correction.
 // (the partials are followed by the anchor's (s, c) pairs: up to
 // kAnchorSplit x J x 64 float2)
-constexpr int kAnchorSplit = 96;
+constexpr int kAnchorSplit = 192;
 struct Fp32Work {
   size_t x, lo_tiles, partial, total;
   int lo_nz, max_nz;
@@ -967,10 +966,11 @@ static int extrude_jobs(const char* who, const ExtrudeForm& form, int W, int m,
                              form.anchor->u};
           const int R = form.anchor->modes, Kt = K + (form.incr ? 2 : 1) * W;
           const int jb = (J + 63) / 64;
-          // about two CTAs per SM, chunks of 64 columns
-          const int nsplit = std::max(1, std::min(std::min(kAnchorSplit, (Kt + 63) / 64),
-                                                  (2 * 152 + jb - 1) / jb));
-          const int kslice = ((Kt + nsplit - 1) / nsplit + 63) / 64 * 64;
+          // about four CTAs per SM (a single wave of two left SMs idle in its
+          // tail), slices of 32 or more columns
+          const int nsplit = std::max(1, std::min(std::min(kAnchorSplit, (Kt + 31) / 32),
+                                                  (4 * 152 + jb - 1) / jb));
+          const int kslice = ((Kt + nsplit - 1) / nsplit + 31) / 32 * 32;
           const int nz_a = (Kt + kslice - 1) / kslice;
           float2* apart =
               (float2*)((char*)partial + al256((size_t)fw.max_nz * J * W * sizeof(float)));
