@@ -16,7 +16,20 @@ struct FftDesc {
   int n;
   int nstages;
   int radix[kMaxStages];
+  // Bluestein form (M > 0), for lengths with a large prime factor: the
+  // length-n transform as a circular convolution of length M, a power of two
+  // >= 2n - 1, on the radix-8/4/2 stages; buffers then hold M elements a
+  // vector (fft_buf_len)
+  int M;
+  int mstages;
+  int mradix[kMaxStages];
+  const float2* chirp;  // (n) exp(+i pi (e^2 mod 2n) / n)
+  const float2* bhat;   // (M) sum_m b[m] exp(+2 pi i m k / M), b the wrapped conj(chirp)
+  const float2* twM;    // (M) exp(+2 pi i e / M)
 };
+
+// Elements a vector buffer of fft_smem must hold for this transform.
+__host__ __device__ inline int fft_buf_len(const FftDesc& d) { return d.M > 0 ? d.M : d.n; }
 
 // Factor n into the stage radices used by the Stockham passes. Radix 8
 // first keeps the stage count low; leftover prime factors > 7 become a
@@ -217,22 +230,21 @@ __device__ __forceinline__ void stage_generic(const float2* __restrict__ a, floa
   }
 }
 
-// Run all stages on `nvec` vectors held in shared memory. Element e of vector
-// v sits at buf[v * vs + e * es]. Returns the buffer holding the result
-// (a or b). Ends with __syncthreads().
-__device__ inline float2* fft_smem(float2* a, float2* b, const FftDesc& d, const float2* tw,
-                                   int nvec, int vs, int es, bool vfast) {
+// The Stockham stages of a length-n transform with the given radices.
+__device__ inline float2* fft_stages(float2* a, float2* b, const int* radix, int nstages,
+                                     const float2* tw, int n, int nvec, int vs, int es,
+                                     bool vfast) {
   int Ns = 1;
-  for (int s = 0; s < d.nstages; ++s) {
-    const int R = d.radix[s];
+  for (int s = 0; s < nstages; ++s) {
+    const int R = radix[s];
     switch (R) {
-      case 2: stage_r<2>(a, b, tw, d.n, Ns, nvec, vs, es, vfast); break;
-      case 3: stage_r<3>(a, b, tw, d.n, Ns, nvec, vs, es, vfast); break;
-      case 4: stage_r<4>(a, b, tw, d.n, Ns, nvec, vs, es, vfast); break;
-      case 5: stage_r<5>(a, b, tw, d.n, Ns, nvec, vs, es, vfast); break;
-      case 7: stage_r<7>(a, b, tw, d.n, Ns, nvec, vs, es, vfast); break;
-      case 8: stage_r<8>(a, b, tw, d.n, Ns, nvec, vs, es, vfast); break;
-      default: stage_generic(a, b, tw, d.n, R, Ns, nvec, vs, es); break;
+      case 2: stage_r<2>(a, b, tw, n, Ns, nvec, vs, es, vfast); break;
+      case 3: stage_r<3>(a, b, tw, n, Ns, nvec, vs, es, vfast); break;
+      case 4: stage_r<4>(a, b, tw, n, Ns, nvec, vs, es, vfast); break;
+      case 5: stage_r<5>(a, b, tw, n, Ns, nvec, vs, es, vfast); break;
+      case 7: stage_r<7>(a, b, tw, n, Ns, nvec, vs, es, vfast); break;
+      case 8: stage_r<8>(a, b, tw, n, Ns, nvec, vs, es, vfast); break;
+      default: stage_generic(a, b, tw, n, R, Ns, nvec, vs, es); break;
     }
     __syncthreads();
     float2* t = a;
@@ -241,6 +253,49 @@ __device__ inline float2* fft_smem(float2* a, float2* b, const FftDesc& d, const
     Ns *= R;
   }
   return a;
+}
+
+// Bluestein: with w[e] = exp(+i pi e^2 / n) and n k = (n^2 + k^2 - (k - n)^2)/2,
+//   X[k] = w[k] (a (*) b)[k],  a[e] = x[e] w[e] (e < n, zero up to M),
+// b[m] = conj(w[m]) for |m| < n wrapped modulo M, and the circular
+// convolution is (1/M) conj(F(conj(F(a) bhat))) with F the inverse-sign
+// transform of length M and bhat = F(b) precomputed.
+__device__ inline float2* fft_bluestein(float2* a, float2* b, const FftDesc& d, int nvec, int vs,
+                                        int es, bool vfast) {
+  const int n = d.n, M = d.M;
+  for (int t = threadIdx.x; t < nvec * M; t += blockDim.x) {
+    const int v = vfast ? t % nvec : t / M, e = vfast ? t / nvec : t % M;
+    float2* p = a + v * vs + e * es;
+    *p = e < n ? cmul(*p, __ldg(d.chirp + e)) : make_float2(0.f, 0.f);
+  }
+  __syncthreads();
+  float2* x = fft_stages(a, b, d.mradix, d.mstages, d.twM, M, nvec, vs, es, vfast);
+  float2* y = x == a ? b : a;
+  for (int t = threadIdx.x; t < nvec * M; t += blockDim.x) {
+    const int v = vfast ? t % nvec : t / M, e = vfast ? t / nvec : t % M;
+    float2* p = x + v * vs + e * es;
+    *p = cconj(cmul(*p, __ldg(d.bhat + e)));
+  }
+  __syncthreads();
+  float2* z = fft_stages(x, y, d.mradix, d.mstages, d.twM, M, nvec, vs, es, vfast);
+  const float inv = 1.0f / (float)M;
+  for (int t = threadIdx.x; t < nvec * n; t += blockDim.x) {
+    const int v = vfast ? t % nvec : t / n, e = vfast ? t / nvec : t % n;
+    float2* p = z + v * vs + e * es;
+    *p = cscale(cmul(__ldg(d.chirp + e), cconj(*p)), inv);
+  }
+  __syncthreads();
+  return z;
+}
+
+// Run all stages on `nvec` vectors held in shared memory. Element e of vector
+// v sits at buf[v * vs + e * es]; both buffers hold fft_buf_len(d) elements
+// a vector. Returns the buffer holding the result (a or b). Ends with
+// __syncthreads().
+__device__ inline float2* fft_smem(float2* a, float2* b, const FftDesc& d, const float2* tw,
+                                   int nvec, int vs, int es, bool vfast) {
+  if (d.M > 0) return fft_bluestein(a, b, d, nvec, vs, es, vfast);
+  return fft_stages(a, b, d.radix, d.nstages, tw, d.n, nvec, vs, es, vfast);
 }
 
 }  // namespace pt

@@ -41,6 +41,7 @@ struct pt_grid {
   double* beta;     // (P, 3, 2) grid mean of each basis row
   int sym;          // every level's frequencies are {-a, 0, +a}
   int cols_variant; // power-of-two column pass: 0 register-fed, 1 TMA-fed
+  float2* blu;      // Bluestein tables of desc (chirp, bhat, twM), or NULL
 };
 
 namespace pt {
@@ -69,8 +70,10 @@ static inline int gen_chunk(int ns) {
 }
 // Rows per CTA of the shared-memory row pass: about 2048 elements, so every
 // stage gives most of the 256 threads a butterfly.
-static inline int rows_per_cta(int ns) { return std::max(1, std::min(16, 2048 / ns)); }
-static inline int cols_per_cta(int ns) { return std::max(1, std::min(16, 4096 / ns)); }
+// rows / columns a CTA of the shared-memory passes transforms, from the
+// buffer length (fft_buf_len: M for a Bluestein grid)
+static inline int rows_per_cta(int nb) { return std::max(1, std::min(16, 2048 / nb)); }
+static inline int cols_per_cta(int nb) { return std::max(1, std::min(16, 4096 / nb)); }
 
 static inline void count_launch(int k = 1) {
   __atomic_add_fetch(launch_counter(), (uint64_t)k, __ATOMIC_RELAXED);
@@ -181,7 +184,7 @@ k_rows(FftDesc d, const float2* __restrict__ tw, int rpc, const float2* __restri
   const int row0 = blockIdx.x * rpc;
   const int img = blockIdx.y;  // image within this chunk
   if (gen) gen_coef_pair(ga, img);
-  const int vs = ns + 1;
+  const int vs = fft_buf_len(d) + 1;
   float2* bufA = sm;
   float2* bufB = sm + rpc * vs;
   float2* stw = sm + 2 * rpc * vs;
@@ -238,7 +241,7 @@ k_frame_rows(FftDesc d, const float2* __restrict__ tw, FrameRowArgs a, float2* _
   const int pair = blockIdx.y;
   const int kxa = rp, kxb = (ns - rp) % ns;
   const int nrows = (kxa == kxb) ? 1 : 2;
-  const int vs = ns + 1;
+  const int vs = fft_buf_len(d) + 1;
   // X rows: [frame 0 row a, frame 0 row b, frame 1 row a, frame 1 row b]
   float2* X = sm;                // 4 * vs
   float2* bufA = sm + 4 * vs;    // 2 * vs
@@ -346,7 +349,7 @@ k_frame_rows_uniform(FftDesc d, const float2* __restrict__ tw,
   const int ns = d.n;
   const int kx = blockIdx.x;
   const int fbeg = blockIdx.y * kAnchor;  // this CTA's frames [fbeg, fbeg + kAnchor)
-  const int vs = ns + 1;
+  const int vs = fft_buf_len(d) + 1;
   float2* bufA = sm;
   float2* bufB = sm + kPairsPerFft * vs;
   float2* stw = sm + 2 * kPairsPerFft * vs;
@@ -451,9 +454,10 @@ k_pair_cols(FftDesc d, const float2* __restrict__ tw, const float2* __restrict__
   const int y0 = blockIdx.x * C;
   const int pl = blockIdx.y;  // pair within chunk
   const int pair = pair0 + pl;
+  const int nb = fft_buf_len(d);
   float2* bufA = sm;
-  float2* bufB = sm + ns * C;
-  float2* stw = bufB + ns * C;
+  float2* bufB = sm + nb * C;
+  float2* stw = bufB + nb * C;
   // column tables from an even float2 offset: utab below is read as float4
   float2* mtab = stw + ((ns + 1) & ~1);  // (2, 3P, C)
   for (int i = threadIdx.x; i < ns; i += blockDim.x) stw[i] = tw[i];
@@ -567,9 +571,10 @@ k_plain_cols(FftDesc d, const float2* __restrict__ tw, const float2* __restrict_
   const int ns = d.n;
   const int y0 = blockIdx.x * C;
   const int img = blockIdx.y;
+  const int nb = fft_buf_len(d);
   float2* bufA = sm;
-  float2* bufB = sm + ns * C;
-  float2* stw = bufB + ns * C;
+  float2* bufB = sm + nb * C;
+  float2* stw = bufB + nb * C;
   for (int i = threadIdx.x; i < ns; i += blockDim.x) stw[i] = tw[i];
   for (int i = threadIdx.x; i < ns * C; i += blockDim.x) {
     const int x = i / C, c = i % C;
@@ -747,15 +752,35 @@ __global__ void k_lgs_zoom(int L, int ns, int n, int T, const int32_t* __restric
 #include "gt_fast.cuh"       // register transforms of length 3 * 2^k (Good-Thomas)
 
 // ================================================================ host helpers
-static size_t rows_smem(int ns, int rpc) {
-  return (size_t)(2 * rpc * (ns + 1) + ns) * sizeof(float2);
+// shared memory of the generic passes: nb = fft_buf_len of the grid's
+// transform (exchange buffers), ns twiddles
+static size_t rows_smem(int ns, int nb, int rpc) {
+  return (size_t)(2 * rpc * (nb + 1) + ns) * sizeof(float2);
 }
-static size_t frame_rows_smem(int ns) { return (size_t)(8 * (ns + 1) + ns) * sizeof(float2); }
-static size_t cols_smem(int ns, int C, int P) {
+static size_t frame_rows_smem(int ns, int nb) {
+  return (size_t)(8 * (nb + 1) + ns) * sizeof(float2);
+}
+static size_t cols_smem(int ns, int nb, int C, int P) {
   // exchange buffers, twiddles, (m, U/W, K) column tables, staged basis rows
-  return (size_t)(2 * ns * C + ((ns + 1) & ~1) + 8 * std::max(P, 1) * C + C +
+  return (size_t)(2 * nb * C + ((ns + 1) & ~1) + 8 * std::max(P, 1) * C + C +
                   (P * ns <= kColBasisMax ? P * ns : 0)) *
          sizeof(float2);
+}
+
+// The grid's transform for the frame passes: the Bluestein form only when
+// its buffers fit (the frame row kernels hold eight and 2 x kPairsPerFft
+// rows); otherwise the direct-sum stages.
+static FftDesc frame_desc(const pt_grid* g) {
+  FftDesc d = g->desc;
+  const int ns = g->ns;
+  if (d.M > 0) {
+    const size_t cap = 220 * 1024;
+    if (frame_rows_smem(ns, d.M) > cap ||
+        (size_t)(2 * kPairsPerFft * (d.M + 1) + ns) * sizeof(float2) > cap ||
+        cols_smem(ns, d.M, cols_per_cta(d.M), g->P) > cap)
+      d.M = 0;
+  }
+  return d;
 }
 
 template <class K>
@@ -819,14 +844,15 @@ static int launch_uniform_t(const pt_grid* g, const float2* spectra, int L, int 
   const dim3 grid(ns, (nf + kAnchor - 1) / kAnchor);
   ProfScope ps("k_frame_rows_uniform", s);
   (void)ptab;  // the power-of-two sizes 256/512/1024 take launch_uniform_reg_chunk instead
-  const size_t smem = (size_t)(2 * kPairsPerFft * (ns + 1) + ns) * sizeof(float2);
+  const FftDesc fd = frame_desc(g);
+  const size_t smem = (size_t)(2 * kPairsPerFft * (fft_buf_len(fd) + 1) + ns) * sizeof(float2);
   if (ns <= 512) {
     if (int rc = set_smem(k_frame_rows_uniform<LM, 1>, smem, "k_frame_rows_uniform")) return rc;
-    k_frame_rows_uniform<LM, 1><<<grid, ns, smem, s>>>(g->desc, g->tw, spectra, L, nf, up, hn,
+    k_frame_rows_uniform<LM, 1><<<grid, ns, smem, s>>>(fd, g->tw, spectra, L, nf, up, hn,
                                                        img);
   } else {
     if (int rc = set_smem(k_frame_rows_uniform<LM, 2>, smem, "k_frame_rows_uniform")) return rc;
-    k_frame_rows_uniform<LM, 2><<<grid, (ns + 1) / 2, smem, s>>>(g->desc, g->tw, spectra, L, nf,
+    k_frame_rows_uniform<LM, 2><<<grid, (ns + 1) / 2, smem, s>>>(fd, g->tw, spectra, L, nf,
                                                                 up, hn, img);
   }
   return PT_OK;
@@ -1172,6 +1198,90 @@ extern "C" int pt_selftest_wait_timeout(long long limit, int* timed_out) {
 using namespace pt;
 
 // ================================================================ C-ABI
+// Lengths whose largest prime factor exceeds kBluesteinPrime take the
+// Bluestein form (fft_bluestein) when its padded length M fits the passes'
+// shared memory: the direct-sum stage costs O(p) per element for a prime p.
+constexpr int kBluesteinPrime = 61;
+constexpr int kBluesteinMaxM = 8192;
+
+static int largest_prime_factor(int n) {
+  int best = 1;
+  for (int p = 2; (long long)p * p <= n; ++p)
+    while (n % p == 0) {
+      best = p;
+      n /= p;
+    }
+  return n > 1 ? std::max(best, n) : best;
+}
+
+// In-place radix-2 transform of a power-of-two length, exp(+2 pi i j k / n), FP64.
+static void host_fft_pow2(std::vector<double>& re, std::vector<double>& im) {
+  const size_t n = re.size();
+  for (size_t i = 1, j = 0; i < n; ++i) {
+    size_t bit = n >> 1;
+    for (; j & bit; bit >>= 1) j ^= bit;
+    j ^= bit;
+    if (i < j) {
+      std::swap(re[i], re[j]);
+      std::swap(im[i], im[j]);
+    }
+  }
+  for (size_t len = 2; len <= n; len <<= 1) {
+    const double a = 2.0 * M_PI / (double)len;
+    for (size_t i = 0; i < n; i += len)
+      for (size_t k = 0; k < len / 2; ++k) {
+        const double c = std::cos(a * (double)k), sn = std::sin(a * (double)k);
+        const size_t u = i + k, v = i + k + len / 2;
+        const double tr = re[v] * c - im[v] * sn, ti = re[v] * sn + im[v] * c;
+        re[v] = re[u] - tr;
+        im[v] = im[u] - ti;
+        re[u] += tr;
+        im[u] += ti;
+      }
+  }
+}
+
+static int bluestein_plan(pt_grid* g) {
+  const int n = g->ns;
+  if (largest_prime_factor(n) <= kBluesteinPrime) return PT_OK;
+  int M = 1;
+  while (M < 2 * n - 1) M <<= 1;
+  if (M > kBluesteinMaxM) return PT_OK;  // keeps the direct-sum stage
+  const FftDesc dm = make_fft_desc(M);
+  std::vector<float2> tab((size_t)n + 2 * M);
+  std::vector<double> br(M, 0.0), bi(M, 0.0);
+  for (int e = 0; e < n; ++e) {
+    const long long q = (long long)e * e % (2LL * n);  // exact phase index
+    const double a = M_PI * (double)q / (double)n;
+    const double c = std::cos(a), sn = std::sin(a);
+    tab[e] = make_float2((float)c, (float)sn);
+    br[e] = c;
+    bi[e] = -sn;
+    if (e > 0) {
+      br[M - e] = c;
+      bi[M - e] = -sn;
+    }
+  }
+  host_fft_pow2(br, bi);
+  for (int k = 0; k < M; ++k) {
+    tab[(size_t)n + k] = make_float2((float)br[k], (float)bi[k]);
+    const double a = 2.0 * M_PI * (double)k / (double)M;
+    tab[(size_t)n + M + k] = make_float2((float)std::cos(a), (float)std::sin(a));
+  }
+  int rc = check_cuda(cudaMalloc(&g->blu, tab.size() * sizeof(float2)), "pt_grid_create: cudaMalloc");
+  if (!rc)
+    rc = check_cuda(cudaMemcpy(g->blu, tab.data(), tab.size() * sizeof(float2), cudaMemcpyHostToDevice),
+                    "pt_grid_create: cudaMemcpy");
+  if (rc) return rc;
+  g->desc.M = M;
+  g->desc.mstages = dm.nstages;
+  for (int i = 0; i < dm.nstages; ++i) g->desc.mradix[i] = dm.radix[i];
+  g->desc.chirp = g->blu;
+  g->desc.bhat = g->blu + n;
+  g->desc.twM = g->blu + n + M;
+  return PT_OK;
+}
+
 extern "C" int pt_grid_create(pt_grid** out, int ns, double dx, int P, const double* sh_freq) {
   if (!out) return fail(PT_ERR_ARG, "pt_grid_create: out is NULL");
   *out = nullptr;
@@ -1225,6 +1335,7 @@ extern "C" int pt_grid_create(pt_grid** out, int ns, double dx, int P, const dou
   if (!rc) rc = check_cuda(cudaMemcpy(g->basis, basis.data(), basis.size() * sizeof(float2), cudaMemcpyHostToDevice), "pt_grid_create: cudaMemcpy");
   if (!rc) rc = check_cuda(cudaMemcpy(g->sh_freq, freq.data(), freq.size() * sizeof(double), cudaMemcpyHostToDevice), "pt_grid_create: cudaMemcpy");
   if (!rc) rc = check_cuda(cudaMemcpy(g->beta, beta.data(), beta.size() * sizeof(double), cudaMemcpyHostToDevice), "pt_grid_create: cudaMemcpy");
+  if (!rc) rc = bluestein_plan(g);
   if (rc) {
     pt_grid_destroy(g);
     return rc;
@@ -1271,6 +1382,7 @@ extern "C" int pt_grid_destroy(pt_grid* g) {
   cudaFree(g->basis);
   cudaFree(g->sh_freq);
   cudaFree(g->beta);
+  cudaFree(g->blu);
   delete g;
   return PT_OK;
 }
@@ -1287,8 +1399,9 @@ extern "C" int pt_ifft2(const pt_grid* g, const float* in, float* out, int batch
   SpecWork w = carve(g, 1, work);
   if (!work || work_bytes < w.bytes) return fail(PT_ERR_ARG, "pt_ifft2: workspace too small");
   cudaStream_t s = (cudaStream_t)stream;
-  const int ns = g->ns, ch = gen_chunk(ns), rpc = rows_per_cta(ns), C = cols_per_cta(ns);
-  const size_t rs = rows_smem(ns, rpc), cs = cols_smem(ns, C, 0);
+  const int ns = g->ns, blen = fft_buf_len(g->desc), ch = gen_chunk(ns),
+            rpc = rows_per_cta(blen), C = cols_per_cta(blen);
+  const size_t rs = rows_smem(ns, blen, rpc), cs = cols_smem(ns, blen, C, 0);
   if (int rc = set_smem(k_rows, rs, "k_rows")) return rc;
   if (int rc = set_smem(k_plain_cols, cs, "k_plain_cols")) return rc;
   GenRowArgs none{};
@@ -1330,8 +1443,9 @@ static int generate_impl(const pt_grid* g, int count, const float* amplitude,
   if (!work || work_bytes < w.bytes) return fail(PT_ERR_ARG, "pt_generate: workspace too small");
   cudaStream_t s = (cudaStream_t)stream;
   const int n_fft = (count + 1) / 2;
-  const int ch = gen_chunk(ns), rpc = rows_per_cta(ns), C = cols_per_cta(ns);
-  const size_t rs = rows_smem(ns, rpc), cs = cols_smem(ns, C, P);
+  const int blen = fft_buf_len(g->desc);
+  const int ch = gen_chunk(ns), rpc = rows_per_cta(blen), C = cols_per_cta(blen);
+  const size_t rs = rows_smem(ns, blen, rpc), cs = cols_smem(ns, blen, C, P);
   if (int rc = set_smem(k_rows, rs, "k_rows")) return rc;
   if (int rc = set_smem(k_pair_cols, cs, "k_pair_cols")) return rc;
   for (int b0 = 0; b0 < n_fft; b0 += ch) {
@@ -1442,10 +1556,12 @@ extern "C" int pt_frames(const pt_grid* g, int L, const float* spectra, const fl
   SpecWork w = carve(g, L, work);
   if (!work || work_bytes < w.bytes) return fail(PT_ERR_ARG, "pt_frames: workspace too small");
   cudaStream_t s = (cudaStream_t)stream;
-  const int ch = image_chunk(ns), C = cols_per_cta(ns);
+  const FftDesc fd = frame_desc(g);
+  const int blen = fft_buf_len(fd);
+  const int ch = image_chunk(ns), C = cols_per_cta(blen);
   const int J = per_layer ? 1 : L;
   if (2 * J > kShiftDoubles) return fail(PT_ERR_UNSUPPORTED, "pt_frames: at most 896 layers");
-  const size_t rs = frame_rows_smem(ns), cs = cols_smem(ns, C, P);
+  const size_t rs = frame_rows_smem(ns, blen), cs = cols_smem(ns, blen, C, P);
   if (int rc = set_smem(k_frame_rows, rs, "k_frame_rows")) return rc;
   if (int rc = set_smem(k_pair_cols, cs, "k_pair_cols")) return rc;
   const int fchunk = 2 * ch;
@@ -1505,7 +1621,7 @@ extern "C" int pt_frames(const pt_grid* g, int L, const float* spectra, const fl
     } else {
       FrameRowArgs fa{(const float2*)spectra, w.px, w.py, J, nf, f0, per_layer};
       ProfScope ps("k_frame_rows", s);
-      k_frame_rows<<<dim3(ns / 2 + 1, npair), kThreads, rs, s>>>(g->desc, g->tw, fa, w.img);
+      k_frame_rows<<<dim3(ns / 2 + 1, npair), kThreads, rs, s>>>(fd, g->tw, fa, w.img);
     }
     count_launch();
     PairStore st{};
@@ -1531,7 +1647,7 @@ extern "C" int pt_frames(const pt_grid* g, int L, const float* spectra, const fl
       if (int rc = pair_cols_reg(g, w.img, npair, 0, st, s)) return rc;
     } else {
       ProfScope ps("k_pair_cols", s);
-      k_pair_cols<<<dim3((ns + C - 1) / C, npair), kThreads, cs, s>>>(g->desc, g->tw, w.img, C, 0,
+      k_pair_cols<<<dim3((ns + C - 1) / C, npair), kThreads, cs, s>>>(fd, g->tw, w.img, C, 0,
                                                                      st);
     }
     count_launch();
@@ -1664,8 +1780,8 @@ extern "C" int pt_ifft2_noalloc(int ns, const float* in, float* out, int batch, 
       65535, std::max<size_t>(1, kNoAllocScratchBytes / (per * sizeof(float2))));
   k_noalloc_twiddles<<<(ns + 127) / 128, 128, 0, s>>>(g.tw, ns);
   count_launch();
-  const int rpc = rows_per_cta(ns), C = cols_per_cta(ns);
-  const size_t rs = rows_smem(ns, rpc), cs = cols_smem(ns, C, 0);
+  const int rpc = rows_per_cta(ns), C = cols_per_cta(ns);  // no Bluestein form here
+  const size_t rs = rows_smem(ns, ns, rpc), cs = cols_smem(ns, ns, C, 0);
   if (!pow2_fast(ns)) {
     if (int rc = set_smem(k_rows, rs, "k_rows")) return rc;
     if (int rc = set_smem(k_plain_cols, cs, "k_plain_cols")) return rc;
@@ -1860,10 +1976,10 @@ k_psd_series(FftDesc d, const float2* __restrict__ tw, int count,
              const float* __restrict__ series, float* __restrict__ partial) {
   extern __shared__ float2 sm[];
   __shared__ double red[32];
-  const int T = d.n, H = T / 2 + 1;
+  const int T = d.n, H = T / 2 + 1, nb = fft_buf_len(d);
   float2* bufA = sm;
-  float2* bufB = sm + T;
-  float2* stw = sm + 2 * T;
+  float2* bufB = sm + nb;
+  float2* stw = sm + 2 * nb;
   float* acc = (float*)(stw + T);
   for (int i = threadIdx.x; i < T; i += blockDim.x) stw[i] = tw[i];
   for (int f = threadIdx.x; f < H; f += blockDim.x) acc[f] = 0.f;
@@ -1880,7 +1996,7 @@ k_psd_series(FftDesc d, const float2* __restrict__ tw, int count,
     const float mean = (float)(tot / T);
     for (int i = threadIdx.x; i < T; i += blockDim.x) bufA[i] = make_float2(x[i] - mean, 0.f);
     __syncthreads();
-    const float2* res = fft_smem(bufA, bufB, d, stw, 1, T, 1, false);
+    const float2* res = fft_smem(bufA, bufB, d, stw, 1, nb, 1, false);
     __syncthreads();
     for (int f = threadIdx.x; f < H; f += blockDim.x) {
       const float2 v = res[f];
@@ -1916,7 +2032,8 @@ extern "C" int pt_temporal_psd(const pt_grid* g, int count, const float* series,
   if (!work || work_bytes < pt_temporal_psd_workspace_bytes(g, count))
     return fail(PT_ERR_ARG, "pt_temporal_psd: workspace too small");
   const int T = g->ns, H = T / 2 + 1, G = psd_blocks(count);
-  const size_t smem = (size_t)3 * T * sizeof(float2) + (size_t)H * sizeof(float);
+  const size_t smem = (size_t)(2 * fft_buf_len(g->desc) + T) * sizeof(float2) +
+                      (size_t)H * sizeof(float);
   if (smem > 220 * 1024) return fail(PT_ERR_UNSUPPORTED, "pt_temporal_psd: series longer than 8192");
   if (int rc = set_smem(k_psd_series, smem, "k_psd_series")) return rc;
   cudaStream_t s = (cudaStream_t)stream;

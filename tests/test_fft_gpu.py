@@ -1,5 +1,6 @@
 """The shared-memory Stockham inverse FFT against numpy (mixed radix, primes,
-batches larger than one internal chunk)."""
+the Bluestein form for large prime factors, batches larger than one internal
+chunk)."""
 
 import ctypes as C
 
@@ -25,8 +26,10 @@ def _ifft2_gpu(x):
     return o[..., 0] + 1j * o[..., 1]
 
 
-@pytest.mark.parametrize("n", [2, 3, 8, 12, 30, 37, 49, 64, 96, 121, 128, 256, 384, 512, 768,
-                               1024, 1447, 2048])
+# 127, 202 = 2 x 101, 586 = 2 x 293, 1031 and 1447 (prime factors above 61)
+# take the Bluestein form; 37 and 121 = 11^2 the direct-sum stages
+@pytest.mark.parametrize("n", [2, 3, 8, 12, 30, 37, 49, 64, 96, 121, 127, 128, 202, 256, 384,
+                               512, 586, 768, 1024, 1031, 1447, 2048])
 def test_ifft2_matches_numpy(n):
     rng = np.random.default_rng(n)
     batch = 3 if n <= 1024 else 1

@@ -1,7 +1,8 @@
 """Screens drawn with the kernels' own Philox noise against the float64
 oracle fed the same normals (oracle/philox.py), on every transform path of
-generate: power-of-two register (64, 256), mixed-radix shared memory (96) and
-Good-Thomas register (192, 384, 768, 1536 = 3 x 2^k). Tolerance: relative L2
+generate: power-of-two register (64, 256), mixed-radix shared memory (96),
+Good-Thomas register (192, 384, 768, 1536 = 3 x 2^k) and the Bluestein form
+of the shared-memory passes (202 = 2 x 101, 586 = 2 x 293). Tolerance: relative L2
 1e-5 (the device's Box-Muller uses hardware log2 / sqrt / sincos, absolute
 error near 1e-6 per normal)."""
 
@@ -12,7 +13,7 @@ pytestmark = pytest.mark.gpu
 
 
 @pytest.mark.parametrize("n,count", [(64, 5), (256, 4), (96, 7), (192, 3), (384, 4), (768, 3),
-                                     (1536, 1)])
+                                     (1536, 1), (202, 3), (586, 2)])
 def test_device_noise_screens_match_oracle(n, count):
     import oracle
     import pyturb_gb300 as G

@@ -39,7 +39,7 @@ def run(S, w, sx, sy, dx, crop, n_out, scale, g):
 
 
 @pytest.mark.parametrize("uniform", [False, True], ids=["arbitrary", "uniform"])
-@pytest.mark.parametrize("ns,F,L", [(64, 5, 3), (96, 4, 2), (512, 6, 9)])
+@pytest.mark.parametrize("ns,F,L", [(64, 5, 3), (96, 4, 2), (512, 6, 9), (202, 4, 2)])
 def test_synthesis_and_vjp_match_oracle(ns, F, L, uniform):
     rng = np.random.default_rng(ns + F + L)
     S = (rng.standard_normal((L, ns, ns)) + 1j * rng.standard_normal((L, ns, ns))) / ns
