@@ -63,6 +63,8 @@ int pt_selftest_wait_timeout(long long limit, int* timed_out);
  * geometry part of PhaseScreen._build_filters (src/pyturb/fourier.py:174-228).
  * sh_freq: (n_levels, 3) host FP64 subharmonic frequencies f_p = {-1,0,1} df/3^p.
  * Allocates its constant tables on the current device; not a hot-path call.
+ * A length with a prime factor above 61 whose padded length (the power of two
+ * >= 2 ns - 1) is at most 8192 gets a Bluestein form of its transforms.
  */
 typedef struct pt_grid pt_grid;
 
