@@ -932,6 +932,19 @@ def main() -> None:
         "wall_s_timed_region": wall,
     }
     line["generate_256_screens_per_s"] = bench_generate(torch, G)
+    # config 1 and Monte-Carlo against HBM: the algorithmic bytes are the
+    # float32 screens written (the spectra are generated in registers)
+    for key, sps, n_px, prof_note in (
+            ("generate_256_roofline", line["generate_256_screens_per_s"], 256,
+             "64 screens per call"),
+            ("mc_roofline", mc_sps, N_PIX, f"Atmosphere.sample({MC_BATCH})")):
+        gbs = sps * n_px * n_px * 4 / 1e9
+        line[key] = {"bound": "hbm", "achieved": gbs, "peak": hbm, "unit": "GB/s",
+                     "frac": gbs / hbm, "bytes_per_screen": n_px * n_px * 4,
+                     "workload": f"{n_px}^2 screens, {prof_note}",
+                     "note": "issue-bound kernels (Philox + Box-Muller + register FFT rows; "
+                             "barrier-bound 1024-thread column pass): profiles/"
+                             "generate_512_mc.md"}
     line["dft_512_tc_vs_fp32"] = bench_tc_dft(torch)
     if not args.no_extrude:
         line["extrude_1024"] = bench_extrude(torch, G)
