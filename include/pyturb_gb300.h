@@ -99,8 +99,8 @@ int pt_ifft2(const pt_grid* grid, const float* in, float* out, int batch, void* 
  * no reference counterpart beyond the transform it replaces,
  * src/pyturb/fourier.py:259 and src/pyturb/atmosphere.py:918): each 512-point
  * line is a four-step DFT (32 x 16) of two small matrix products on tcgen05,
- * operands split into three bf16 terms with fp32 accumulation, a row pass
- * then a column pass. in and out may alias. Other sizes: PT_ERR_UNSUPPORTED. */
+ * operands of each power-of-two scaled line split into two fp16 terms with
+ * fp32 accumulation, a row pass then a column pass. in and out may alias. Other sizes: PT_ERR_UNSUPPORTED. */
 int pt_ifft2_tc(int ns, const float* in, float* out, int batch, void* stream);
 
 /* Allocation-free variant of pt_ifft2 — no counterpart in the reference.

@@ -13,12 +13,13 @@
 // (A K-major). Then a twiddle multiply in registers. Stage 2: the 256 jobs
 // (line, k1) times the 32 x 32 block form of the 16-point DFT, two M = 128
 // tiles, N = 32, K = 32 (A MN-major, so that a thread's 8 consecutive k1 rows
-// are one 16-byte store). Data operands are split into three bf16 terms by
-// truncation (x = hi + mid + lo exactly), the DFT matrices by rounding; the
-// six products with term indices summing to at most 2 accumulate in fp32 in
-// tensor memory. The lines are staged through shared memory, so loads and
-// stores coalesce for both the row and the column pass.
-#include <cuda_bf16.h>
+// are one 16-byte store). Operands are split into two fp16 terms (x = hi +
+// lo + O(2^-24 x)) after each line is scaled by a power of two that keeps
+// them in fp16 range; the three products hi hi, hi lo, lo hi accumulate in
+// fp32 in tensor memory, and the scale is undone on the way out. The lines
+// are staged through shared memory, so loads and stores coalesce for both
+// the row and the column pass.
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -39,46 +40,41 @@ static __device__ int g_dft_error;
 
 namespace dft {
 constexpr int N = 512, N1 = 32, N2 = 16, LINES = 8, THREADS = 256;
-constexpr int A1_TILE = 128 * 64 * 2;   // bytes of one bf16 term of a stage-1 A tile
+constexpr int A1_TILE = 128 * 64 * 2;   // bytes of one fp16 term of a stage-1 A tile
 constexpr int B1_TILE = 64 * 64 * 2;    // stage-1 B (the 32-point DFT block matrix)
 constexpr int A2_TILE = 128 * 32 * 2;   // one stage-2 A tile, one term
 constexpr int B2_TILE = 32 * 32 * 2;    // stage-2 B (the 16-point DFT block matrix)
-constexpr int TERMS = 3;
+constexpr int TERMS = 2;
 // shared memory: staged lines (fp32 complex) | A (stage 1, reused by stage 2) |
-// B1 | B2, 110 KB, so that two CTAs share an SM (the twiddles live in
-// registers). Unswizzled operands need 16-byte alignment; the base is rounded
-// up to 128 bytes.
+// B1 | B2, 84 KB, two CTAs an SM (the twiddles live in registers).
+// Unswizzled operands need 16-byte alignment; the base is rounded up to 128
+// bytes.
 constexpr int OFF_X = 0;
 constexpr int OFF_A = OFF_X + LINES * N * 8;                       // 32 KB
-constexpr int OFF_B1 = OFF_A + TERMS * A1_TILE;                    // + 48 KB
-constexpr int OFF_B2 = OFF_B1 + TERMS * B1_TILE;                   // + 24 KB
-constexpr int SMEM = OFF_B2 + TERMS * B2_TILE + 128;               // + 6 KB + alignment
+constexpr int OFF_B1 = OFF_A + TERMS * A1_TILE;                    // + 32 KB
+constexpr int OFF_B2 = OFF_B1 + TERMS * B1_TILE;                   // + 16 KB
+constexpr int SMEM = OFF_B2 + TERMS * B2_TILE + 128;               // + 4 KB + alignment
 static_assert(2 * TERMS * A2_TILE <= TERMS * A1_TILE, "stage-2 tiles reuse the stage-1 space");
+// The stage-1 operand of a line is scaled by a power of two so that its
+// largest component is below 2^kScaleExp: the fp16 terms then stay in range
+// through the 32-point stage (|Y| <= 32 sqrt(2) 2^9 < 65504).
+constexpr int kScaleExp = 9;
 
-__device__ __forceinline__ void split3(float v, uint16_t* t) {
-  float r = v;
-#pragma unroll
-  for (int i = 0; i < TERMS; ++i) {
-    const __nv_bfloat16 h = __float2bfloat16_rn(r);
-    t[i] = __bfloat16_as_ushort(h);
-    r -= __bfloat162float(h);
-  }
+// two values as fp16 hi and lo terms (v = hi + lo + O(2^-24 v), round to
+// nearest twice), packed in pairs (a at the lower address)
+__device__ __forceinline__ void split2h(float a, float b, uint32_t& hi, uint32_t& lo) {
+  const __half2 h = __floats2half2_rn(a, b);
+  const float2 hf = __half22float2(h);
+  const __half2 l = __floats2half2_rn(a - hf.x, b - hf.y);
+  hi = *reinterpret_cast<const uint32_t*>(&h);
+  lo = *reinterpret_cast<const uint32_t*>(&l);
 }
 
-// v = hi + mid + lo exactly, each a bf16 in the high half of the returned
-// bit pattern: truncate to the 8 leading significant bits, twice (both
-// differences are exact in fp32); the remainder has at most 8 significant
-// bits and so is a bf16 itself.
-__device__ __forceinline__ void split3t(float v, uint32_t* t) {
-  const uint32_t h = __float_as_uint(v) & 0xFFFF0000u;
-  const float r1 = v - __uint_as_float(h);
-  const uint32_t m = __float_as_uint(r1) & 0xFFFF0000u;
-  t[0] = h;
-  t[1] = m;
-  t[2] = __float_as_uint(r1 - __uint_as_float(m));
+// Instruction descriptor of kind::f16 with fp16 A and B (format 0), fp32 D,
+// K-major unless kMajorMN_A.
+__host__ __device__ constexpr uint32_t idesc_f16(int M, int N) {
+  return (1u << 4) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
-// two bf16 (the high halves of a and b) as one 32-bit word, a at the lower address
-__device__ __forceinline__ uint32_t pack_hi(uint32_t a, uint32_t b) { return __byte_perm(a, b, 0x7632); }
 
 // The stage-2 A tiles are MN-major without swizzle: 8 consecutive rows (M) of
 // one K index make a 16-byte core-matrix row, 8 K indices a core matrix; core
@@ -109,11 +105,11 @@ __device__ void build_dft_b(uint8_t* sb, int tile_bytes) {
     float v;
     if (o < M) v = kk < M ? w.x : -w.y;
     else v = kk < M ? w.y : w.x;
-    uint16_t t[TERMS];
-    split3(v, t);
+    const __half h = __float2half_rn(v);
+    const __half l = __float2half_rn(v - __half2float(h));
     const uint32_t off = tc::core_offset(o, kk, K);
-#pragma unroll
-    for (int q = 0; q < TERMS; ++q) *(uint16_t*)(sb + q * tile_bytes + off) = t[q];
+    *(__half*)(sb + off) = h;
+    *(__half*)(sb + tile_bytes + off) = l;
   }
 }
 }  // namespace dft
@@ -134,6 +130,7 @@ k_dft512_tc(const float2* in, float2* out, int lines, long long img) {
   extern __shared__ uint8_t smraw[];
   __shared__ uint64_t bar;
   __shared__ uint32_t tslot;
+  __shared__ float sc[LINES], isc[LINES];  // per-line power-of-two scale and its inverse
   uint8_t* base = (uint8_t*)(((uintptr_t)smraw + 127) & ~(uintptr_t)127);
   float2* xs = (float2*)(base + OFF_X);
   uint8_t* sA = base + OFF_A;
@@ -166,8 +163,9 @@ k_dft512_tc(const float2* in, float2* out, int lines, long long img) {
   const uint32_t tmem = tslot;
   // this warp's tensor-memory lane quarter
   const uint32_t trow = tmem + ((uint32_t)((warp & 3) * 32) << 16);
-  constexpr int pa[6] = {0, 0, 1, 0, 2, 1};
-  constexpr int pb[6] = {0, 1, 0, 2, 0, 1};
+  constexpr int NPROD = 3;  // hi hi, hi lo, lo hi
+  constexpr int pa[NPROD] = {0, 0, 1};
+  constexpr int pb[NPROD] = {0, 1, 0};
   bool alive = true;
   for (int grp = blockIdx.x; grp < groups && alive; grp += gridDim.x) {
     const int L0 = grp * LINES;
@@ -199,10 +197,29 @@ k_dft512_tc(const float2* in, float2* out, int lines, long long img) {
       }
     }
     __syncthreads();
-    // stage-1 A (K-major): job q = 16 r + n2, K = [re x[16 n1 + n2] (n1 < 32) | im ...];
-    // this half: n1 in [16 half, 16 half + 16)
+    {
+      // line r = warp: the power of two that puts its largest component below 2^kScaleExp
+      float mx = 0.f;
+#pragma unroll
+      for (int i = 0; i < N / 32; ++i) {
+        const float2 v = xs[warp * N + lane + 32 * i];
+        mx = fmaxf(mx, fmaxf(fabsf(v.x), fabsf(v.y)));
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+      if (lane == 0) {
+        int ex = 0;
+        if (mx > 0.f) frexpf(mx, &ex);  // mx < 2^ex
+        sc[warp] = ldexpf(1.f, kScaleExp - ex);
+        isc[warp] = ldexpf(1.f, ex - kScaleExp);
+      }
+    }
+    __syncthreads();
+    // stage-1 A (K-major): job q = 16 r + n2, K = [re x[16 n1 + n2] (n1 < 32) | im ...],
+    // scaled by the line's sc; this half: n1 in [16 half, 16 half + 16)
     {
       const int r = q >> 4, n2 = q & 15;
+      const float s1 = sc[r];
 #pragma unroll
       for (int gg = 0; gg < 2; ++gg) {
         const int g = 2 * half + gg;  // n1 in [8 g, 8 g + 8): K groups g (re) and g + 4 (im)
@@ -211,15 +228,8 @@ k_dft512_tc(const float2* in, float2* out, int lines, long long img) {
         for (int h = 0; h < 4; ++h) {
           const float2 xa = xs[r * N + 16 * (8 * g + 2 * h) + n2];
           const float2 xb = xs[r * N + 16 * (8 * g + 2 * h + 1) + n2];
-          uint32_t a[TERMS], c[TERMS];
-          split3t(xa.x, a);
-          split3t(xb.x, c);
-#pragma unroll
-          for (int t = 0; t < TERMS; ++t) wr[t][h] = pack_hi(a[t], c[t]);
-          split3t(xa.y, a);
-          split3t(xb.y, c);
-#pragma unroll
-          for (int t = 0; t < TERMS; ++t) wi[t][h] = pack_hi(a[t], c[t]);
+          split2h(xa.x * s1, xb.x * s1, wr[0][h], wr[1][h]);
+          split2h(xa.y * s1, xb.y * s1, wi[0][h], wi[1][h]);
         }
         const uint32_t o_re = tc::core_offset(q, 8 * g, 64), o_im = tc::core_offset(q, 32 + 8 * g, 64);
 #pragma unroll
@@ -234,9 +244,9 @@ k_dft512_tc(const float2* in, float2* out, int lines, long long img) {
     __syncthreads();
     tc::tc_fence_after();
     if (tid == 0) {
-      const uint32_t idesc = tc::idesc_bf16(128, 64);
+      const uint32_t idesc = idesc_f16(128, 64);
       const uint32_t a0 = tc::smem_u32(sA), b0 = tc::smem_u32(sB1);
-      for (int p = 0; p < 6; ++p)
+      for (int p = 0; p < NPROD; ++p)
         for (int ks = 0; ks < 4; ++ks) {
           const uint64_t ad = tc::smem_desc(a0 + pa[p] * A1_TILE + ks * 256, 128, 64 * 16);
           const uint64_t bd = tc::smem_desc(b0 + pb[p] * B1_TILE + ks * 256, 128, 64 * 16);
@@ -267,17 +277,11 @@ k_dft512_tc(const float2* in, float2* out, int lines, long long img) {
         uint32_t wr[TERMS][4], wi[TERMS][4];
 #pragma unroll
         for (int h = 0; h < 4; ++h) {
-          uint32_t ar[TERMS], br[TERMS], ai[TERMS], bi[TERMS];
           const int ka = 8 * jj + 2 * h, kb = ka + 1;
-          split3t(re[ka] * twr[ka] - im[ka] * twi[ka], ar);
-          split3t(re[ka] * twi[ka] + im[ka] * twr[ka], ai);
-          split3t(re[kb] * twr[kb] - im[kb] * twi[kb], br);
-          split3t(re[kb] * twi[kb] + im[kb] * twr[kb], bi);
-#pragma unroll
-          for (int t = 0; t < TERMS; ++t) {
-            wr[t][h] = pack_hi(ar[t], br[t]);
-            wi[t][h] = pack_hi(ai[t], bi[t]);
-          }
+          split2h(re[ka] * twr[ka] - im[ka] * twi[ka], re[kb] * twr[kb] - im[kb] * twi[kb],
+                  wr[0][h], wr[1][h]);
+          split2h(re[ka] * twi[ka] + im[ka] * twr[ka], re[kb] * twi[kb] + im[kb] * twr[kb],
+                  wi[0][h], wi[1][h]);
         }
         const int mc = 4 * (r & 3) + 2 * half + jj;  // core matrix along M
         const uint32_t o_re = mn_offset(mc, n2), o_im = mn_offset(mc, 16 + n2);
@@ -293,11 +297,11 @@ k_dft512_tc(const float2* in, float2* out, int lines, long long img) {
     __syncthreads();
     tc::tc_fence_after();
     if (tid == 0) {
-      const uint32_t idesc = tc::idesc_bf16(128, 32) | kMajorMN_A;
+      const uint32_t idesc = idesc_f16(128, 32) | kMajorMN_A;
       const uint32_t b0 = tc::smem_u32(sB2);
       for (int m = 0; m < 2; ++m) {
         const uint32_t a0 = tc::smem_u32(sA + m * (TERMS * A2_TILE));
-        for (int p = 0; p < 6; ++p)
+        for (int p = 0; p < NPROD; ++p)
           for (int ks = 0; ks < 2; ++ks) {
             const uint64_t ad = tc::smem_desc(a0 + pa[p] * A2_TILE + ks * 2 * A2_KCORE, A2_KCORE, 128);
             const uint64_t bd = tc::smem_desc(b0 + pb[p] * B2_TILE + ks * 256, 128, 32 * 16);
@@ -321,8 +325,10 @@ k_dft512_tc(const float2* in, float2* out, int lines, long long img) {
       tc::tmem_ld16(trow + 64 + 32 * half, v);
       tc::tmem_ld16(trow + 64 + 32 * half + 16, v + 16);
       const int r = 4 * half + (warp & 3), k1 = lane;
+      const float u = isc[r];
 #pragma unroll
-      for (int k2 = 0; k2 < 16; ++k2) xs[r * N + k1 + 32 * k2] = make_float2(v[k2], v[16 + k2]);
+      for (int k2 = 0; k2 < 16; ++k2)
+        xs[r * N + k1 + 32 * k2] = make_float2(v[k2] * u, v[16 + k2] * u);
     }
     tc::tc_fence_before();
     __syncthreads();
