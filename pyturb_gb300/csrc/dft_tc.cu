@@ -55,6 +55,7 @@ constexpr int OFF_B1 = OFF_A + TERMS * A1_TILE;                    // + 32 KB
 constexpr int OFF_B2 = OFF_B1 + TERMS * B1_TILE;                   // + 16 KB
 constexpr int SMEM = OFF_B2 + TERMS * B2_TILE + 128;               // + 4 KB + alignment
 static_assert(2 * TERMS * A2_TILE <= TERMS * A1_TILE, "stage-2 tiles reuse the stage-1 space");
+static_assert(LINES * N * 8 <= TERMS * A1_TILE, "the output lines are staged in the operand space");
 // The stage-1 operand of a line is scaled by a power of two so that its
 // largest component is below 2^kScaleExp: the fp16 terms then stay in range
 // through the 32-point stage (|Y| <= 32 sqrt(2) 2^9 < 65504).
@@ -68,6 +69,35 @@ __device__ __forceinline__ void split2h(float a, float b, uint32_t& hi, uint32_t
   const __half2 l = __floats2half2_rn(a - hf.x, b - hf.y);
   hi = *reinterpret_cast<const uint32_t*>(&h);
   lo = *reinterpret_cast<const uint32_t*>(&l);
+}
+
+// Issue the asynchronous copies of group grp's 8 lines into xs[r * N + n]:
+// rows are one contiguous 32 KB block (16-byte copies), columns 64 bytes a
+// row index (8-byte copies, one line each).
+template <bool kCols>
+__device__ __forceinline__ void stage_group(const float2* in, long long img, int grp, float2* xs) {
+  const int L0 = grp * LINES;
+  const float2* src = in + (L0 / N) * img + (long long)(L0 % N) * (kCols ? 1 : N);
+  if (!kCols) {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int c = threadIdx.x + THREADS * i;  // 16-byte chunk
+      asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(
+                       (uint32_t)__cvta_generic_to_shared(xs + 2 * c)),
+                   "l"(src + 2 * c)
+                   : "memory");
+    }
+  } else {
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+      const int e = threadIdx.x + THREADS * i, n = e >> 3, r = e & 7;
+      asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(
+                       (uint32_t)__cvta_generic_to_shared(xs + r * N + n)),
+                   "l"(src + (long long)n * N + r)
+                   : "memory");
+    }
+  }
+  asm volatile("cp.async.commit_group;" ::: "memory");
 }
 
 // Instruction descriptor of kind::f16 with fp16 A and B (format 0), fp32 D,
@@ -134,6 +164,7 @@ k_dft512_tc(const float2* in, float2* out, int lines, long long img) {
   uint8_t* base = (uint8_t*)(((uintptr_t)smraw + 127) & ~(uintptr_t)127);
   float2* xs = (float2*)(base + OFF_X);
   uint8_t* sA = base + OFF_A;
+  float2* ob = (float2*)sA;  // the transformed lines, staged in the dead operand space
   uint8_t* sB1 = base + OFF_B1;
   uint8_t* sB2 = base + OFF_B2;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -167,35 +198,15 @@ k_dft512_tc(const float2* in, float2* out, int lines, long long img) {
   constexpr int pa[NPROD] = {0, 0, 1};
   constexpr int pb[NPROD] = {0, 1, 0};
   bool alive = true;
+  // the first group's lines; every later group is prefetched while the one
+  // before it is transformed (xs is free once the stage-1 operand is built)
+  stage_group<kCols>(in, img, blockIdx.x, xs);
   for (int grp = blockIdx.x; grp < groups && alive; grp += gridDim.x) {
     const int L0 = grp * LINES;
     const long long b = L0 / N;
     const int j0 = L0 % N;
-    const float2* src = in + b * img + (long long)j0 * ls;
     float2* dst = out + b * img + (long long)j0 * ls;
-    // stage the 8 lines, 16-byte loads, all 8 of a thread in flight before
-    // their stores: rows along the line, columns across the 8 lines (64 bytes
-    // per element index)
-    {
-      float4 v[8];
-#pragma unroll
-      for (int i = 0; i < 8; ++i) {
-        const int e4 = tid + THREADS * i;
-        v[i] = kCols ? *(const float4*)(src + (e4 >> 2) * N + 2 * (e4 & 3))
-                     : *(const float4*)(src + (e4 >> 8) * N + 2 * (e4 & 255));
-      }
-#pragma unroll
-      for (int i = 0; i < 8; ++i) {
-        const int e4 = tid + THREADS * i;
-        if (kCols) {
-          const int n = e4 >> 2, r = 2 * (e4 & 3);
-          xs[r * N + n] = make_float2(v[i].x, v[i].y);
-          xs[(r + 1) * N + n] = make_float2(v[i].z, v[i].w);
-        } else {
-          *(float4*)(xs + 2 * e4) = v[i];
-        }
-      }
-    }
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
     __syncthreads();
     {
       // line r = warp: the power of two that puts its largest component below 2^kScaleExp
@@ -243,6 +254,7 @@ k_dft512_tc(const float2* in, float2* out, int lines, long long img) {
     tc::tc_fence_before();
     __syncthreads();
     tc::tc_fence_after();
+    if (grp + (int)gridDim.x < groups) stage_group<kCols>(in, img, grp + gridDim.x, xs);
     if (tid == 0) {
       const uint32_t idesc = idesc_f16(128, 64);
       const uint32_t a0 = tc::smem_u32(sA), b0 = tc::smem_u32(sB1);
@@ -328,7 +340,7 @@ k_dft512_tc(const float2* in, float2* out, int lines, long long img) {
       const float u = isc[r];
 #pragma unroll
       for (int k2 = 0; k2 < 16; ++k2)
-        xs[r * N + k1 + 32 * k2] = make_float2(v[k2] * u, v[16 + k2] * u);
+        ob[r * N + k1 + 32 * k2] = make_float2(v[k2] * u, v[16 + k2] * u);
     }
     tc::tc_fence_before();
     __syncthreads();
@@ -337,14 +349,15 @@ k_dft512_tc(const float2* in, float2* out, int lines, long long img) {
       const int e4 = tid + THREADS * i;
       if (kCols) {
         const int n = e4 >> 2, r = 2 * (e4 & 3);
-        const float2 u = xs[r * N + n], w = xs[(r + 1) * N + n];
+        const float2 u = ob[r * N + n], w = ob[(r + 1) * N + n];
         *(float4*)(dst + (e4 >> 2) * N + r) = make_float4(u.x, u.y, w.x, w.y);
       } else {
-        *(float4*)(dst + (e4 >> 8) * N + 2 * (e4 & 255)) = *(const float4*)(xs + 2 * e4);
+        *(float4*)(dst + (e4 >> 8) * N + 2 * (e4 & 255)) = *(const float4*)(ob + 2 * e4);
       }
     }
     __syncthreads();
   }
+  asm volatile("cp.async.wait_group 0;" ::: "memory");
   tc::tc_fence_before();
   __syncthreads();
   if (warp == 0) tc::tmem_dealloc(tmem, 128);
@@ -360,6 +373,8 @@ using namespace pt;
 extern "C" int pt_ifft2_tc(int ns, const float* in, float* out, int batch, void* stream) {
   if (ns != dft::N) return fail(PT_ERR_UNSUPPORTED, "pt_ifft2_tc: the tensor-core DFT is built for ns = 512");
   if (!in || !out || batch < 0) return fail(PT_ERR_ARG, "pt_ifft2_tc: bad arguments");
+  if ((uintptr_t)in % 16 || (uintptr_t)out % 16)
+    return fail(PT_ERR_ARG, "pt_ifft2_tc: in and out must be 16-byte aligned");
   if (batch == 0) return PT_OK;
   if ((long long)batch * dft::N / dft::LINES > 0x7fffffffLL)
     return fail(PT_ERR_ARG, "pt_ifft2_tc: batch too large");
