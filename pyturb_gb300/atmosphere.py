@@ -527,6 +527,50 @@ class Atmosphere:
             gen._generate_into(out, c, self.margin_pix, self.n, scale, accumulate=g > 0)
         return out[0] if squeeze else out
 
+    def sample_host(self, count: int, wavelength: Optional[float] = None, out=None,
+                    chunk: int = 64):
+        """``count`` independent OPDs delivered into host memory.
+
+        Returns a pinned CPU tensor ``(count, n, n)`` (or fills ``out``, which
+        should be pinned for the copies to overlap). Chunks of ``chunk``
+        screens are drawn into two alternating device buffers and copied to the
+        host on a side stream while the next chunk draws; each chunk is one
+        :meth:`sample` call, so the screens are those of repeated
+        ``sample(chunk)`` calls (the last one shorter)."""
+        count, chunk = int(count), int(chunk)
+        if count < 1:
+            raise ValueError("count must be >= 1")
+        if chunk < 1:
+            raise ValueError("chunk must be >= 1")
+        torch = torch_module()
+        if out is None:
+            out = torch.empty((count, self.n, self.n), dtype=torch.float32, pin_memory=True)
+        scale = self._scale(wavelength)
+        gens = self._generators()
+        dev = gens[0]._grid.device
+        k = min(chunk, count)
+        bufs = [torch.empty((k, self.n, self.n), dtype=torch.float32, device=dev)
+                for _ in range(2)]
+        done_copy = [None, None]
+        main = torch.cuda.current_stream(dev)
+        side = torch.cuda.Stream(dev)
+        for c, start in enumerate(range(0, count, k)):
+            m = min(k, count - start)
+            b = c % 2
+            if done_copy[b] is not None:
+                main.wait_event(done_copy[b])
+            for g, gen in enumerate(gens):
+                gen._generate_into(bufs[b], m, self.margin_pix, self.n, scale, accumulate=g > 0)
+            ready = torch.cuda.Event()
+            ready.record(main)
+            with torch.cuda.stream(side):
+                side.wait_event(ready)
+                out[start:start + m].copy_(bufs[b][:m], non_blocking=True)
+                done_copy[b] = torch.cuda.Event()
+                done_copy[b].record(side)
+        side.synchronize()
+        return out
+
     def reset(self) -> "Atmosphere":
         """Back to ``t = 0`` with the initial turbulence (``src/pyturb/atmosphere.py:1221-1243``)."""
         self._t = 0.0

@@ -159,3 +159,22 @@ def test_sample_config2_vs_oracle():
                               l.L0) for l in lys], host_noise=np.random.default_rng, **kw)
     o = oracle.OracleAtmosphere(lys, **kw)
     assert cases.rel_l2(to_numpy(a.sample(6)), o.sample(6)) < TOL
+
+
+def test_sample_host_equals_repeated_sample():
+    """sample_host(count, chunk) delivers the screens of repeated sample(chunk)
+    calls into pinned host memory (two L0 groups, a short last chunk)."""
+    import torch
+
+    import pyturb_gb300 as G
+
+    lys = _config2_layers(3)
+    lys[-1] = cases.layer_objs([(20000, 0.03, 12.0, 40.0, 50.0)])[0]  # a second L0 group
+    kw = dict(r0=0.15, zenith_angle=10.0, diameter=4.0, n=128, subharmonics=2, seed=21)
+    mk = lambda: G.Atmosphere([G.Layer(l.altitude, l.cn2_fraction, l.wind_speed,
+                                       l.wind_direction, l.L0) for l in lys], **kw)
+    got = mk().sample_host(22, chunk=8)
+    assert got.device.type == "cpu" and got.is_pinned() and tuple(got.shape) == (22, 128, 128)
+    a = mk()
+    want = torch.cat([a.sample(8).cpu(), a.sample(8).cpu(), a.sample(6).cpu()])
+    assert torch.equal(got, want)
