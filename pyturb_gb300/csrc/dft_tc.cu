@@ -46,11 +46,15 @@ constexpr int A2_TILE = 128 * 32 * 2;   // one stage-2 A tile, one term
 constexpr int B2_TILE = 32 * 32 * 2;    // stage-2 B (the 16-point DFT block matrix)
 constexpr int TERMS = 2;
 // shared memory: staged lines (fp32 complex) | A (stage 1, reused by stage 2) |
-// B1 | B2, 84 KB, two CTAs an SM (the twiddles live in registers).
+// B1 | B2, 92 KB, two CTAs an SM (the twiddles live in registers).
 // Unswizzled operands need 16-byte alignment; the base is rounded up to 128
 // bytes.
+// The staged lines: rows as xs[r * N + n]; columns as xs[n * XCS + r], so
+// that a row index's 8 lines (64 bytes in memory) arrive in 16-byte copies
+// and the stage-1 reads stay free of bank conflicts (a stride of 10 float2).
+constexpr int XCS = 10;
 constexpr int OFF_X = 0;
-constexpr int OFF_A = OFF_X + LINES * N * 8;                       // 32 KB
+constexpr int OFF_A = OFF_X + N * XCS * 8;                         // 40 KB
 constexpr int OFF_B1 = OFF_A + TERMS * A1_TILE;                    // + 32 KB
 constexpr int OFF_B2 = OFF_B1 + TERMS * B1_TILE;                   // + 16 KB
 constexpr int SMEM = OFF_B2 + TERMS * B2_TILE + 128;               // + 4 KB + alignment
@@ -71,9 +75,12 @@ __device__ __forceinline__ void split2h(float a, float b, uint32_t& hi, uint32_t
   lo = *reinterpret_cast<const uint32_t*>(&l);
 }
 
-// Issue the asynchronous copies of group grp's 8 lines into xs[r * N + n]:
-// rows are one contiguous 32 KB block (16-byte copies), columns 64 bytes a
-// row index (8-byte copies, one line each).
+// Element n of line r of the staged group.
+template <bool kCols>
+__device__ __forceinline__ int xat(int r, int n) { return kCols ? n * XCS + r : r * N + n; }
+
+// Issue the asynchronous copies of group grp's 8 lines into xs: rows are one
+// contiguous 32 KB block, columns 64 bytes a row index; 16-byte copies.
 template <bool kCols>
 __device__ __forceinline__ void stage_group(const float2* in, long long img, int grp, float2* xs) {
   const int L0 = grp * LINES;
@@ -89,10 +96,10 @@ __device__ __forceinline__ void stage_group(const float2* in, long long img, int
     }
   } else {
 #pragma unroll
-    for (int i = 0; i < 16; ++i) {
-      const int e = threadIdx.x + THREADS * i, n = e >> 3, r = e & 7;
-      asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(
-                       (uint32_t)__cvta_generic_to_shared(xs + r * N + n)),
+    for (int i = 0; i < 8; ++i) {
+      const int c = threadIdx.x + THREADS * i, n = c >> 2, r = 2 * (c & 3);  // lines r, r + 1
+      asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(
+                       (uint32_t)__cvta_generic_to_shared(xs + n * XCS + r)),
                    "l"(src + (long long)n * N + r)
                    : "memory");
     }
@@ -213,7 +220,7 @@ k_dft512_tc(const float2* in, float2* out, int lines, long long img) {
       float mx = 0.f;
 #pragma unroll
       for (int i = 0; i < N / 32; ++i) {
-        const float2 v = xs[warp * N + lane + 32 * i];
+        const float2 v = xs[xat<kCols>(warp, lane + 32 * i)];
         mx = fmaxf(mx, fmaxf(fabsf(v.x), fabsf(v.y)));
       }
 #pragma unroll
@@ -237,8 +244,8 @@ k_dft512_tc(const float2* in, float2* out, int lines, long long img) {
         uint32_t wr[TERMS][4], wi[TERMS][4];
 #pragma unroll
         for (int h = 0; h < 4; ++h) {
-          const float2 xa = xs[r * N + 16 * (8 * g + 2 * h) + n2];
-          const float2 xb = xs[r * N + 16 * (8 * g + 2 * h + 1) + n2];
+          const float2 xa = xs[xat<kCols>(r, 16 * (8 * g + 2 * h) + n2)];
+          const float2 xb = xs[xat<kCols>(r, 16 * (8 * g + 2 * h + 1) + n2)];
           split2h(xa.x * s1, xb.x * s1, wr[0][h], wr[1][h]);
           split2h(xa.y * s1, xb.y * s1, wi[0][h], wi[1][h]);
         }
