@@ -249,9 +249,10 @@ def bench_tc_dft(torch, batch: int = 96, reps: int = 20) -> dict:
                    "of two-term fp16 splits of power-of-two scaled lines (three products, fp32 "
                    "accumulation in tensor memory), twiddles in registers; persistent "
                    "256-thread CTAs, two per SM, the next 8-line group prefetched with "
-                   "cp.async. "
-                   "fp32_fft = the register FFT under generate / sample / frames. The "
-                   "tc bound counts the transform alone (no spectrum fill, no pair "
+                   "16-byte cp.async (column groups staged transposed). "
+                   "fp32_fft = the register FFT under generate / sample / frames, where "
+                   "it is fused with the noise, recurrence and subharmonic work. The tc "
+                   "bound counts the transform alone (no spectrum fill, no pair "
                    "extraction): a whole tc-form pipeline is slower than that")
     return res
 
