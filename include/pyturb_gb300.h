@@ -48,10 +48,11 @@ int pt_prof_enable(int on);
 int pt_prof_report(char* buf, size_t len);
 
 /* Failure detection (no reference counterpart). Kernels that wait on an
- * mbarrier (the TMA-fed column pass) bound every wait; a wait that runs out
- * sets bit 1 of a device error word and the kernel finishes instead of
- * hanging. pt_device_error synchronises the device and reads (and, with
- * clear != 0, resets) that word. pt_selftest_wait_timeout runs one wait that
+ * mbarrier (the TMA-fed column pass, the tensor-core extrusion products and
+ * the tensor-core DFT) bound every wait; a wait that runs out sets bit 1 of a
+ * device error word and the kernel finishes instead of hanging.
+ * pt_device_error synchronises the device and reads (and, with clear != 0,
+ * resets) those words, combined. pt_selftest_wait_timeout runs one wait that
  * nothing completes, with `limit` polls (1..2^24), and reports in *timed_out
  * whether it ran out as designed. */
 int pt_device_error(int* out, int clear);

@@ -370,6 +370,21 @@ k_dft512_tc(const float2* in, float2* out, int lines, long long img) {
   if (warp == 0) tc::tmem_dealloc(tmem, 128);
 }
 
+// The tensor-core DFT's error word (bounded waits that ran out), for
+// pt_device_error.
+int dft_device_error(int* out, int clear) {
+  int v = 0;
+  if (int rc = check_cuda(cudaMemcpyFromSymbol(&v, g_dft_error, sizeof(int)), "dft error word"))
+    return rc;
+  if (clear) {
+    const int z = 0;
+    if (int rc = check_cuda(cudaMemcpyToSymbol(g_dft_error, &z, sizeof(int)), "dft error word"))
+      return rc;
+  }
+  *out = v;
+  return PT_OK;
+}
+
 }  // namespace pt
 
 using namespace pt;

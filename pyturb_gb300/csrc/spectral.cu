@@ -1161,6 +1161,7 @@ using namespace pt;
 // Device error word set by bounded waits that ran out (0 = none).
 namespace pt {
 int tc_device_error(int* out, int clear);
+int dft_device_error(int* out, int clear);
 }
 
 extern "C" int pt_device_error(int* out, int clear) {
@@ -1175,9 +1176,10 @@ extern "C" int pt_device_error(int* out, int clear) {
                             "pt_device_error: clear"))
       return rc;
   }
-  int tcw = 0;  // the tensor-core kernels' own error word (separate module)
+  int tcw = 0, dftw = 0;  // the tensor-core kernels' own error words (separate modules)
   if (int rc = tc_device_error(&tcw, clear)) return rc;
-  *out |= tcw;
+  if (int rc = dft_device_error(&dftw, clear)) return rc;
+  *out |= tcw | dftw;
   return PT_OK;
 }
 

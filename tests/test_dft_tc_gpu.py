@@ -52,6 +52,12 @@ def test_tc_dft_matches_float64_and_the_fp32_fft():
         e_fft = _rel(_host(ref), exact)
         print(f"relative L2 vs float64: tensor-core DFT {e_tc:.2e}, FP32 FFT {e_fft:.2e}")
         assert e_tc < TOL
+    # every bounded barrier wait of the products completed
+    import ctypes as C
+
+    err = C.c_int(-1)
+    _lib.call("pt_device_error", C.byref(err), 1)
+    assert err.value == 0
 
 
 def test_tc_dft_refuses_other_sizes():
