@@ -77,6 +77,10 @@ k_rows_reg(const float2* __restrict__ tw, const float2* __restrict__ in, int gen
   const int v = threadIdx.x / T, j = threadIdx.x % T;
   const RowLayout s{sm + N + v * fft_padded(N)};
   const RowLayout s2{sm + N + (NV + v) * fft_padded(N)};  // second exchange vector
+  // a column pass launched as a programmatic dependent may start its
+  // prologue once every CTA of this grid is running (it waits for this
+  // grid's completion before it reads any result)
+  asm volatile("griddepcontrol.launch_dependents;");
   load_stage_tw<N>(stw, tw);
   const int kx = blockIdx.x * NV + v;
   const int img = blockIdx.y;
@@ -168,6 +172,9 @@ k_pair_cols_reg(const float2* __restrict__ tw, const float2* __restrict__ work, 
   const ColLayout<C> s{buf + c};
   const ColLayout<C> s2{buf + N * C + c};
   load_stage_tw<N>(stw, tw);
+  // launched as a programmatic dependent of the row pass: everything below
+  // reads the row pass's results (a no-op in an ordinary launch)
+  asm volatile("griddepcontrol.wait;" ::: "memory");
   const int y = blockIdx.x * C + c;
   const int pl = blockIdx.y;
   const int pair = pair0 + pl;
@@ -330,6 +337,9 @@ k_frame_rows_uniform_reg(const float2* __restrict__ tw, const float2* __restrict
   // once here instead of by one thread inside the pair loop (which stalled
   // every batch's barrier on a global load)
   __shared__ float2 hcol[kAnchor];
+  // the column pass after it is a programmatic dependent (it waits for this
+  // grid's completion before reading the rows)
+  asm volatile("griddepcontrol.launch_dependents;");
   load_stage_tw<N>(stw, tw);
   const int kx = blockIdx.x;
   const int fbeg = blockIdx.y * kAnchor;

@@ -1017,9 +1017,21 @@ static int pair_cols_reg_t(const pt_grid* g, const float2* work, int npair, int 
                       sizeof(float2);
   if (int rc = set_smem(k_pair_cols_reg<N>, smem, "k_pair_cols_reg")) return rc;
   ProfScope ps("k_pair_cols", s);
-  k_pair_cols_reg<N><<<dim3((N + Cfg::C - 1) / Cfg::C, npair), Cfg::THREADS, smem, s>>>(
-      g->tw, work, pair0, st);
-  return PT_OK;
+  // a programmatic dependent of the row pass before it on the stream: its
+  // CTAs stage their twiddles while the row pass's last wave runs, then wait
+  // (griddepcontrol.wait) for the row pass to complete
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((N + Cfg::C - 1) / Cfg::C, npair);
+  cfg.blockDim = dim3(Cfg::THREADS);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return check_cuda(cudaLaunchKernelEx(&cfg, k_pair_cols_reg<N>, g->tw, work, pair0, st),
+                    "k_pair_cols_reg");
 }
 
 // ---- TMA-fed column pass (N = 256, 512, 1024)
