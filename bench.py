@@ -6,7 +6,10 @@ Workload (one step): ``Atmosphere`` with 9 layers at h = [0, 0.5, 1, 2, 4, 8,
 0.03], winds U[5, 30] m/s with seeded directions, n = 512, D = 8 m,
 r0 = 0.157 m, L0 = 25 m, zenith 30 deg, 3 subharmonic levels, dt = 1 ms:
 2000 frames rendered into HBM. Secondary: ``Atmosphere.sample(64)`` at 512^2
-(MC screens/s). Synthetic seeded inputs throughout.
+(MC screens/s), the metric's tensor-core form of the 512^2 transform beside
+the FP32 FFT (``dft_512_tc_vs_fp32``), config 1 generate, config 3
+extrusion, config 4 differentiable readout and config 5 ragged ensembles.
+Synthetic seeded inputs throughout.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
