@@ -398,7 +398,7 @@ extern "C" int pt_ifft2_tc(int ns, const float* in, float* out, int batch, void*
   if ((uintptr_t)in % 16 || (uintptr_t)out % 16)
     return fail(PT_ERR_ARG, "pt_ifft2_tc: in and out must be 16-byte aligned");
   if (batch == 0) return PT_OK;
-  if ((long long)batch * dft::N / dft::LINES > 0x7fffffffLL)
+  if ((long long)batch * dft::N > 0x7fffffffLL)
     return fail(PT_ERR_ARG, "pt_ifft2_tc: batch too large");
   cudaStream_t s = (cudaStream_t)stream;
   static int resident = 0;  // CTAs of k_dft512_tc the device holds at once
