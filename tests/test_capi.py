@@ -101,3 +101,15 @@ def test_workspace_queries_are_pure():
     assert nbytes >= (3 * 100 + 2) ** 2 * 8
     assert lib.pt_aw_workspace_bytes(100, 2, None) >= (3 * 100) ** 2 * 8
     assert lib.pt_aw_workspace_bytes(100, 2, C.byref(_lib.sparse_stencil([(1, 10)]))) == 0
+
+
+def test_tensor_core_dft_argument_errors():
+    """pt_ifft2_tc rejects other sizes, misaligned buffers and oversized batches
+    before any device work."""
+    ok = 1 << 20  # a 16-byte aligned stand-in address, never dereferenced
+    assert _status("pt_ifft2_tc", 256, ok, ok, 1, None) == _lib.PT_ERR_UNSUPPORTED
+    assert _status("pt_ifft2_tc", 512, ok + 8, ok, 1, None) == _lib.PT_ERR_ARG
+    assert "aligned" in _lib.last_error()
+    assert _status("pt_ifft2_tc", 512, ok, ok, 5_000_000, None) == _lib.PT_ERR_ARG
+    assert _status("pt_ifft2_tc", 512, ok, ok, -1, None) == _lib.PT_ERR_ARG
+    assert _status("pt_ifft2_tc", 512, ok, ok, 0, None) == 0
