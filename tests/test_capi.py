@@ -113,3 +113,14 @@ def test_tensor_core_dft_argument_errors():
     assert _status("pt_ifft2_tc", 512, ok, ok, 5_000_000, None) == _lib.PT_ERR_ARG
     assert _status("pt_ifft2_tc", 512, ok, ok, -1, None) == _lib.PT_ERR_ARG
     assert _status("pt_ifft2_tc", 512, ok, ok, 0, None) == 0
+
+
+def test_adjoint_argument_errors():
+    ok = 1 << 20
+    assert _status("pt_synth_adj_sh", None, 1, 0, 8, ok, ok, None) == _lib.PT_ERR_ARG
+    assert "grid is NULL" in _lib.last_error()
+    mag = (C.c_double * 1)(1.0)
+    # pupil footprint wider than the screen
+    assert _status("pt_lr_grad_screens", 1, 1, 16, 1, 1, 32, mag, ok, ok, ok, 0, ok,
+                   None) == _lib.PT_ERR_ARG
+    assert _status("pt_synth_adj_spectra", 0, 1, 1, ok, ok, ok, 1, ok, None) == _lib.PT_ERR_ARG
