@@ -140,3 +140,39 @@ def test_subharmonic_vjp_matches_central_differences():
             fd = (val(c_=cp) - val(c_=cm)) / (2 * eps)
             want = gc[idx].real if part == "re" else gc[idx].imag
             assert fd == pytest.approx(want, rel=1e-6, abs=1e-7)
+
+
+def test_subharmonic_vjp_matches_torch_autograd():
+    torch = pytest.importorskip("torch")
+    S, w, sx, sy, dx, crop, n_out, scale, g = case(seed=12, L=2, ns=16, n_out=11)
+    coef, freqs = sh_case(L=2, ns=16)
+    L, ns, _ = S.shape
+    tS = torch.tensor(S, requires_grad=True)
+    tw = torch.tensor(w, requires_grad=True)
+    tsx = torch.tensor(sx, requires_grad=True)
+    tsy = torch.tensor(sy, requires_grad=True)
+    tc = torch.tensor(coef, requires_grad=True)
+    f = torch.tensor(np.fft.fftfreq(ns, dx))
+    fp = torch.tensor(freqs)
+    px = torch.exp(2j * np.pi * f[None, None, :] * tsx[..., None])
+    py = torch.exp(2j * np.pi * f[None, None, :] * tsy[..., None])
+    X = torch.einsum("l,lij,fli,flj->fij", tw.to(torch.complex128), tS, px, py)
+    y = torch.fft.ifft2(X).real * ns * ns
+    x = torch.tensor((np.arange(ns) - ns / 2.0) * dx)
+    basis = torch.exp(2j * np.pi * fp[:, :, None] * x[None, None, :])           # (P, 3, ns)
+    ex = torch.exp(2j * np.pi * tsx[:, :, None, None] * fp[None, None])          # (F, L, P, 3)
+    ey = torch.exp(2j * np.pi * tsy[:, :, None, None] * fp[None, None])
+    C = torch.einsum("l,plij,flpi,flpj->fpij", tw.to(torch.complex128), tc, ex, ey)
+    low = torch.einsum("pix,fpij,pjy->fxy", basis, C, basis).real
+    y = y + low - low.mean(dim=(1, 2), keepdim=True)
+    y = scale * y[:, crop:crop + n_out, crop:crop + n_out]
+    (y * torch.tensor(g)).sum().backward()
+    gS, gw, gsx, gsy, gc = sd.synth_vjp(S, w, sx, sy, dx, crop, n_out, scale, g, sh=(coef, freqs))
+    np.testing.assert_allclose(y.detach().numpy(),
+                               sd.synth_frames(S, w, sx, sy, dx, crop, n_out, scale,
+                                               sh=(coef, freqs)), rtol=1e-11, atol=1e-10)
+    np.testing.assert_allclose(tS.grad.numpy(), gS, rtol=1e-10, atol=1e-9)
+    np.testing.assert_allclose(tw.grad.numpy(), gw, rtol=1e-10)
+    np.testing.assert_allclose(tsx.grad.numpy(), gsx, rtol=1e-9, atol=1e-8)
+    np.testing.assert_allclose(tsy.grad.numpy(), gsy, rtol=1e-9, atol=1e-8)
+    np.testing.assert_allclose(tc.grad.numpy(), gc, rtol=1e-10, atol=1e-10)
